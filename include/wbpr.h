@@ -1,0 +1,255 @@
+/*
+ * wbpr.h -- C ABI of the GB300 push-relabel maximum-flow library (libwbpr.so).
+ *
+ * This is the only surface through which host code reaches CUDA.  Every
+ * signature uses plain C types: pointers, sizes and the structs below.  The
+ * library owns all device memory it allocates; inputs are copied at
+ * create time; no entry point calls exit().  One handle per host thread.
+ *
+ * Reference interfaces replaced (paths inside the WBPR project):
+ *   - preflow(...)        maxflow-cuda/include/parallel_graph.cuh:44-46,
+ *                         maxflow-cuda/src/preflow.cu:3-31
+ *   - push_relabel(...)   maxflow-cuda/include/parallel_graph.cuh:47-54,
+ *                         maxflow-cuda/src/push_relabel.cu:35-221
+ *   - global_relabel / global_relabel_gpu
+ *                         maxflow-cuda/src/global_relabel.cu:4-178,
+ *                         maxflow-bcsr/src/global_relabel_gpu.cu:4-189
+ *   - CSRGraph readers    maxflow-cuda/src/graph.cpp:28-67,151-214,219-233,292-314
+ *   - ResidualGraph::buildFromCSRGraph
+ *                         maxflow-cuda/src/graph.cpp:317-402 (RCSR),
+ *                         maxflow-bcsr/src/graph.cpp:317-360 (BCSR),
+ *                         maxflow-bcsr2/src/graph.cpp:326-362 (BCSR2)
+ */
+#ifndef WBPR_H_
+#define WBPR_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WBPR_ABI_VERSION 1
+
+typedef enum wbpr_status {
+  WBPR_OK = 0,
+  WBPR_ERR_INVALID_ARG = 1,    /* bad pointer, vertex id, size or enum      */
+  WBPR_ERR_CUDA = 2,           /* a CUDA runtime call failed                */
+  WBPR_ERR_NO_CONVERGENCE = 3, /* round / time budget exhausted             */
+  WBPR_ERR_OVERFLOW = 4,       /* int32 excess or arc index would overflow  */
+  WBPR_ERR_VERIFY = 5,         /* device invariant check failed             */
+  WBPR_ERR_IO = 6,             /* file missing, truncated or malformed      */
+  WBPR_ERR_NO_DEVICE = 7,      /* no CUDA device visible                    */
+  WBPR_ERR_TIMEOUT = 8         /* a bounded grid-wide wait gave up          */
+} wbpr_status;
+
+/* Residual-graph layout kept on the device. */
+typedef enum wbpr_layout {
+  WBPR_LAYOUT_RCSR = 0,  /* forward CSR + reversed CSR with flow index        */
+  WBPR_LAYOUT_BCSR = 1,  /* one row per vertex holding forward and reverse    */
+                         /* arcs; 16-byte arc record {dst, cf | rev, cap}     */
+  WBPR_LAYOUT_BCSR2 = 2  /* accepted alias of BCSR: the reference's BCSR2     */
+                         /* {cf, rev} pair is the same record                 */
+} wbpr_layout;
+
+typedef enum wbpr_algo {
+  WBPR_ALGO_TC = 0, /* thread-centric: one thread discharges one vertex       */
+  WBPR_ALGO_VC = 1  /* vertex-centric: one 8/16/32-lane tile per vertex       */
+} wbpr_algo;
+
+/* Input graph in CSR form (the reference's CSRGraph, graph.h:28-58).
+ * Arc i of vertex u is offsets[u] <= i < offsets[u+1], head destinations[i],
+ * capacity capacities[i] >= 0.  capacities may be NULL (all capacities 1). */
+typedef struct wbpr_csr {
+  int32_t num_nodes;
+  int64_t num_edges;
+  const int32_t* offsets;      /* num_nodes + 1 */
+  const int32_t* destinations; /* num_edges     */
+  const int32_t* capacities;   /* num_edges or NULL */
+  int32_t source;              /* -1 if the file did not name one */
+  int32_t sink;
+} wbpr_csr;
+
+/* Host-owned CSR returned by the readers and generators; free with
+ * wbpr_host_csr_free. */
+typedef struct wbpr_host_csr {
+  int32_t num_nodes;
+  int64_t num_edges;
+  int64_t num_edges_declared; /* value of the file header (DIMACS p / SNAP #) */
+  int32_t* offsets;
+  int32_t* destinations;
+  int32_t* capacities;
+  int32_t source;
+  int32_t sink;
+} wbpr_host_csr;
+
+typedef struct wbpr_tuning {
+  int32_t tile;          /* VC tile width: 8, 16 or 32 (0 = auto)                 */
+  int32_t block;         /* threads per block: 128..1024, multiple of 32 (0=auto) */
+  int32_t heavy_degree;  /* rows longer than this are discharged by a whole      */
+                         /* block (0 = auto)                                      */
+  int32_t blocks_per_sm; /* resident blocks per SM for the persistent grid (0=max) */
+  double gr_alpha;       /* global relabel after alpha*(n + arcs) units of work   */
+  int64_t max_rounds;    /* push/relabel round budget (0 = unlimited)             */
+  double max_ms;         /* wall-clock budget of one solve in ms (0 = 600000)     */
+  int32_t verify;        /* 1: run the device certificate check after the solve  */
+  int32_t reserved;
+} wbpr_tuning;
+
+typedef struct wbpr_result {
+  int64_t flow;            /* maximum-flow value: excess of the sink         */
+  float solve_ms;          /* device time, reset + preflow + solve           */
+  float kernel_ms;         /* push/relabel rounds only (reference's timer)   */
+  float gr_ms;             /* global relabel BFS time                        */
+  uint64_t arcs_scanned;   /* residual arcs read by discharges               */
+  uint64_t pushes;         /* arcs that carried a push                       */
+  uint64_t relabels;       /* vertex relabels                                */
+  uint64_t vertex_visits;  /* active-vertex discharges                       */
+  uint64_t bfs_arcs;       /* arcs inspected by global relabels              */
+  uint64_t bfs_vertices;   /* vertex checks by global relabels               */
+  uint64_t alg_bytes;      /* algorithmic bytes from the counters above      */
+  int32_t rounds;          /* push/relabel supersteps                        */
+  int32_t global_relabels; /* BFS passes                                     */
+  int32_t stranded;        /* vertices left with excess unable to reach t    */
+  float launch_ms;         /* CUDA-event time of the persistent solver kernel */
+} wbpr_result;
+
+typedef struct wbpr_verify_report {
+  int32_t ok;                 /* 1 when every check passed                 */
+  int32_t capacity_violations;/* arcs with cf < 0 or cf > cap + cap(rev)   */
+  int32_t conservation_violations; /* vertices whose excess != in - out    */
+  int32_t source_reaches_sink;/* 1 if a residual s->t path exists          */
+  int32_t excess_reaches_sink;/* vertices with excess that reach t         */
+  int32_t reserved;
+  int64_t cut_value;          /* capacity of the sink-side residual cut    */
+  int64_t flow_value;         /* excess of the sink                        */
+} wbpr_verify_report;
+
+typedef struct wbpr_graph wbpr_graph;
+
+/* ---- status / version ---------------------------------------------------- */
+const char* wbpr_status_str(wbpr_status s);
+int32_t wbpr_abi_version(void);
+void wbpr_default_tuning(wbpr_tuning* t);
+/* Number of CUDA devices (0 when none); never fails. */
+int32_t wbpr_device_count(void);
+/* Text of the last CUDA failure seen by this host thread ("" if none). */
+const char* wbpr_last_error(void);
+
+/* ---- graph readers (replace CSRGraph::build* / loadFromBinary) ----------- */
+/* -v 0: SNAP text, "# Nodes: N Edges: M" header, capacity 1 (graph.cpp:28-67) */
+wbpr_status wbpr_read_snap_txt(const char* path, wbpr_host_csr** out);
+/* -v 1: SNAP binary [n][m][m_processed][dst...][offsets...] (graph.cpp:292-314) */
+wbpr_status wbpr_read_snap_bin(const char* path, wbpr_host_csr** out);
+/* -v 2: DIMACS max-flow "p max / n s|t / a u v c", 1-based (graph.cpp:151-214) */
+wbpr_status wbpr_read_dimacs(const char* path, wbpr_host_csr** out);
+/* Writers: SNAP binary (graph.cpp:219-233) and DIMACS text. */
+wbpr_status wbpr_write_snap_bin(const char* path, const wbpr_csr* g);
+wbpr_status wbpr_write_dimacs(const char* path, const wbpr_csr* g);
+/* Copy a caller CSR into a library-owned one. */
+wbpr_status wbpr_host_csr_copy(const wbpr_csr* in, wbpr_host_csr** out);
+void wbpr_host_csr_free(wbpr_host_csr* g);
+
+/* ---- seeded synthetic generators (integer arithmetic, same bits on x86 and
+ *      aarch64) ---------------------------------------------------------- */
+/* GENRMF-shaped frames: b frames of a x a grids; in-frame 4-neighbour arcs of
+ * capacity c2*a*a, one inter-frame arc per vertex to a seeded permutation of
+ * the next frame with capacity uniform in [c1, c2]; s = 0, t = n - 1. */
+wbpr_status wbpr_gen_genrmf(int32_t a, int32_t b, int32_t c1, int32_t c2,
+                            uint64_t seed, wbpr_host_csr** out);
+/* R-MAT scale/edge-factor with quadrant probabilities a,b,c (d = rest),
+ * self loops and duplicates removed, capacities uniform in [cap_lo, cap_hi];
+ * s = max out-degree vertex, t = max in-degree vertex (lowest id on ties). */
+wbpr_status wbpr_gen_rmat(int32_t scale, int32_t edge_factor, double a,
+                          double b, double c, int32_t cap_lo, int32_t cap_hi,
+                          uint64_t seed, wbpr_host_csr** out);
+/* Unit-capacity bipartite matching network: s=0, left 1..L, right L+1..L+R,
+ * t=L+R+1; left degrees ~ Zipf(zipf_s) clipped to [1, dmax]. */
+wbpr_status wbpr_gen_bipartite(int32_t left, int32_t right, double zipf_s,
+                               int32_t dmax, uint64_t seed,
+                               wbpr_host_csr** out);
+/* Layered network: s=0, `layers` layers of `width` vertices, each vertex has
+ * deg_lo..deg_hi arcs into the next layer, t = n-1; caps in [cap_lo, cap_hi]. */
+wbpr_status wbpr_gen_layered(int32_t layers, int32_t width, int32_t deg_lo,
+                             int32_t deg_hi, int32_t cap_lo, int32_t cap_hi,
+                             uint64_t seed, wbpr_host_csr** out);
+/* Vision graph-cut grid w x h, 4-connected n-links, t-links; s = w*h,
+ * t = w*h + 1 (smooth seeded field, see the generator for the formulas). */
+wbpr_status wbpr_gen_grid(int32_t w, int32_t h, uint64_t seed,
+                          wbpr_host_csr** out);
+
+/* ---- residual-graph builders (exact reverse pairing, O(n + m)) ----------- */
+/* RCSR (maxflow-cuda/src/graph.cpp:317-402): roffsets[n+1], rdestinations[m],
+ * flow_index[m] (reverse entry -> forward arc id).  Caller-allocated. */
+wbpr_status wbpr_build_rcsr(const wbpr_csr* g, int32_t* roffsets,
+                            int32_t* rdestinations, int32_t* flow_index);
+/* BCSR (maxflow-bcsr/src/graph.cpp:317-360): every input arc gets its own
+ * reverse twin.  offsets[n+1], destinations[2m], capacities[2m] (0 for a
+ * twin), backward_idx[2m].  Caller-allocated. */
+wbpr_status wbpr_build_bcsr(const wbpr_csr* g, int32_t* offsets,
+                            int32_t* destinations, int32_t* capacities,
+                            int32_t* backward_idx);
+/* BCSR2 (maxflow-bcsr2/src/graph.cpp:326-362): as BCSR, with the interleaved
+ * flows[2a] = residual, flows[2a+1] = reverse arc id.  flows is 4m ints. */
+wbpr_status wbpr_build_bcsr2(const wbpr_csr* g, int32_t* offsets,
+                             int32_t* destinations, int32_t* flows);
+
+/* ---- device graph and solve --------------------------------------------- */
+wbpr_status wbpr_graph_create(const wbpr_csr* g, wbpr_layout layout,
+                              wbpr_graph** out);
+wbpr_status wbpr_graph_destroy(wbpr_graph* g);
+/* Bytes of device memory held by the handle. */
+int64_t wbpr_graph_device_bytes(const wbpr_graph* g);
+/* Fresh solve: reset residuals to capacities, preflow from s, push/relabel to
+ * a maximum preflow.  Result flow = excess(t). s/t = -1 use the graph's. */
+wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo,
+                       const wbpr_tuning* tuning, wbpr_result* out);
+/* Read back the state after a solve (host buffers, any may be NULL):
+ * height[n], excess[n], and per input arc flow = cap - residual (m). */
+wbpr_status wbpr_read_state(wbpr_graph* g, int32_t* height, int32_t* excess,
+                            int32_t* arc_flow);
+/* Certificate check on the device: capacities, conservation, and that no
+ * residual path leads from s or from any excess vertex to t (so the value is
+ * maximal), and cut value == flow value. */
+wbpr_status wbpr_verify(wbpr_graph* g, wbpr_verify_report* rep);
+/* Min-cut adjoint: per input arc int8 indicator g[e] of the exact
+ * (super)gradient d maxflow / d cap(e).  side 0: sink-side cut (vertices that
+ * can reach t form T, g = [u not in T and v in T]); side 1: source-side cut
+ * (S = vertices reachable from s once the stranded excess is returned,
+ * g = [u in S and v not in S]).  `indicator` is a host buffer of m bytes. */
+wbpr_status wbpr_mincut_adjoint(wbpr_graph* g, int32_t side, int8_t* indicator,
+                                float* adjoint_ms);
+
+/* ---- drop-ins for the reference host functions (RCSR arrays, in place) --- */
+/* Same arguments and meaning as preflow() in maxflow-cuda/src/preflow.cu:3-31,
+ * except that excess is accumulated (+=) so parallel source arcs are not lost.
+ * Returns a wbpr_status. */
+int32_t wbpr_rcsr_preflow(int32_t V, int32_t source, int32_t sink,
+                          int32_t* cpu_height, int32_t* cpu_excess_flow,
+                          const int32_t* offsets, const int32_t* destinations,
+                          const int32_t* capacities, int32_t* forward_flows,
+                          int32_t* backward_flows, const int32_t* roffsets,
+                          const int32_t* rdestinations, const int32_t* flow_idx,
+                          int32_t* Excess_total);
+/* Same arguments and in-place contract as push_relabel() in
+ * maxflow-cuda/src/push_relabel.cu:35-221 (host arrays only: the library owns
+ * the device copies).  On return cpu_height, cpu_excess_flow, cpu_fflows and
+ * cpu_bflows hold the final state, cpu_excess_flow[sink] is the maximum flow,
+ * *Excess_total = e(s) + e(t), and *kernel_ms (may be NULL) the push/relabel
+ * kernel time.  Returns a wbpr_status. */
+int32_t wbpr_rcsr_push_relabel(int32_t algo_type, int32_t V, int32_t E,
+                               int32_t source, int32_t sink,
+                               int32_t* cpu_height, int32_t* cpu_excess_flow,
+                               const int32_t* cpu_offsets,
+                               const int32_t* cpu_destinations,
+                               const int32_t* cpu_capacities,
+                               int32_t* cpu_fflows, int32_t* cpu_bflows,
+                               const int32_t* cpu_roffsets,
+                               const int32_t* cpu_rdestinations,
+                               const int32_t* cpu_flow_idx,
+                               int32_t* Excess_total, float* kernel_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WBPR_H_ */

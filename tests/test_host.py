@@ -1,0 +1,192 @@
+"""Host logic of libwbpr without a GPU: ABI surface, readers and writers,
+residual builders (exact reverse pairing), seeded generators, CLI errors."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import wbpr_gb300 as W
+from wbpr_gb300 import build as wb
+from conftest import ROOT, graph_of
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "wbpr.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(wbpr_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = W.lib()
+    declared = header_functions()
+    assert set(declared) == set(W.EXPORTED)
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert lib.wbpr_abi_version() == 1
+
+
+def test_status_strings():
+    for s in range(9):
+        assert W.status_str(s)
+    assert W.status_str(0) == "ok"
+
+
+def test_no_device_is_reported_not_faked(has_gpu):
+    if has_gpu:
+        pytest.skip("host has a GPU")
+    g = W.gen_genrmf(3, 3, 1, 10, 0)
+    with pytest.raises(W.WbprError) as ei:
+        W.DeviceGraph(g, "bcsr")
+    assert ei.value.status == 7  # WBPR_ERR_NO_DEVICE
+
+
+def test_dimacs_roundtrip(tmp_path, golden):
+    for c in golden[:12]:
+        g = graph_of(c)
+        p = str(tmp_path / "g.dimacs")
+        W.write_dimacs(p, g)
+        h = W.read_dimacs(p)
+        assert (h.n, h.s, h.t) == (g.n, g.s, g.t)
+        assert np.array_equal(h.off, g.off) and np.array_equal(h.dst, g.dst)
+        assert np.array_equal(h.cap, g.cap)
+
+
+def test_snap_readers(tmp_path):
+    p = tmp_path / "g.txt"
+    p.write_text("# Directed graph\n# Nodes: 5 Edges: 6\n0 3\n0 1\n0 2\n1 4\n2 4\n3 4\n")
+    g = W.read_snap_txt(str(p))
+    assert g.n == 5 and g.m == 6
+    assert list(g.dst[g.off[0]:g.off[1]]) == [1, 2, 3]  # rows sorted by head
+    assert (g.cap == 1).all()
+    b = str(tmp_path / "g.bin")
+    W.write_snap_bin(b, g)
+    h = W.read_snap_bin(b)
+    assert np.array_equal(h.off, g.off) and np.array_equal(h.dst, g.dst) and (h.cap == 1).all()
+
+
+@pytest.mark.parametrize("text", [
+    "p max 3 1\na 1 4 5\n",          # head out of range
+    "p max 3 1\na 1 2\n",            # truncated arc line
+    "a 1 2 3\n",                     # arc before problem line
+    "p max 3 1\na 1 2 -4\n",         # negative capacity
+    "p max 3 1\nq 1 2 3\n",          # unknown line type
+    "p max -2 1\n",                  # bad vertex count
+])
+def test_malformed_dimacs_is_an_io_error(tmp_path, text):
+    p = tmp_path / "bad.dimacs"
+    p.write_text(text)
+    with pytest.raises(W.WbprError) as ei:
+        W.read_dimacs(str(p))
+    assert ei.value.status == 6
+
+
+def test_missing_and_truncated_files(tmp_path):
+    with pytest.raises(W.WbprError) as ei:
+        W.read_dimacs(str(tmp_path / "nope"))
+    assert ei.value.status == 6
+    b = tmp_path / "t.bin"
+    b.write_bytes(np.asarray([5, 6, 6, 1, 2], np.int32).tobytes())
+    with pytest.raises(W.WbprError):
+        W.read_snap_bin(str(b))
+
+
+def _check_pairing_bcsr(g, off, dst, cap, bidx):
+    n, m = g.n, g.m
+    assert off[-1] == 2 * m
+    tail = np.repeat(np.arange(n), np.diff(off))
+    assert (bidx[bidx] == np.arange(2 * m)).all()          # involution
+    assert (dst[bidx] == tail).all() and (tail[bidx] == dst).all()
+    assert ((cap == 0) | (cap[bidx] == 0)).all()           # one side of each pair is a twin
+    assert cap.sum() == g.cap.sum()
+
+
+def test_bcsr_builders_pair_exactly():
+    # parallel and antiparallel arcs included
+    g = W.Graph.from_arcs(4, [0, 0, 1, 2, 1, 3, 2], [1, 1, 0, 3, 2, 1, 3], [3, 4, 5, 6, 7, 8, 9], 0, 3)
+    off, dst, cap, bidx = W.build_bcsr(g)
+    _check_pairing_bcsr(g, off, dst, cap, bidx)
+    off2, dst2, flows = W.build_bcsr2(g)
+    assert np.array_equal(off2, off) and np.array_equal(dst2, dst)
+    assert np.array_equal(flows[0::2], cap) and np.array_equal(flows[1::2], bidx)
+    for seed in range(5):
+        h = W.gen_rmat(8, 8, seed=seed)
+        _check_pairing_bcsr(h, *W.build_bcsr(h))
+
+
+def test_rcsr_builder_pairs_exactly():
+    g = W.Graph.from_arcs(4, [0, 0, 1, 2, 1, 3, 2], [1, 1, 0, 3, 2, 1, 3], [3, 4, 5, 6, 7, 8, 9], 0, 3)
+    roff, rdst, fidx = W.build_rcsr(g)
+    tail = np.repeat(np.arange(g.n), np.diff(g.off))
+    assert sorted(fidx.tolist()) == list(range(g.m))        # a permutation (no first-match aliasing)
+    rhead = np.repeat(np.arange(g.n), np.diff(roff))
+    assert (g.dst[fidx] == rhead).all() and (tail[fidx] == rdst).all()
+
+
+def test_generator_shapes():
+    g = W.gen_genrmf(8, 16, 1, 10000, 1)
+    assert (g.n, g.m, g.s, g.t) == (1024, 4544, 0, 1023)
+    tail, head, cap = g.arcs()
+    inframe = (tail // 64) == (head // 64)
+    assert (cap[inframe] == 640000).all()
+    assert ((cap[~inframe] >= 1) & (cap[~inframe] <= 10000)).all()
+    r = W.gen_rmat(10, 16, seed=3)
+    tail, head, cap = r.arcs()
+    assert (tail != head).all()
+    assert len(np.unique(tail.astype(np.int64) * r.n + head)) == r.m
+    assert cap.min() >= 1 and cap.max() <= 100
+    deg = np.diff(r.off)
+    assert r.s == int(np.argmax(deg))
+    b = W.gen_bipartite(200, 150, 2.0, 4096, 2)
+    assert b.n == 352 and b.s == 0 and b.t == 351 and (b.cap == 1).all()
+    lay = W.gen_layered(5, 7, 3, 6, 1, 1000, 1)
+    assert lay.n == 37
+    grid = W.gen_grid(16, 12, 4)
+    assert grid.n == 16 * 12 + 2 and grid.m == 2 * (15 * 12 + 16 * 11) + 2 * 16 * 12
+
+
+def test_generators_are_pinned(golden):
+    """Same seed, same bits: hashes recorded by the golden script."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mg", os.path.join(ROOT, "tests", "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    make = {
+        "genrmf_a4_b6_s0": lambda: W.gen_genrmf(4, 6, 1, 10000, 0),
+        "genrmf_a8_b16_s1": lambda: W.gen_genrmf(8, 16, 1, 10000, 1),
+        "layered_6x12_s3": lambda: W.gen_layered(6, 12, 3, 6, 1, 1000, 3),
+        "bipartite_40x30_s5": lambda: W.gen_bipartite(40, 30, 2.0, 4096, 5),
+        "grid_8x8_s2": lambda: W.gen_grid(8, 8, 2),
+        "rmat_s7_s1": lambda: W.gen_rmat(7, 8, 0.57, 0.19, 0.19, 1, 100, 1),
+    }
+    hashes = {c["name"]: c.get("csr_hash") for c in golden}
+    for name, fn in make.items():
+        assert mg.csr_hash(fn()) == hashes[name], name
+
+
+def test_rmat_independent_of_thread_count():
+    env = dict(os.environ, WBPR_HOST_THREADS="1")
+    code = ("import sys; sys.path.insert(0, %r); import wbpr_gb300 as W, hashlib;"
+            "g=W.gen_rmat(12,16,seed=9); print(hashlib.sha256(g.dst.tobytes()+g.cap.tobytes()).hexdigest())" % ROOT)
+    one = subprocess.run(["python3", "-c", code], env=env, capture_output=True, text=True, check=True).stdout
+    many = subprocess.run(["python3", "-c", code], capture_output=True, text=True, check=True).stdout
+    assert one == many
+
+
+def test_overflowing_capacities_are_rejected(has_gpu):
+    # sum of capacities into t exceeds int32: refused before any device work
+    g = W.Graph.from_arcs(3, [0, 0, 1, 1], [1, 2, 2, 2], [2**31 - 1, 2**31 - 1, 2**31 - 1, 5], 0, 2)
+    with pytest.raises(W.WbprError) as ei:
+        W.DeviceGraph(g, "bcsr")
+    assert ei.value.status == 4
+
+
+def test_cli_usage_and_errors(tmp_path):
+    cli = wb.CLI
+    r = subprocess.run([cli, "-h"], capture_output=True, text=True)
+    assert r.returncode == 0 and "Vertex-centric push-relabel" in r.stdout
+    r = subprocess.run([cli, "-v", "2", "-f", str(tmp_path / "missing")], capture_output=True, text=True)
+    assert r.returncode == 1
+    r = subprocess.run([cli, "-v", "9", "-f", "x"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Invalid file type" in r.stdout

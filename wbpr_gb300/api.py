@@ -1,0 +1,400 @@
+"""ctypes binding of libwbpr (include/wbpr.h).
+
+Host-side mirror of the reference's solve path for Python callers and tests:
+read or generate a CSR graph, create a device residual graph (RCSR or BCSR),
+solve (thread-centric or vertex-centric), verify, read back state, min-cut
+adjoint, and the reference drop-ins ``rcsr_preflow`` / ``rcsr_push_relabel``
+(maxflow-cuda/src/preflow.cu:3-31, maxflow-cuda/src/push_relabel.cu:35-221).
+
+Every call goes through the compiled library; there is no Python fallback.
+A missing library or CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import build as _build
+
+_i32p = C.POINTER(C.c_int32)
+_i8p = C.POINTER(C.c_int8)
+
+
+class WbprError(RuntimeError):
+    def __init__(self, status: int, what: str, detail: str = ""):
+        self.status = status
+        msg = f"{what}: {status_str(status)} (status {status})"
+        if detail:
+            msg += f" [{detail}]"
+        super().__init__(msg)
+
+
+class CsrView(C.Structure):
+    _fields_ = [("num_nodes", C.c_int32), ("num_edges", C.c_int64), ("offsets", _i32p),
+                ("destinations", _i32p), ("capacities", _i32p), ("source", C.c_int32),
+                ("sink", C.c_int32)]
+
+
+class HostCsr(C.Structure):
+    _fields_ = [("num_nodes", C.c_int32), ("num_edges", C.c_int64), ("num_edges_declared", C.c_int64),
+                ("offsets", _i32p), ("destinations", _i32p), ("capacities", _i32p),
+                ("source", C.c_int32), ("sink", C.c_int32)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("tile", C.c_int32), ("block", C.c_int32), ("heavy_degree", C.c_int32),
+                ("blocks_per_sm", C.c_int32), ("gr_alpha", C.c_double), ("max_rounds", C.c_int64),
+                ("max_ms", C.c_double), ("verify", C.c_int32), ("reserved", C.c_int32)]
+
+
+class Result(C.Structure):
+    _fields_ = [("flow", C.c_int64), ("solve_ms", C.c_float), ("kernel_ms", C.c_float),
+                ("gr_ms", C.c_float), ("arcs_scanned", C.c_uint64), ("pushes", C.c_uint64),
+                ("relabels", C.c_uint64), ("vertex_visits", C.c_uint64), ("bfs_arcs", C.c_uint64),
+                ("bfs_vertices", C.c_uint64), ("alg_bytes", C.c_uint64), ("rounds", C.c_int32),
+                ("global_relabels", C.c_int32), ("stranded", C.c_int32), ("launch_ms", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class VerifyReport(C.Structure):
+    _fields_ = [("ok", C.c_int32), ("capacity_violations", C.c_int32),
+                ("conservation_violations", C.c_int32), ("source_reaches_sink", C.c_int32),
+                ("excess_reaches_sink", C.c_int32), ("reserved", C.c_int32),
+                ("cut_value", C.c_int64), ("flow_value", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+LAYOUTS = {"rcsr": 0, "bcsr": 1, "bcsr2": 2}
+ALGOS = {"tc": 0, "vc": 1, 0: 0, 1: 1}
+
+# every symbol declared in include/wbpr.h
+EXPORTED = [
+    "wbpr_status_str", "wbpr_abi_version", "wbpr_default_tuning", "wbpr_device_count",
+    "wbpr_last_error", "wbpr_read_snap_txt", "wbpr_read_snap_bin", "wbpr_read_dimacs",
+    "wbpr_write_snap_bin", "wbpr_write_dimacs", "wbpr_host_csr_copy", "wbpr_host_csr_free",
+    "wbpr_gen_genrmf", "wbpr_gen_rmat", "wbpr_gen_bipartite", "wbpr_gen_layered", "wbpr_gen_grid",
+    "wbpr_build_rcsr", "wbpr_build_bcsr", "wbpr_build_bcsr2", "wbpr_graph_create",
+    "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_solve", "wbpr_read_state",
+    "wbpr_verify", "wbpr_mincut_adjoint", "wbpr_rcsr_preflow", "wbpr_rcsr_push_relabel",
+]
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libwbpr.so (building it first when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path) or os.environ.get("WBPR_REBUILD"):
+        _build.build()
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    hp = C.POINTER(C.POINTER(HostCsr))
+    sig = {
+        "wbpr_status_str": (C.c_char_p, [C.c_int]),
+        "wbpr_abi_version": (C.c_int32, []),
+        "wbpr_default_tuning": (None, [C.POINTER(Tuning)]),
+        "wbpr_device_count": (C.c_int32, []),
+        "wbpr_last_error": (C.c_char_p, []),
+        "wbpr_read_snap_txt": (C.c_int, [C.c_char_p, hp]),
+        "wbpr_read_snap_bin": (C.c_int, [C.c_char_p, hp]),
+        "wbpr_read_dimacs": (C.c_int, [C.c_char_p, hp]),
+        "wbpr_write_snap_bin": (C.c_int, [C.c_char_p, C.POINTER(CsrView)]),
+        "wbpr_write_dimacs": (C.c_int, [C.c_char_p, C.POINTER(CsrView)]),
+        "wbpr_host_csr_copy": (C.c_int, [C.POINTER(CsrView), hp]),
+        "wbpr_host_csr_free": (None, [C.POINTER(HostCsr)]),
+        "wbpr_gen_genrmf": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, hp]),
+        "wbpr_gen_rmat": (C.c_int, [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double,
+                                    C.c_int32, C.c_int32, C.c_uint64, hp]),
+        "wbpr_gen_bipartite": (C.c_int, [C.c_int32, C.c_int32, C.c_double, C.c_int32, C.c_uint64, hp]),
+        "wbpr_gen_layered": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                       C.c_int32, C.c_uint64, hp]),
+        "wbpr_gen_grid": (C.c_int, [C.c_int32, C.c_int32, C.c_uint64, hp]),
+        "wbpr_build_rcsr": (C.c_int, [C.POINTER(CsrView), _i32p, _i32p, _i32p]),
+        "wbpr_build_bcsr": (C.c_int, [C.POINTER(CsrView), _i32p, _i32p, _i32p, _i32p]),
+        "wbpr_build_bcsr2": (C.c_int, [C.POINTER(CsrView), _i32p, _i32p, _i32p]),
+        "wbpr_graph_create": (C.c_int, [C.POINTER(CsrView), C.c_int, C.POINTER(vp)]),
+        "wbpr_graph_destroy": (C.c_int, [vp]),
+        "wbpr_graph_device_bytes": (C.c_int64, [vp]),
+        "wbpr_solve": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int, C.POINTER(Tuning), C.POINTER(Result)]),
+        "wbpr_read_state": (C.c_int, [vp, _i32p, _i32p, _i32p]),
+        "wbpr_verify": (C.c_int, [vp, C.POINTER(VerifyReport)]),
+        "wbpr_mincut_adjoint": (C.c_int, [vp, C.c_int32, _i8p, C.POINTER(C.c_float)]),
+        "wbpr_rcsr_preflow": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, _i32p, _i32p, _i32p, _i32p,
+                                          _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p]),
+        "wbpr_rcsr_push_relabel": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                               _i32p, _i32p, _i32p, _i32p, _i32p, _i32p, _i32p,
+                                               _i32p, _i32p, _i32p, _i32p, C.POINTER(C.c_float)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def status_str(st: int) -> str:
+    return lib().wbpr_status_str(st).decode()
+
+
+def _check(st: int, what: str) -> None:
+    if st != 0:
+        raise WbprError(st, what, lib().wbpr_last_error().decode())
+
+
+def device_count() -> int:
+    return int(lib().wbpr_device_count())
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_i32p)
+
+
+@dataclass
+class Graph:
+    """Host CSR graph (the reference's CSRGraph, maxflow-cuda/include/graph.h:28-58)."""
+    n: int
+    off: np.ndarray
+    dst: np.ndarray
+    cap: np.ndarray
+    s: int = -1
+    t: int = -1
+    m_declared: int = -1
+    _keep: list = field(default_factory=list, repr=False)
+
+    @property
+    def m(self) -> int:
+        return int(len(self.dst))
+
+    def view(self) -> CsrView:
+        self.off = np.ascontiguousarray(self.off, dtype=np.int32)
+        self.dst = np.ascontiguousarray(self.dst, dtype=np.int32)
+        self.cap = np.ascontiguousarray(self.cap, dtype=np.int32)
+        d = self.dst if len(self.dst) else np.zeros(1, np.int32)
+        c = self.cap if len(self.cap) else np.zeros(1, np.int32)
+        self._keep = [d, c]
+        return CsrView(self.n, self.m, _p(self.off), _p(d), _p(c), self.s, self.t)
+
+    def arcs(self):
+        """(tail, head, cap) arrays, input order."""
+        tail = np.repeat(np.arange(self.n, dtype=np.int32), np.diff(self.off))
+        return tail, self.dst, self.cap
+
+    @staticmethod
+    def from_arcs(n: int, tail, head, cap, s: int, t: int) -> "Graph":
+        """CSR grouped by tail, keeping the given order inside each row."""
+        tail = np.asarray(tail, np.int64)
+        order = np.argsort(tail, kind="stable")
+        off = np.zeros(n + 1, np.int64)
+        np.add.at(off, tail + 1, 1)
+        return Graph(n, np.cumsum(off).astype(np.int32), np.asarray(head, np.int32)[order],
+                     np.asarray(cap, np.int32)[order], s, t)
+
+
+def _take(ptr) -> Graph:
+    h = ptr.contents
+    n, m = h.num_nodes, h.num_edges
+    off = np.ctypeslib.as_array(h.offsets, shape=(n + 1,)).copy()
+    dst = np.ctypeslib.as_array(h.destinations, shape=(max(m, 1),))[:m].copy()
+    cap = np.ctypeslib.as_array(h.capacities, shape=(max(m, 1),))[:m].copy()
+    g = Graph(n, off, dst, cap, h.source, h.sink, h.num_edges_declared)
+    lib().wbpr_host_csr_free(ptr)
+    return g
+
+
+def _reader(fn: str, path: str) -> Graph:
+    out = C.POINTER(HostCsr)()
+    _check(getattr(lib(), fn)(os.fsencode(path), C.byref(out)), fn)
+    return _take(out)
+
+
+def read_snap_txt(path: str) -> Graph:
+    return _reader("wbpr_read_snap_txt", path)
+
+
+def read_snap_bin(path: str) -> Graph:
+    return _reader("wbpr_read_snap_bin", path)
+
+
+def read_dimacs(path: str) -> Graph:
+    return _reader("wbpr_read_dimacs", path)
+
+
+def read_graph(path: str, file_type: int) -> Graph:
+    return [read_snap_txt, read_snap_bin, read_dimacs][file_type](path)
+
+
+def write_dimacs(path: str, g: Graph) -> None:
+    v = g.view()
+    _check(lib().wbpr_write_dimacs(os.fsencode(path), C.byref(v)), "wbpr_write_dimacs")
+
+
+def write_snap_bin(path: str, g: Graph) -> None:
+    v = g.view()
+    _check(lib().wbpr_write_snap_bin(os.fsencode(path), C.byref(v)), "wbpr_write_snap_bin")
+
+
+def _gen(fn: str, *args) -> Graph:
+    out = C.POINTER(HostCsr)()
+    _check(getattr(lib(), fn)(*args, C.byref(out)), fn)
+    return _take(out)
+
+
+def gen_genrmf(a: int, b: int, c1: int = 1, c2: int = 10000, seed: int = 0) -> Graph:
+    return _gen("wbpr_gen_genrmf", a, b, c1, c2, seed)
+
+
+def gen_rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             cap_lo: int = 1, cap_hi: int = 100, seed: int = 1) -> Graph:
+    return _gen("wbpr_gen_rmat", scale, edge_factor, a, b, c, cap_lo, cap_hi, seed)
+
+
+def gen_bipartite(left: int, right: int, zipf_s: float = 2.0, dmax: int = 4096, seed: int = 0) -> Graph:
+    return _gen("wbpr_gen_bipartite", left, right, zipf_s, dmax, seed)
+
+
+def gen_layered(layers: int, width: int, deg_lo: int = 3, deg_hi: int = 6, cap_lo: int = 1,
+                cap_hi: int = 1000, seed: int = 0) -> Graph:
+    return _gen("wbpr_gen_layered", layers, width, deg_lo, deg_hi, cap_lo, cap_hi, seed)
+
+
+def gen_grid(w: int, h: int, seed: int = 0) -> Graph:
+    return _gen("wbpr_gen_grid", w, h, seed)
+
+
+def build_rcsr(g: Graph):
+    v = g.view()
+    roff = np.zeros(g.n + 1, np.int32)
+    rdst = np.zeros(max(g.m, 1), np.int32)
+    fidx = np.zeros(max(g.m, 1), np.int32)
+    _check(lib().wbpr_build_rcsr(C.byref(v), _p(roff), _p(rdst), _p(fidx)), "wbpr_build_rcsr")
+    return roff, rdst[:g.m], fidx[:g.m]
+
+
+def build_bcsr(g: Graph):
+    v = g.view()
+    off = np.zeros(g.n + 1, np.int32)
+    k = max(2 * g.m, 1)
+    dst, cap, bidx = (np.zeros(k, np.int32) for _ in range(3))
+    _check(lib().wbpr_build_bcsr(C.byref(v), _p(off), _p(dst), _p(cap), _p(bidx)), "wbpr_build_bcsr")
+    return off, dst[:2 * g.m], cap[:2 * g.m], bidx[:2 * g.m]
+
+
+def build_bcsr2(g: Graph):
+    v = g.view()
+    off = np.zeros(g.n + 1, np.int32)
+    dst = np.zeros(max(2 * g.m, 1), np.int32)
+    flows = np.zeros(max(4 * g.m, 1), np.int32)
+    _check(lib().wbpr_build_bcsr2(C.byref(v), _p(off), _p(dst), _p(flows)), "wbpr_build_bcsr2")
+    return off, dst[:2 * g.m], flows[:4 * g.m]
+
+
+def default_tuning(**kw) -> Tuning:
+    t = Tuning()
+    lib().wbpr_default_tuning(C.byref(t))
+    for k, v in kw.items():
+        if not hasattr(t, k):
+            raise TypeError(f"unknown tuning field {k}")
+        setattr(t, k, v)
+    return t
+
+
+class DeviceGraph:
+    """Device residual graph (library-owned device memory)."""
+
+    def __init__(self, g: Graph, layout: str = "bcsr"):
+        self._h = None
+        self.n, self.m = g.n, g.m
+        self.s, self.t = g.s, g.t
+        self.layout = layout
+        v = g.view()
+        h = C.c_void_p()
+        _check(lib().wbpr_graph_create(C.byref(v), LAYOUTS[layout], C.byref(h)), "wbpr_graph_create")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().wbpr_graph_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().wbpr_graph_device_bytes(self._h))
+
+    def solve(self, algo="vc", s: int | None = None, t: int | None = None, **tuning) -> Result:
+        r = Result()
+        tu = default_tuning(**tuning)
+        _check(lib().wbpr_solve(self._h, -1 if s is None else s, -1 if t is None else t, ALGOS[algo],
+                                C.byref(tu), C.byref(r)), "wbpr_solve")
+        if s is not None:
+            self.s = s
+        if t is not None:
+            self.t = t
+        return r
+
+    def verify(self) -> dict:
+        rep = VerifyReport()
+        _check(lib().wbpr_verify(self._h, C.byref(rep)), "wbpr_verify")
+        return rep.as_dict()
+
+    def read_state(self):
+        h = np.zeros(self.n, np.int32)
+        e = np.zeros(self.n, np.int32)
+        f = np.zeros(max(self.m, 1), np.int32)
+        _check(lib().wbpr_read_state(self._h, _p(h), _p(e), _p(f)), "wbpr_read_state")
+        return h, e, f[:self.m]
+
+    def mincut_adjoint(self, side: int = 0):
+        ind = np.zeros(max(self.m, 1), np.int8)
+        ms = C.c_float(0)
+        _check(lib().wbpr_mincut_adjoint(self._h, side, ind.ctypes.data_as(_i8p), C.byref(ms)),
+               "wbpr_mincut_adjoint")
+        return ind[:self.m], float(ms.value)
+
+
+def maxflow(g: Graph, algo="vc", layout="bcsr", **tuning) -> int:
+    with DeviceGraph(g, layout) as d:
+        return int(d.solve(algo, g.s, g.t, **tuning).flow)
+
+
+def rcsr_preflow(g: Graph, roff, rdst, fidx):
+    """Reference preflow() over host RCSR arrays; returns the mutable state."""
+    n = g.n
+    h = np.zeros(n, np.int32)
+    e = np.zeros(n, np.int32)
+    ff = g.cap.astype(np.int32).copy()
+    bf = np.zeros_like(ff)
+    tot = C.c_int32(0)
+    _check(lib().wbpr_rcsr_preflow(n, g.s, g.t, _p(h), _p(e), _p(g.off), _p(g.dst), _p(g.cap), _p(ff),
+                                   _p(bf), _p(roff), _p(rdst), _p(fidx), C.byref(tot)), "wbpr_rcsr_preflow")
+    return h, e, ff, bf, int(tot.value)
+
+
+def rcsr_push_relabel(algo_type: int, g: Graph, state, roff, rdst, fidx):
+    """Reference push_relabel() drop-in; mutates `state` in place and returns
+    (max flow = excess[sink], Excess_total, kernel_ms)."""
+    h, e, ff, bf, _ = state
+    tot = C.c_int32(0)
+    ms = C.c_float(0)
+    _check(lib().wbpr_rcsr_push_relabel(algo_type, g.n, g.m, g.s, g.t, _p(h), _p(e), _p(g.off), _p(g.dst),
+                                        _p(g.cap), _p(ff), _p(bf), _p(roff), _p(rdst), _p(fidx),
+                                        C.byref(tot), C.byref(ms)), "wbpr_rcsr_push_relabel")
+    return int(e[g.t]), int(tot.value), float(ms.value)

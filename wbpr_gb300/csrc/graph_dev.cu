@@ -1,0 +1,770 @@
+// Device graph handle, solve orchestration, certificate check, min-cut
+// adjoint and the reference drop-ins of libwbpr.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "pr_launch.h"
+#include "wbpr_internal.h"
+
+using namespace wbpr_dev;
+
+static thread_local std::string g_last_error;
+
+#define CK(call)                                                            \
+  do {                                                                      \
+    cudaError_t e_ = (call);                                                \
+    if (e_ != cudaSuccess) {                                                \
+      g_last_error = std::string(#call) + ": " + cudaGetErrorString(e_);    \
+      return WBPR_ERR_CUDA;                                                 \
+    }                                                                       \
+  } while (0)
+
+struct wbpr_graph {
+  int device = 0;
+  int sms = 0;
+  wbpr_layout layout = WBPR_LAYOUT_BCSR;
+  int32_t n = 0;
+  int64_t m = 0;
+  int32_t s = -1, t = -1;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+  // BCSR16
+  int* row = nullptr;
+  int2* arc = nullptr;
+  int2* arx = nullptr;
+  // RCSR
+  int* frow = nullptr;
+  int2* farc = nullptr;
+  int* fcb = nullptr;
+  int* fcap = nullptr;
+  int* rrow = nullptr;
+  int2* rarc = nullptr;
+  // input row offsets (maps input arc i of u to its residual slot)
+  int* ioff = nullptr;
+  // per-vertex state and scratch
+  int* h = nullptr;
+  int* e = nullptr;
+  int* rl_min = nullptr;
+  int* rl_left = nullptr;
+  int* lq[2] = {nullptr, nullptr};
+  int* hq[2] = {nullptr, nullptr};
+  int* qraw = nullptr;
+  int* fr[3] = {nullptr, nullptr, nullptr};
+  int* frh[3] = {nullptr, nullptr, nullptr};
+  int* cls = nullptr;
+  int* vlab = nullptr;
+  int8_t* ind = nullptr;
+  int* flow_tmp = nullptr;
+  int n_light = 0, n_medium = 0, n_heavy = 0;
+  long long total_deg = 0;
+  double avg_deg = 0;
+  Ctl* ctl = nullptr;
+  Stats* st = nullptr;
+  int64_t bytes = 0;
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+template <class T>
+wbpr_status dalloc(wbpr_graph* g, T** p, size_t count) {
+  void* q = nullptr;
+  size_t bytes = sizeof(T) * std::max<size_t>(count, 1);
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    return WBPR_ERR_CUDA;
+  }
+  g->allocs.push_back(q);
+  g->bytes += (int64_t)bytes;
+  *p = (T*)q;
+  return WBPR_OK;
+}
+
+void release(wbpr_graph* g) {
+  if (!g) return;
+  cudaSetDevice(g->device);
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  for (void* q : g->allocs) cudaFree(q);
+  if (g->ev0) cudaEventDestroy(g->ev0);
+  if (g->ev1) cudaEventDestroy(g->ev1);
+  if (g->ev2) cudaEventDestroy(g->ev2);
+  if (g->ev3) cudaEventDestroy(g->ev3);
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+}
+
+// ---------------------------------------------------------------------------
+// small kernels
+__global__ void reset_bcsr(int2* arc, const int2* arx, long long na) {
+  for (long long a = blockIdx.x * (long long)blockDim.x + threadIdx.x; a < na;
+       a += (long long)gridDim.x * blockDim.x)
+    arc[a].y = __ldg(&arx[a].y);
+}
+__global__ void reset_rcsr(int2* farc, int* fcb, const int* fcap, long long m) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m;
+       i += (long long)gridDim.x * blockDim.x) {
+    farc[i].y = __ldg(fcap + i);
+    fcb[i] = 0;
+  }
+}
+
+struct VerifyAcc {
+  int cap_viol;
+  int cons_viol;
+  int excess_reach;
+  int pad;
+  long long cut;
+};
+
+// warp per vertex: capacity pair invariant, conservation, cut of the sink side
+__global__ void verify_bcsr(const int* row, const int2* arc, const int2* arx, const int* e,
+                            const int* lab, int n, int s, int t, VerifyAcc* out) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int v = gw; v < n; v += nw) {
+    long long net = 0, cut = 0;
+    int bad = 0;
+    const bool vin = lab[v] < n;
+    for (int a = row[v] + lane; a < row[v + 1]; a += 32) {
+      const int2 r = arc[a], x = arx[a];
+      const int2 rr = arc[x.x], xr = arx[x.x];
+      if (r.y < 0 || (long long)r.y + rr.y != (long long)x.y + xr.y) ++bad;
+      net += (long long)r.y - x.y;
+      if (!vin && x.y > 0 && lab[r.x] < n) cut += x.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      net += __shfl_down_sync(0xffffffffu, net, o);
+      cut += __shfl_down_sync(0xffffffffu, cut, o);
+      bad += __shfl_down_sync(0xffffffffu, bad, o);
+    }
+    if (lane == 0) {
+      if (bad) atomicAdd(&out->cap_viol, bad);
+      if (v != s && net != (long long)e[v]) atomicAdd(&out->cons_viol, 1);
+      if (cut) atomicAdd((unsigned long long*)&out->cut, (unsigned long long)cut);
+      if (v != s && v != t && e[v] > 0 && vin) atomicAdd(&out->excess_reach, 1);
+    }
+  }
+}
+
+__global__ void verify_rcsr(const int* frow, const int2* farc, const int* fcb, const int* fcap,
+                            const int* rrow, const int2* rarc, const int* e, const int* lab, int n,
+                            int s, int t, VerifyAcc* out) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int v = gw; v < n; v += nw) {
+    long long net = 0, cut = 0;
+    int bad = 0;
+    const bool vin = lab[v] < n;
+    for (int i = frow[v] + lane; i < frow[v + 1]; i += 32) {
+      const int2 r = farc[i];
+      const int b = fcb[i], c = fcap[i];
+      if (r.y < 0 || b < 0 || (long long)r.y + b != c) ++bad;
+      net -= b;
+      if (!vin && c > 0 && lab[r.x] < n) cut += c;
+    }
+    for (int j = rrow[v] + lane; j < rrow[v + 1]; j += 32) net += fcb[rarc[j].y];
+    for (int o = 16; o > 0; o >>= 1) {
+      net += __shfl_down_sync(0xffffffffu, net, o);
+      cut += __shfl_down_sync(0xffffffffu, cut, o);
+      bad += __shfl_down_sync(0xffffffffu, bad, o);
+    }
+    if (lane == 0) {
+      if (bad) atomicAdd(&out->cap_viol, bad);
+      if (v != s && net != (long long)e[v]) atomicAdd(&out->cons_viol, 1);
+      if (cut) atomicAdd((unsigned long long*)&out->cut, (unsigned long long)cut);
+      if (v != s && v != t && e[v] > 0 && vin) atomicAdd(&out->excess_reach, 1);
+    }
+  }
+}
+
+// per input arc (tail u, head v): side 0 -> [u cannot reach t, v can];
+// side 1 -> [u reached from s, v not]
+__global__ void indicator_kernel(const int* ioff, const int* row, const int2* arc, const int2* farc,
+                                 const int* lab, int n, int side, int8_t* ind) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int u = gw; u < n; u += nw) {
+    const int b = ioff[u], e = ioff[u + 1];
+    const bool uin = lab[u] < n;
+    for (int i = b + lane; i < e; i += 32) {
+      const int v = row ? arc[row[u] + (i - b)].x : farc[i].x;
+      const bool vin = lab[v] < n;
+      ind[i] = side == 0 ? (int8_t)(!uin && vin) : (int8_t)(uin && !vin);
+    }
+  }
+}
+
+__global__ void flow_kernel(const int* ioff, const int* row, const int2* arc, const int2* arx,
+                            const int* fcb, int n, int* flow) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int u = gw; u < n; u += nw) {
+    const int b = ioff[u], e = ioff[u + 1];
+    for (int i = b + lane; i < e; i += 32) {
+      if (row) {
+        const int a = row[u] + (i - b);
+        flow[i] = arx[a].y - arc[a].y;
+      } else {
+        flow[i] = fcb[i];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out) {
+  if (!out) return WBPR_ERR_INVALID_ARG;
+  *out = nullptr;
+  wbpr_status st = wbpr::check_csr(in);
+  if (st) return st;
+  if (in->num_nodes < 2) return WBPR_ERR_INVALID_ARG;
+  if (layout != WBPR_LAYOUT_RCSR && layout != WBPR_LAYOUT_BCSR && layout != WBPR_LAYOUT_BCSR2)
+    return WBPR_ERR_INVALID_ARG;
+  if (wbpr::max_in_capacity(in) > std::numeric_limits<int32_t>::max()) return WBPR_ERR_OVERFLOW;
+  if (2 * in->num_edges > std::numeric_limits<int32_t>::max()) return WBPR_ERR_OVERFLOW;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return WBPR_ERR_NO_DEVICE;
+  }
+  wbpr_graph* g = new wbpr_graph();
+  g->layout = layout == WBPR_LAYOUT_RCSR ? WBPR_LAYOUT_RCSR : WBPR_LAYOUT_BCSR;
+  g->n = in->num_nodes;
+  g->m = in->num_edges;
+  g->s = in->source;
+  g->t = in->sink;
+  auto fail = [&](wbpr_status s) {
+    release(g);
+    return s;
+  };
+#define TRY(x)                          \
+  do {                                  \
+    wbpr_status s_ = (x);               \
+    if (s_) return fail(s_);            \
+  } while (0)
+#define TRYC(x)                                                           \
+  do {                                                                    \
+    cudaError_t e_ = (x);                                                 \
+    if (e_ != cudaSuccess) {                                              \
+      g_last_error = std::string(#x) + ": " + cudaGetErrorString(e_);     \
+      return fail(WBPR_ERR_CUDA);                                         \
+    }                                                                     \
+  } while (0)
+  TRYC(cudaGetDevice(&g->device));
+  TRYC(cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, g->device));
+  TRYC(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+  TRYC(cudaEventCreate(&g->ev0));
+  TRYC(cudaEventCreate(&g->ev1));
+  TRYC(cudaEventCreate(&g->ev2));
+  TRYC(cudaEventCreate(&g->ev3));
+  const int n = g->n;
+  const int64_t m = g->m;
+  std::vector<int32_t> deg((size_t)n);
+  if (g->layout == WBPR_LAYOUT_BCSR) {
+    wbpr::Bcsr16 b;
+    TRY(wbpr::build_bcsr16(in, &b));
+    TRY(dalloc(g, &g->row, (size_t)n + 1));
+    TRY(dalloc(g, &g->arc, (size_t)(2 * m)));
+    TRY(dalloc(g, &g->arx, (size_t)(2 * m)));
+    TRYC(cudaMemcpy(g->row, b.row.data(), 4 * ((size_t)n + 1), cudaMemcpyHostToDevice));
+    if (m) {
+      TRYC(cudaMemcpy(g->arc, b.arc.data(), 16 * (size_t)m, cudaMemcpyHostToDevice));
+      TRYC(cudaMemcpy(g->arx, b.arx.data(), 16 * (size_t)m, cudaMemcpyHostToDevice));
+    }
+    for (int u = 0; u < n; ++u) deg[u] = b.row[u + 1] - b.row[u];
+  } else {
+    wbpr::Rcsr r;
+    TRY(wbpr::build_rcsr_dev(in, &r));
+    TRY(dalloc(g, &g->frow, (size_t)n + 1));
+    TRY(dalloc(g, &g->farc, (size_t)m));
+    TRY(dalloc(g, &g->fcb, (size_t)m));
+    TRY(dalloc(g, &g->fcap, (size_t)m));
+    TRY(dalloc(g, &g->rrow, (size_t)n + 1));
+    TRY(dalloc(g, &g->rarc, (size_t)m));
+    TRYC(cudaMemcpy(g->frow, r.frow.data(), 4 * ((size_t)n + 1), cudaMemcpyHostToDevice));
+    TRYC(cudaMemcpy(g->rrow, r.rrow.data(), 4 * ((size_t)n + 1), cudaMemcpyHostToDevice));
+    if (m) {
+      TRYC(cudaMemcpy(g->farc, r.farc.data(), 8 * (size_t)m, cudaMemcpyHostToDevice));
+      TRYC(cudaMemcpy(g->fcap, r.fcap.data(), 4 * (size_t)m, cudaMemcpyHostToDevice));
+      TRYC(cudaMemcpy(g->rarc, r.rarc.data(), 8 * (size_t)m, cudaMemcpyHostToDevice));
+      TRYC(cudaMemset(g->fcb, 0, 4 * (size_t)m));
+    }
+    for (int u = 0; u < n; ++u) deg[u] = (r.frow[u + 1] - r.frow[u]) + (r.rrow[u + 1] - r.rrow[u]);
+  }
+  TRY(dalloc(g, &g->ioff, (size_t)n + 1));
+  TRYC(cudaMemcpy(g->ioff, in->offsets, 4 * ((size_t)n + 1), cudaMemcpyHostToDevice));
+  // length classes for the BFS (isolated vertices are left out)
+  std::vector<int32_t> cls;
+  cls.reserve((size_t)n);
+  for (int pass = 0; pass < 3; ++pass)
+    for (int u = 0; u < n; ++u) {
+      const int d = deg[u];
+      if (d == 0) continue;
+      const int c = d <= kLightDeg ? 0 : (d <= kHeavyDeg ? 1 : 2);
+      if (c == pass) cls.push_back(u);
+    }
+  for (int u = 0; u < n; ++u) {
+    const int d = deg[u];
+    g->total_deg += d;
+    if (d == 0) continue;
+    if (d <= kLightDeg) ++g->n_light;
+    else if (d <= kHeavyDeg) ++g->n_medium;
+    else ++g->n_heavy;
+  }
+  g->avg_deg = n ? (double)g->total_deg / std::max<int64_t>(1, g->n_light + g->n_medium + g->n_heavy) : 0;
+  TRY(dalloc(g, &g->cls, cls.size()));
+  if (!cls.empty()) TRYC(cudaMemcpy(g->cls, cls.data(), 4 * cls.size(), cudaMemcpyHostToDevice));
+  int** vec[] = {&g->h, &g->e, &g->rl_min, &g->rl_left, &g->lq[0], &g->lq[1], &g->hq[0], &g->hq[1],
+                 &g->qraw, &g->fr[0], &g->fr[1], &g->fr[2], &g->vlab};
+  for (int** p : vec) TRY(dalloc(g, p, (size_t)n));
+  for (int k = 0; k < 3; ++k) TRY(dalloc(g, &g->frh[k], (size_t)g->n_heavy + 1));
+  TRY(dalloc(g, &g->ctl, 1));
+  TRY(dalloc(g, &g->st, 1));
+  TRYC(cudaMemset(g->h, 0, 4 * (size_t)n));
+  TRYC(cudaMemset(g->e, 0, 4 * (size_t)n));
+#undef TRY
+#undef TRYC
+  *out = g;
+  return WBPR_OK;
+}
+
+template <class Topo>
+void fill_common(wbpr_graph* g, Params<Topo>& p) {
+  p.n = g->n;
+  p.lab = g->h;
+  p.e = g->e;
+  p.rl_min = g->rl_min;
+  p.rl_left = g->rl_left;
+  for (int k = 0; k < 2; ++k) {
+    p.lq[k] = g->lq[k];
+    p.hq[k] = g->hq[k];
+  }
+  p.qraw = g->qraw;
+  for (int k = 0; k < 3; ++k) {
+    p.fr[k] = g->fr[k];
+    p.frh[k] = g->frh[k];
+  }
+  p.cls = g->cls;
+  p.n_light = g->n_light;
+  p.n_medium = g->n_medium;
+  p.n_heavy = g->n_heavy;
+  p.ctl = g->ctl;
+  p.st = g->st;
+  p.total_deg = g->total_deg;
+  p.bar_timeout_ns = 10ull * 1000 * 1000 * 1000;
+  p.bfs_dir = 0;
+  p.bfs_root = 0;
+  p.bfs_excl = -1;
+}
+
+void topo_of(wbpr_graph* g, TopoB& b) {
+  b.row = g->row;
+  b.arc = g->arc;
+  b.arx = g->arx;
+}
+void topo_of(wbpr_graph* g, TopoR& r) {
+  r.frow = g->frow;
+  r.farc = g->farc;
+  r.fcb = g->fcb;
+  r.rrow = g->rrow;
+  r.rarc = g->rarc;
+}
+
+struct RunCfg {
+  int mode;
+  int s, t;
+  int tile;
+  int threads;
+  int blocks_per_sm;
+  int heavy_deg;
+  unsigned long long gr_threshold;
+  long long max_rounds;
+  unsigned long long budget_ns;
+  int bfs_dir, bfs_root, bfs_excl;
+  int* lab;
+};
+
+template <class Topo>
+wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch_ms) {
+  Params<Topo> p;
+  std::memset(&p, 0, sizeof(p));
+  topo_of(g, p.g);
+  fill_common(g, p);
+  p.s = rc.s;
+  p.t = rc.t;
+  p.mode = rc.mode;
+  p.heavy_deg = rc.heavy_deg;
+  p.gr_threshold = rc.gr_threshold;
+  p.max_rounds = rc.max_rounds;
+  p.budget_ns = rc.budget_ns;
+  p.bfs_dir = rc.bfs_dir;
+  p.bfs_root = rc.bfs_root;
+  p.bfs_excl = rc.bfs_excl;
+  if (rc.lab) p.lab = rc.lab;
+  const int occ = occupancy_pr(&p, rc.tile, rc.threads);
+  if (occ <= 0) {
+    g_last_error = "persistent kernel does not fit on an SM";
+    return WBPR_ERR_CUDA;
+  }
+  const int bps = rc.blocks_per_sm > 0 ? std::min(occ, rc.blocks_per_sm) : occ;
+  CK(cudaMemsetAsync(g->ctl, 0, sizeof(Ctl), g->stream));
+  CK(cudaMemsetAsync(g->st, 0, sizeof(Stats), g->stream));
+  CK(cudaEventRecord(g->ev2, g->stream));
+  CK(launch_pr(p, rc.tile, g->sms * bps, rc.threads, g->stream));
+  CK(cudaEventRecord(g->ev3, g->stream));
+  if (rc.mode != kModeBfsOnly) CK(launch_stranded(p, g->sms * 4, 256, g->stream));
+  Ctl hc;
+  CK(cudaMemcpyAsync(&hc, g->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaMemcpyAsync(hs, g->st, sizeof(Stats), cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  if (launch_ms) CK(cudaEventElapsedTime(launch_ms, g->ev2, g->ev3));
+  if (hc.err) return (wbpr_status)hc.err;
+  return WBPR_OK;
+}
+
+wbpr_status run(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch_ms = nullptr) {
+  return g->layout == WBPR_LAYOUT_RCSR ? run_kernel<TopoR>(g, rc, hs, launch_ms)
+                                       : run_kernel<TopoB>(g, rc, hs, launch_ms);
+}
+
+void tuning_defaults(wbpr_tuning* t) {
+  std::memset(t, 0, sizeof(*t));
+  t->gr_alpha = 1.0;
+  t->max_ms = 600000.0;
+}
+
+wbpr_status make_cfg(wbpr_graph* g, int s, int t, wbpr_algo algo, const wbpr_tuning* tu, RunCfg* rc) {
+  wbpr_tuning d;
+  tuning_defaults(&d);
+  if (!tu) tu = &d;
+  if (algo != WBPR_ALGO_TC && algo != WBPR_ALGO_VC) return WBPR_ERR_INVALID_ARG;
+  if (s < 0 || t < 0 || s >= g->n || t >= g->n || s == t) return WBPR_ERR_INVALID_ARG;
+  std::memset(rc, 0, sizeof(*rc));
+  rc->s = s;
+  rc->t = t;
+  int tile = tu->tile;
+  if (tile != 0 && tile != 8 && tile != 16 && tile != 32) return WBPR_ERR_INVALID_ARG;
+  if (tile == 0) tile = g->avg_deg < 10 ? 8 : (g->avg_deg < 20 ? 16 : 32);
+  rc->tile = algo == WBPR_ALGO_TC ? 1 : tile;
+  int threads = tu->block ? tu->block : 256;
+  if (threads < 64 || threads > 256 || threads % 32) return WBPR_ERR_INVALID_ARG;
+  rc->threads = threads;
+  rc->blocks_per_sm = tu->blocks_per_sm > 0 ? tu->blocks_per_sm : 2;
+  rc->heavy_deg = tu->heavy_degree > 0 ? tu->heavy_degree : (algo == WBPR_ALGO_TC ? 128 : 1024);
+  const double alpha = tu->gr_alpha > 0 ? tu->gr_alpha : 1.0;
+  rc->gr_threshold = (unsigned long long)(alpha * ((double)g->n + (double)g->total_deg)) + 1;
+  rc->max_rounds = tu->max_rounds;
+  const double ms = tu->max_ms > 0 ? tu->max_ms : 600000.0;
+  rc->budget_ns = (unsigned long long)(ms * 1e6);
+  rc->bfs_excl = -1;
+  return WBPR_OK;
+}
+
+uint64_t alg_bytes(const wbpr_graph* g, const Stats& s) {
+  // bytes each counted unit must move (residual layout of this handle)
+  const uint64_t arc_b = 12;   // {dst, cf} record + label of the head
+  const uint64_t visit_b = 16; // row bounds, excess, label
+  const uint64_t push_b = 24;  // twin index, residual store, twin RMW, excess RMW
+  const uint64_t rel_b = 12;   // relabel record + label store
+  const uint64_t bfs_arc_b = 12, bfs_v_b = 8;
+  // reset: BCSR reads cap and writes cf of 2m residual arcs; RCSR writes
+  // cf_f and cf_b and reads cap of m forward arcs
+  const uint64_t reset_b = g->layout == WBPR_LAYOUT_RCSR ? 12ull * g->m : 16ull * g->m;
+  return s.arcs_scanned * arc_b + s.vertex_visits * visit_b + s.pushes * push_b +
+         s.relabels * rel_b + s.bfs_arcs * bfs_arc_b + s.bfs_vertices * bfs_v_b + reset_b +
+         (uint64_t)g->n * 12 + (uint64_t)s.grs * g->n * 4;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char* wbpr_last_error(void) { return g_last_error.c_str(); }
+
+void wbpr_default_tuning(wbpr_tuning* t) {
+  if (t) tuning_defaults(t);
+}
+
+int32_t wbpr_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+wbpr_status wbpr_graph_create(const wbpr_csr* g, wbpr_layout layout, wbpr_graph** out) {
+  return create_impl(g, layout, out);
+}
+
+wbpr_status wbpr_graph_destroy(wbpr_graph* g) {
+  if (!g) return WBPR_ERR_INVALID_ARG;
+  release(g);
+  return WBPR_OK;
+}
+
+int64_t wbpr_graph_device_bytes(const wbpr_graph* g) { return g ? g->bytes : 0; }
+
+wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, const wbpr_tuning* tu,
+                       wbpr_result* out) {
+  if (!g) return WBPR_ERR_INVALID_ARG;
+  if (s < 0) s = g->s;
+  if (t < 0) t = g->t;
+  RunCfg rc;
+  wbpr_status st = make_cfg(g, s, t, algo, tu, &rc);
+  if (st) return st;
+  rc.mode = kModeFresh;
+  rc.bfs_excl = s;
+  CK(cudaSetDevice(g->device));
+  CK(cudaEventRecord(g->ev0, g->stream));
+  if (g->layout == WBPR_LAYOUT_RCSR) {
+    if (g->m) reset_rcsr<<<g->sms * 8, 256, 0, g->stream>>>(g->farc, g->fcb, g->fcap, g->m);
+  } else {
+    if (g->m) reset_bcsr<<<g->sms * 8, 256, 0, g->stream>>>(g->arc, g->arx, 2 * g->m);
+  }
+  CK(cudaGetLastError());
+  Stats hs;
+  float launch_ms = 0;
+  st = run(g, rc, &hs, &launch_ms);
+  CK(cudaEventRecord(g->ev1, g->stream));
+  CK(cudaEventSynchronize(g->ev1));
+  if (st) return st;
+  int et = 0;
+  CK(cudaMemcpy(&et, g->e + t, 4, cudaMemcpyDeviceToHost));
+  if (out) {
+    std::memset(out, 0, sizeof(*out));
+    out->flow = et;
+    CK(cudaEventElapsedTime(&out->solve_ms, g->ev0, g->ev1));
+    out->kernel_ms = (float)(hs.round_ns * 1e-6);
+    out->gr_ms = (float)(hs.gr_ns * 1e-6);
+    out->arcs_scanned = hs.arcs_scanned;
+    out->pushes = hs.pushes;
+    out->relabels = hs.relabels;
+    out->vertex_visits = hs.vertex_visits;
+    out->bfs_arcs = hs.bfs_arcs;
+    out->bfs_vertices = hs.bfs_vertices;
+    out->rounds = hs.rounds;
+    out->global_relabels = hs.grs;
+    out->stranded = hs.stranded;
+    out->alg_bytes = alg_bytes(g, hs);
+    out->launch_ms = launch_ms;
+  }
+  g->s = s;
+  g->t = t;
+  if (tu && tu->verify) {
+    wbpr_verify_report rep;
+    st = wbpr_verify(g, &rep);
+    if (st) return st;
+    if (!rep.ok) return WBPR_ERR_VERIFY;
+  }
+  return WBPR_OK;
+}
+
+wbpr_status wbpr_read_state(wbpr_graph* g, int32_t* height, int32_t* excess, int32_t* arc_flow) {
+  if (!g) return WBPR_ERR_INVALID_ARG;
+  CK(cudaSetDevice(g->device));
+  CK(cudaStreamSynchronize(g->stream));
+  if (height) CK(cudaMemcpy(height, g->h, 4 * (size_t)g->n, cudaMemcpyDeviceToHost));
+  if (excess) CK(cudaMemcpy(excess, g->e, 4 * (size_t)g->n, cudaMemcpyDeviceToHost));
+  if (arc_flow && g->m) {
+    if (!g->flow_tmp) {
+      wbpr_status st = dalloc(g, &g->flow_tmp, (size_t)g->m);
+      if (st) return st;
+    }
+    flow_kernel<<<g->sms * 4, 256, 0, g->stream>>>(g->ioff, g->row, g->arc, g->arx, g->fcb, g->n,
+                                                   g->flow_tmp);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(arc_flow, g->flow_tmp, 4 * (size_t)g->m, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+  }
+  return WBPR_OK;
+}
+
+static wbpr_status bfs_labels(wbpr_graph* g, int root, int dir, int excl) {
+  RunCfg rc;
+  wbpr_status st = make_cfg(g, g->s, g->t, WBPR_ALGO_VC, nullptr, &rc);
+  if (st) return st;
+  rc.mode = kModeBfsOnly;
+  rc.bfs_root = root;
+  rc.bfs_dir = dir;
+  rc.bfs_excl = excl;
+  rc.lab = g->vlab;
+  Stats hs;
+  return run(g, rc, &hs);
+}
+
+wbpr_status wbpr_verify(wbpr_graph* g, wbpr_verify_report* rep) {
+  if (!g || !rep) return WBPR_ERR_INVALID_ARG;
+  std::memset(rep, 0, sizeof(*rep));
+  if (g->s < 0 || g->t < 0) return WBPR_ERR_INVALID_ARG;
+  CK(cudaSetDevice(g->device));
+  wbpr_status st = bfs_labels(g, g->t, 0, -1);
+  if (st) return st;
+  VerifyAcc* dacc = nullptr;
+  CK(cudaMalloc(&dacc, sizeof(VerifyAcc)));
+  cudaMemsetAsync(dacc, 0, sizeof(VerifyAcc), g->stream);
+  if (g->layout == WBPR_LAYOUT_RCSR)
+    verify_rcsr<<<g->sms * 4, 256, 0, g->stream>>>(g->frow, g->farc, g->fcb, g->fcap, g->rrow, g->rarc,
+                                                   g->e, g->vlab, g->n, g->s, g->t, dacc);
+  else
+    verify_bcsr<<<g->sms * 4, 256, 0, g->stream>>>(g->row, g->arc, g->arx, g->e, g->vlab, g->n, g->s,
+                                                   g->t, dacc);
+  VerifyAcc h;
+  int ls = 0, et = 0;
+  cudaError_t ce = cudaGetLastError();
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(&h, dacc, sizeof(h), cudaMemcpyDeviceToHost, g->stream);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(&ls, g->vlab + g->s, 4, cudaMemcpyDeviceToHost, g->stream);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(&et, g->e + g->t, 4, cudaMemcpyDeviceToHost, g->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(g->stream);
+  cudaFree(dacc);
+  if (ce != cudaSuccess) {
+    g_last_error = std::string("verify: ") + cudaGetErrorString(ce);
+    return WBPR_ERR_CUDA;
+  }
+  rep->capacity_violations = h.cap_viol;
+  rep->conservation_violations = h.cons_viol;
+  rep->excess_reaches_sink = h.excess_reach;
+  rep->source_reaches_sink = ls < g->n ? 1 : 0;
+  rep->cut_value = h.cut;
+  rep->flow_value = et;
+  rep->ok = (h.cap_viol == 0 && h.cons_viol == 0 && h.excess_reach == 0 && ls >= g->n &&
+             h.cut == (long long)et)
+                ? 1
+                : 0;
+  return WBPR_OK;
+}
+
+wbpr_status wbpr_mincut_adjoint(wbpr_graph* g, int32_t side, int8_t* indicator, float* adjoint_ms) {
+  if (!g || !indicator || (side != 0 && side != 1)) return WBPR_ERR_INVALID_ARG;
+  if (g->s < 0 || g->t < 0) return WBPR_ERR_INVALID_ARG;
+  CK(cudaSetDevice(g->device));
+  if (!g->ind) {
+    wbpr_status st = dalloc(g, &g->ind, (size_t)g->m);
+    if (st) return st;
+  }
+  CK(cudaEventRecord(g->ev0, g->stream));
+  wbpr_status st;
+  if (side == 0) {
+    st = bfs_labels(g, g->t, 0, -1);
+  } else {
+    // return the stranded excess to s (phase 2: s absorbs, t is excluded),
+    // so the residual graph is that of a maximum flow, then BFS from s
+    RunCfg rc;
+    st = make_cfg(g, g->t, g->s, WBPR_ALGO_VC, nullptr, &rc);
+    if (st) return st;
+    rc.mode = kModeState;
+    rc.bfs_excl = g->t;
+    Stats hs;
+    st = run(g, rc, &hs);
+    if (st) return st;
+    st = bfs_labels(g, g->s, 1, -1);
+  }
+  if (st) return st;
+  indicator_kernel<<<g->sms * 4, 256, 0, g->stream>>>(g->ioff, g->row, g->arc, g->farc, g->vlab, g->n,
+                                                      side, g->ind);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(g->ev1, g->stream));
+  CK(cudaMemcpyAsync(indicator, g->ind, (size_t)g->m, cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  if (adjoint_ms) CK(cudaEventElapsedTime(adjoint_ms, g->ev0, g->ev1));
+  return WBPR_OK;
+}
+
+int32_t wbpr_rcsr_preflow(int32_t V, int32_t source, int32_t sink, int32_t* cpu_height,
+                          int32_t* cpu_excess_flow, const int32_t* offsets,
+                          const int32_t* destinations, const int32_t* capacities,
+                          int32_t* forward_flows, int32_t* backward_flows, const int32_t*,
+                          const int32_t*, const int32_t*, int32_t* Excess_total) {
+  if (V < 2 || source < 0 || source >= V || sink < 0 || sink >= V || source == sink || !cpu_height ||
+      !cpu_excess_flow || !offsets || !destinations || !capacities || !forward_flows ||
+      !backward_flows || !Excess_total)
+    return WBPR_ERR_INVALID_ARG;
+  for (int i = 0; i < V; ++i) {
+    cpu_height[i] = 0;
+    cpu_excess_flow[i] = 0;
+  }
+  cpu_height[source] = V;
+  int64_t total = 0;
+  for (int i = offsets[source]; i < offsets[source + 1]; ++i) {
+    const int v = destinations[i];
+    if (v < 0 || v >= V) return WBPR_ERR_INVALID_ARG;
+    if (capacities[i] > 0) {
+      forward_flows[i] = 0;
+      backward_flows[i] = capacities[i];
+      const int64_t ev = (int64_t)cpu_excess_flow[v] + capacities[i];
+      total += capacities[i];
+      if (ev > std::numeric_limits<int32_t>::max() || total > std::numeric_limits<int32_t>::max())
+        return WBPR_ERR_OVERFLOW;
+      cpu_excess_flow[v] = (int32_t)ev;
+    }
+  }
+  *Excess_total = (int32_t)total;
+  return WBPR_OK;
+}
+
+int32_t wbpr_rcsr_push_relabel(int32_t algo_type, int32_t V, int32_t E, int32_t source, int32_t sink,
+                               int32_t* cpu_height, int32_t* cpu_excess_flow,
+                               const int32_t* cpu_offsets, const int32_t* cpu_destinations,
+                               const int32_t* cpu_capacities, int32_t* cpu_fflows,
+                               int32_t* cpu_bflows, const int32_t*, const int32_t*, const int32_t*,
+                               int32_t* Excess_total, float* kernel_ms) {
+  if (!cpu_height || !cpu_excess_flow || !cpu_fflows || !cpu_bflows || !Excess_total)
+    return WBPR_ERR_INVALID_ARG;
+  if (algo_type != 0 && algo_type != 1) return WBPR_ERR_INVALID_ARG;
+  wbpr_csr c{V, E, cpu_offsets, cpu_destinations, cpu_capacities, source, sink};
+  wbpr_graph* g = nullptr;
+  // the reverse pairing is rebuilt exactly from the forward CSR; the caller's
+  // roffsets / rdestinations / flow_idx are not needed on the device
+  wbpr_status st = create_impl(&c, WBPR_LAYOUT_RCSR, &g);
+  if (st) return st;
+  struct Guard {
+    wbpr_graph* g;
+    ~Guard() { release(g); }
+  } guard{g};
+  if (source < 0 || sink < 0 || source >= V || sink >= V || source == sink) return WBPR_ERR_INVALID_ARG;
+  // upload the caller's preflow state
+  std::vector<int32_t> farc(2 * (size_t)E);
+  for (int64_t i = 0; i < E; ++i) {
+    if (cpu_fflows[i] < 0 || cpu_bflows[i] < 0 ||
+        (int64_t)cpu_fflows[i] + cpu_bflows[i] != (int64_t)(cpu_capacities ? cpu_capacities[i] : 1))
+      return WBPR_ERR_INVALID_ARG;
+    farc[2 * i] = cpu_destinations[i];
+    farc[2 * i + 1] = cpu_fflows[i];
+  }
+  CK(cudaSetDevice(g->device));
+  if (E) {
+    CK(cudaMemcpy(g->farc, farc.data(), 8 * (size_t)E, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(g->fcb, cpu_bflows, 4 * (size_t)E, cudaMemcpyHostToDevice));
+  }
+  CK(cudaMemcpy(g->e, cpu_excess_flow, 4 * (size_t)V, cudaMemcpyHostToDevice));
+  RunCfg rc;
+  st = make_cfg(g, source, sink, (wbpr_algo)algo_type, nullptr, &rc);
+  if (st) return st;
+  rc.mode = kModeState;
+  rc.bfs_excl = source;
+  Stats hs;
+  st = run(g, rc, &hs);
+  if (st) return st;
+  if (E) {
+    CK(cudaMemcpy(farc.data(), g->farc, 8 * (size_t)E, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(cpu_bflows, g->fcb, 4 * (size_t)E, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < E; ++i) cpu_fflows[i] = farc[2 * i + 1];
+  }
+  CK(cudaMemcpy(cpu_excess_flow, g->e, 4 * (size_t)V, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(cpu_height, g->h, 4 * (size_t)V, cudaMemcpyDeviceToHost));
+  cpu_height[source] = V;
+  *Excess_total = cpu_excess_flow[source] + cpu_excess_flow[sink];
+  if (kernel_ms) *kernel_ms = (float)(hs.round_ns * 1e-6);
+  return WBPR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,943 @@
+// Host side of libwbpr: graph readers and writers, seeded generators and the
+// residual-graph builders.  Plain C++17, no CUDA.  Every generator draws from
+// a counter-based splitmix64 stream and uses integer thresholds, so the same
+// seed gives the same graph on x86-64 and aarch64 hosts and for any number of
+// host threads.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "wbpr_internal.h"
+
+namespace wbpr {
+
+int host_threads() {
+  unsigned hc = std::thread::hardware_concurrency();
+  if (hc == 0) hc = 1;
+  if (hc > 32) hc = 32;
+  const char* env = std::getenv("WBPR_HOST_THREADS");
+  if (env) {
+    int v = std::atoi(env);
+    if (v >= 1 && v <= 256) return v;
+  }
+  return (int)hc;
+}
+
+template <class F>
+static void parallel_for(int64_t n, F&& f, int64_t grain = 1 << 16) {
+  int T = host_threads();
+  if (n < grain * 2 || T == 1) {
+    f(0, n, 0);
+    return;
+  }
+  int64_t chunks = std::min<int64_t>(T, (n + grain - 1) / grain);
+  std::vector<std::thread> th;
+  th.reserve(chunks);
+  for (int64_t c = 0; c < chunks; ++c) {
+    int64_t b = n * c / chunks, e = n * (c + 1) / chunks;
+    th.emplace_back([&f, b, e, c] { f(b, e, (int)c); });
+  }
+  for (auto& x : th) x.join();
+}
+
+// ---------------------------------------------------------------------------
+// splitmix64 (Steele, Lea, Flood 2014): one 64-bit state step and finalizer.
+static inline uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+struct Stream {
+  uint64_t x;
+  explicit Stream(uint64_t seed, uint64_t a = 0, uint64_t b = 0)
+      : x(mix64(seed ^ mix64(a * 0x9E3779B97F4A7C15ULL + 0x632BE59BD9B4E019ULL) ^
+                mix64(b + 0xD1B54A32D192ED03ULL))) {}
+  uint64_t next() {
+    x += 0x9E3779B97F4A7C15ULL;
+    return mix64(x);
+  }
+  // uniform integer in [lo, hi] (multiply-high, no modulo)
+  int64_t range(int64_t lo, int64_t hi) {
+    uint64_t span = (uint64_t)(hi - lo) + 1;
+    return lo + (int64_t)(((unsigned __int128)next() * span) >> 64);
+  }
+  // uniform double in [0, 1) with 53 random bits
+  double unit() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+};
+
+// ---------------------------------------------------------------------------
+wbpr_status check_csr(const wbpr_csr* g) {
+  if (!g || g->num_nodes < 0 || g->num_edges < 0) return WBPR_ERR_INVALID_ARG;
+  if (g->num_nodes > 0 && (!g->offsets)) return WBPR_ERR_INVALID_ARG;
+  if (g->num_edges > 0 && !g->destinations) return WBPR_ERR_INVALID_ARG;
+  if (g->num_edges > (int64_t)std::numeric_limits<int32_t>::max())
+    return WBPR_ERR_OVERFLOW;
+  const int32_t n = g->num_nodes;
+  if (n == 0) return g->num_edges == 0 ? WBPR_OK : WBPR_ERR_INVALID_ARG;
+  if (g->offsets[0] != 0 || (int64_t)g->offsets[n] != g->num_edges)
+    return WBPR_ERR_INVALID_ARG;
+  for (int32_t u = 0; u < n; ++u)
+    if (g->offsets[u + 1] < g->offsets[u]) return WBPR_ERR_INVALID_ARG;
+  std::atomic<int> bad{0};
+  parallel_for(g->num_edges, [&](int64_t b, int64_t e, int) {
+    for (int64_t i = b; i < e; ++i) {
+      int32_t v = g->destinations[i];
+      if (v < 0 || v >= n) { bad = 1; return; }
+      if (g->capacities && g->capacities[i] < 0) { bad = 1; return; }
+    }
+  });
+  return bad ? WBPR_ERR_INVALID_ARG : WBPR_OK;
+}
+
+int64_t max_in_capacity(const wbpr_csr* g) {
+  std::vector<int64_t> in((size_t)g->num_nodes, 0);
+  for (int64_t i = 0; i < g->num_edges; ++i)
+    in[g->destinations[i]] += g->capacities ? g->capacities[i] : 1;
+  int64_t mx = 0;
+  for (int64_t x : in) mx = std::max(mx, x);
+  return mx;
+}
+
+wbpr_status to_host_csr(Csr&& c, wbpr_host_csr** out) {
+  if (!out) return WBPR_ERR_INVALID_ARG;
+  auto* h = (wbpr_host_csr*)std::calloc(1, sizeof(wbpr_host_csr));
+  if (!h) return WBPR_ERR_INVALID_ARG;
+  h->num_nodes = c.n;
+  h->num_edges = c.m;
+  h->num_edges_declared = c.m_declared;
+  h->source = c.s;
+  h->sink = c.t;
+  h->offsets = (int32_t*)std::malloc(sizeof(int32_t) * ((size_t)c.n + 1));
+  h->destinations = (int32_t*)std::malloc(sizeof(int32_t) * std::max<int64_t>(1, c.m));
+  h->capacities = (int32_t*)std::malloc(sizeof(int32_t) * std::max<int64_t>(1, c.m));
+  if (!h->offsets || !h->destinations || !h->capacities) {
+    wbpr_host_csr_free(h);
+    return WBPR_ERR_INVALID_ARG;
+  }
+  std::memcpy(h->offsets, c.off.data(), sizeof(int32_t) * ((size_t)c.n + 1));
+  if (c.m) {
+    std::memcpy(h->destinations, c.dst.data(), sizeof(int32_t) * c.m);
+    std::memcpy(h->capacities, c.cap.data(), sizeof(int32_t) * c.m);
+  }
+  *out = h;
+  return WBPR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// File readers.  The whole file is read once and parsed by hand; malformed or
+// truncated input returns WBPR_ERR_IO instead of the reference's undefined
+// behaviour.
+static bool slurp(const char* path, std::string* buf) {
+  if (!path) return false;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return false;
+  std::fseek(f, 0, SEEK_END);
+  long sz = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  if (sz < 0) { std::fclose(f); return false; }
+  buf->resize((size_t)sz);
+  size_t got = sz ? std::fread(&(*buf)[0], 1, (size_t)sz, f) : 0;
+  std::fclose(f);
+  return got == (size_t)sz;
+}
+
+namespace {
+struct Lines {
+  const char* p;
+  const char* end;
+  bool next(const char** b, const char** e) {
+    if (p >= end) return false;
+    const char* q = p;
+    while (q < end && *q != '\n') ++q;
+    *b = p;
+    *e = (q > p && q[-1] == '\r') ? q - 1 : q;
+    p = q < end ? q + 1 : q;
+    return true;
+  }
+};
+// Parse a signed decimal integer; advances *p; false on no digits/overflow.
+bool parse_int(const char** p, const char* e, int64_t* v) {
+  const char* q = *p;
+  while (q < e && (*q == ' ' || *q == '\t')) ++q;
+  bool neg = false;
+  if (q < e && (*q == '-' || *q == '+')) { neg = *q == '-'; ++q; }
+  if (q >= e || *q < '0' || *q > '9') return false;
+  int64_t x = 0;
+  while (q < e && *q >= '0' && *q <= '9') {
+    x = x * 10 + (*q - '0');
+    if (x > (int64_t)1 << 40) return false;
+    ++q;
+  }
+  *v = neg ? -x : x;
+  *p = q;
+  return true;
+}
+bool parse_word(const char** p, const char* e, const char** wb, const char** we) {
+  const char* q = *p;
+  while (q < e && (*q == ' ' || *q == '\t')) ++q;
+  if (q >= e) return false;
+  *wb = q;
+  while (q < e && *q != ' ' && *q != '\t') ++q;
+  *we = q;
+  *p = q;
+  return true;
+}
+bool only_space(const char* p, const char* e) {
+  for (; p < e; ++p)
+    if (*p != ' ' && *p != '\t') return false;
+  return true;
+}
+
+// Group (u, v, c) triples into CSR, keeping per-row order of appearance
+// (the reference's adjacency-list append order).
+wbpr_status triples_to_csr(int32_t n, const std::vector<int32_t>& us,
+                           const std::vector<int32_t>& vs,
+                           const std::vector<int32_t>& cs, Csr* c) {
+  c->n = n;
+  c->m = (int64_t)us.size();
+  c->off.assign((size_t)n + 1, 0);
+  for (int32_t u : us) c->off[(size_t)u + 1]++;
+  for (int32_t i = 0; i < n; ++i) c->off[i + 1] += c->off[i];
+  c->dst.resize(us.size());
+  c->cap.resize(us.size());
+  std::vector<int32_t> cur(c->off.begin(), c->off.end() - 1);
+  for (size_t k = 0; k < us.size(); ++k) {
+    int32_t pos = cur[us[k]]++;
+    c->dst[pos] = vs[k];
+    c->cap[pos] = cs[k];
+  }
+  return WBPR_OK;
+}
+}  // namespace
+
+// -v 2 : DIMACS max-flow (reference graph.cpp:151-214).  1-based ids are
+// shifted to 0-based; "n ID s" / "n ID t" set the terminals; arcs keep file
+// order inside each tail row.
+wbpr_status read_dimacs(const char* path, Csr* c) {
+  std::string buf;
+  if (!slurp(path, &buf)) return WBPR_ERR_IO;
+  Lines L{buf.data(), buf.data() + buf.size()};
+  const char *b, *e;
+  int64_t n = -1, mdecl = -1;
+  std::vector<int32_t> us, vs, cs;
+  int32_t s = -1, t = -1;
+  while (L.next(&b, &e)) {
+    const char* p = b;
+    while (p < e && (*p == ' ' || *p == '\t')) ++p;
+    if (p >= e || *p == 'c') continue;
+    char kind = *p++;
+    if (kind == 'p') {
+      const char *wb, *we;
+      if (!parse_word(&p, e, &wb, &we)) return WBPR_ERR_IO;
+      if (!parse_int(&p, e, &n) || !parse_int(&p, e, &mdecl)) return WBPR_ERR_IO;
+      if (n <= 0 || n > std::numeric_limits<int32_t>::max() - 2 || mdecl < 0)
+        return WBPR_ERR_IO;
+      us.reserve((size_t)mdecl);
+      vs.reserve((size_t)mdecl);
+      cs.reserve((size_t)mdecl);
+    } else if (kind == 'n') {
+      int64_t id;
+      const char *wb, *we;
+      if (n < 0 || !parse_int(&p, e, &id) || !parse_word(&p, e, &wb, &we)) return WBPR_ERR_IO;
+      if (id < 1 || id > n) return WBPR_ERR_IO;
+      if (*wb == 's') s = (int32_t)(id - 1);
+      else if (*wb == 't') t = (int32_t)(id - 1);
+    } else if (kind == 'a') {
+      int64_t u, v, cap;
+      if (n < 0 || !parse_int(&p, e, &u) || !parse_int(&p, e, &v) || !parse_int(&p, e, &cap))
+        return WBPR_ERR_IO;
+      if (u < 1 || u > n || v < 1 || v > n || cap < 0 || cap > std::numeric_limits<int32_t>::max())
+        return WBPR_ERR_IO;
+      us.push_back((int32_t)(u - 1));
+      vs.push_back((int32_t)(v - 1));
+      cs.push_back((int32_t)cap);
+    } else {
+      return WBPR_ERR_IO;
+    }
+  }
+  if (n < 0) return WBPR_ERR_IO;
+  if ((int64_t)us.size() > std::numeric_limits<int32_t>::max()) return WBPR_ERR_OVERFLOW;
+  triples_to_csr((int32_t)n, us, vs, cs, c);
+  c->m_declared = mdecl;
+  c->s = s;
+  c->t = t;
+  return WBPR_OK;
+}
+
+// -v 0 : SNAP text (reference graph.cpp:28-67).  "# Nodes: N Edges: M" gives
+// n; other '#' lines are comments; every row is sorted by head; capacity 1.
+// Without the header, n = 1 + largest id seen.
+wbpr_status read_snap_txt(const char* path, Csr* c) {
+  std::string buf;
+  if (!slurp(path, &buf)) return WBPR_ERR_IO;
+  Lines L{buf.data(), buf.data() + buf.size()};
+  const char *b, *e;
+  int64_t n = -1, mdecl = -1, maxid = -1;
+  std::vector<int32_t> us, vs;
+  while (L.next(&b, &e)) {
+    const char* p = b;
+    while (p < e && (*p == ' ' || *p == '\t')) ++p;
+    if (p >= e) continue;
+    if (*p == '#') {
+      const char* k = std::strstr(p, "Nodes:");
+      if (k && k < e) {
+        const char* q = k + 6;
+        int64_t nn, mm;
+        if (!parse_int(&q, e, &nn)) return WBPR_ERR_IO;
+        const char* k2 = std::strstr(q, "Edges:");
+        if (!k2 || k2 >= e) return WBPR_ERR_IO;
+        q = k2 + 6;
+        if (!parse_int(&q, e, &mm)) return WBPR_ERR_IO;
+        if (nn <= 0 || nn > std::numeric_limits<int32_t>::max() - 2) return WBPR_ERR_IO;
+        n = nn;
+        mdecl = mm;
+      }
+      continue;
+    }
+    int64_t u, v;
+    if (!parse_int(&p, e, &u) || !parse_int(&p, e, &v)) return WBPR_ERR_IO;
+    if (u < 0 || v < 0 || u > std::numeric_limits<int32_t>::max() - 2 ||
+        v > std::numeric_limits<int32_t>::max() - 2)
+      return WBPR_ERR_IO;
+    maxid = std::max(maxid, std::max(u, v));
+    us.push_back((int32_t)u);
+    vs.push_back((int32_t)v);
+  }
+  if (n < 0) n = maxid + 1;
+  if (n <= 0) return WBPR_ERR_IO;
+  if (maxid >= n) return WBPR_ERR_IO;
+  std::vector<int32_t> cs(us.size(), 1);
+  triples_to_csr((int32_t)n, us, vs, cs, c);
+  for (int32_t u = 0; u < c->n; ++u)
+    std::sort(c->dst.begin() + c->off[u], c->dst.begin() + c->off[u + 1]);
+  c->m_declared = mdecl < 0 ? c->m : mdecl;
+  return WBPR_OK;
+}
+
+// -v 1 : SNAP binary (reference graph.cpp:219-233 writer, 292-314 reader):
+// int32 n, m, m_processed, destinations[m_processed], offsets[n+1]; cap 1.
+wbpr_status read_snap_bin(const char* path, Csr* c) {
+  std::string buf;
+  if (!slurp(path, &buf)) return WBPR_ERR_IO;
+  if (buf.size() < 12) return WBPR_ERR_IO;
+  int32_t hdr[3];
+  std::memcpy(hdr, buf.data(), 12);
+  int32_t n = hdr[0], mdecl = hdr[1], mp = hdr[2];
+  if (n <= 0 || mp < 0) return WBPR_ERR_IO;
+  size_t need = 12 + 4 * ((size_t)mp + (size_t)n + 1);
+  if (buf.size() < need) return WBPR_ERR_IO;
+  c->n = n;
+  c->m = mp;
+  c->m_declared = mdecl;
+  c->dst.resize((size_t)mp);
+  c->off.resize((size_t)n + 1);
+  std::memcpy(c->dst.data(), buf.data() + 12, 4 * (size_t)mp);
+  std::memcpy(c->off.data(), buf.data() + 12 + 4 * (size_t)mp, 4 * ((size_t)n + 1));
+  c->cap.assign((size_t)mp, 1);
+  wbpr_csr view{c->n, c->m, c->off.data(), c->dst.data(), c->cap.data(), -1, -1};
+  if (check_csr(&view) != WBPR_OK) return WBPR_ERR_IO;
+  return WBPR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Parallel LSD radix sort of 64-bit keys on the low `bits` bits.
+static void radix_sort_u64(std::vector<uint64_t>& a, int bits) {
+  std::vector<uint64_t> tmp(a.size());
+  const int T = host_threads();
+  const int64_t N = (int64_t)a.size();
+  for (int shift = 0; shift < bits; shift += 8) {
+    std::vector<std::vector<int64_t>> hist(T, std::vector<int64_t>(256, 0));
+    auto range = [&](int k, int64_t* b, int64_t* e) {
+      *b = N * k / T;
+      *e = N * (k + 1) / T;
+    };
+    {
+      std::vector<std::thread> th;
+      for (int k = 0; k < T; ++k)
+        th.emplace_back([&, k] {
+          int64_t b, e;
+          range(k, &b, &e);
+          auto& h = hist[k];
+          for (int64_t i = b; i < e; ++i) h[(a[i] >> shift) & 255]++;
+        });
+      for (auto& x : th) x.join();
+    }
+    int64_t base = 0;
+    for (int d = 0; d < 256; ++d)
+      for (int k = 0; k < T; ++k) {
+        int64_t c = hist[k][d];
+        hist[k][d] = base;
+        base += c;
+      }
+    {
+      std::vector<std::thread> th;
+      for (int k = 0; k < T; ++k)
+        th.emplace_back([&, k] {
+          int64_t b, e;
+          range(k, &b, &e);
+          auto& h = hist[k];
+          for (int64_t i = b; i < e; ++i) tmp[h[(a[i] >> shift) & 255]++] = a[i];
+        });
+      for (auto& x : th) x.join();
+    }
+    a.swap(tmp);
+  }
+}
+
+// Sorted unique (u << 32 | v) keys -> CSR with capacities from a stream
+// keyed by the final arc index.
+static void keys_to_csr(int32_t n, const std::vector<uint64_t>& keys, int32_t cap_lo,
+                        int32_t cap_hi, uint64_t seed, Csr* c) {
+  c->n = n;
+  c->m = (int64_t)keys.size();
+  c->m_declared = c->m;
+  c->off.assign((size_t)n + 1, 0);
+  c->dst.resize(keys.size());
+  c->cap.resize(keys.size());
+  for (uint64_t k : keys) c->off[(size_t)(k >> 32) + 1]++;
+  for (int32_t i = 0; i < n; ++i) c->off[i + 1] += c->off[i];
+  parallel_for((int64_t)keys.size(), [&](int64_t b, int64_t e, int) {
+    for (int64_t i = b; i < e; ++i) {
+      c->dst[i] = (int32_t)(keys[i] & 0xffffffffu);
+      Stream r(seed, 0xCA9ULL, (uint64_t)i);
+      c->cap[i] = (int32_t)r.range(cap_lo, cap_hi);
+    }
+  });
+}
+
+// ---------------------------------------------------------------------------
+// Generators.
+wbpr_status gen_genrmf(int32_t a, int32_t b, int32_t c1, int32_t c2, uint64_t seed, Csr* c) {
+  if (a < 1 || b < 1 || c1 < 0 || c2 < c1) return WBPR_ERR_INVALID_ARG;
+  int64_t A2 = (int64_t)a * a;
+  int64_t n = A2 * b;
+  if (n > std::numeric_limits<int32_t>::max() / 8) return WBPR_ERR_OVERFLOW;
+  if ((int64_t)c2 * A2 > std::numeric_limits<int32_t>::max()) return WBPR_ERR_OVERFLOW;
+  const int32_t incap = (int32_t)(c2 * A2);
+  // one seeded Fisher-Yates permutation per frame boundary
+  std::vector<int32_t> perm((size_t)A2);
+  c->n = (int32_t)n;
+  c->off.assign((size_t)n + 1, 0);
+  c->dst.clear();
+  c->cap.clear();
+  c->dst.reserve((size_t)(n * 5));
+  c->cap.reserve((size_t)(n * 5));
+  for (int32_t z = 0; z < b; ++z) {
+    if (z < b - 1) {
+      for (int64_t i = 0; i < A2; ++i) perm[i] = (int32_t)i;
+      Stream r(seed, 0x5EED0001ULL, (uint64_t)z);
+      for (int64_t i = A2 - 1; i > 0; --i) std::swap(perm[i], perm[r.range(0, i)]);
+    }
+    Stream rc(seed, 0x5EED0002ULL, (uint64_t)z);
+    int64_t base = A2 * z;
+    for (int32_t x = 0; x < a; ++x)
+      for (int32_t y = 0; y < a; ++y) {
+        int64_t loc = (int64_t)x * a + y;
+        int64_t v = base + loc;
+        if (z < b - 1) {
+          c->dst.push_back((int32_t)(base + A2 + perm[loc]));
+          c->cap.push_back((int32_t)rc.range(c1, c2));
+        }
+        const int dx[4] = {0, 0, 1, -1}, dy[4] = {1, -1, 0, 0};
+        for (int k = 0; k < 4; ++k) {
+          int32_t nx = x + dx[k], ny = y + dy[k];
+          if (nx < 0 || ny < 0 || nx >= a || ny >= a) continue;
+          c->dst.push_back((int32_t)(base + (int64_t)nx * a + ny));
+          c->cap.push_back(incap);
+        }
+        c->off[(size_t)v + 1] = (int32_t)c->dst.size();
+      }
+  }
+  c->m = (int64_t)c->dst.size();
+  c->m_declared = c->m;
+  c->s = 0;
+  c->t = (int32_t)(n - 1);
+  return WBPR_OK;
+}
+
+wbpr_status gen_rmat(int32_t scale, int32_t ef, double pa, double pb, double pc, int32_t cap_lo,
+                     int32_t cap_hi, uint64_t seed, Csr* c) {
+  if (scale < 1 || scale > 30 || ef < 1 || cap_lo < 0 || cap_hi < cap_lo) return WBPR_ERR_INVALID_ARG;
+  if (pa < 0 || pb < 0 || pc < 0 || pa + pb + pc > 1.0) return WBPR_ERR_INVALID_ARG;
+  const int64_t n = (int64_t)1 << scale;
+  const int64_t M = n * ef;
+  if (M > ((int64_t)1 << 31) - 1) return WBPR_ERR_OVERFLOW;
+  // integer quadrant thresholds on 32-bit draws
+  const uint64_t TA = (uint64_t)std::floor(pa * 4294967296.0);
+  const uint64_t TB = (uint64_t)std::floor((pa + pb) * 4294967296.0);
+  const uint64_t TC = (uint64_t)std::floor((pa + pb + pc) * 4294967296.0);
+  std::vector<uint64_t> keys((size_t)M);
+  parallel_for(M, [&](int64_t b, int64_t e, int) {
+    for (int64_t k = b; k < e; ++k) {
+      Stream r(seed, 0x4D41ULL, (uint64_t)k);
+      uint64_t u = 0, v = 0, w = 0;
+      for (int lvl = 0; lvl < scale; ++lvl) {
+        if ((lvl & 1) == 0) w = r.next();
+        uint64_t x = (lvl & 1) ? (w >> 32) : (w & 0xffffffffu);
+        uint64_t bit = (uint64_t)1 << (scale - 1 - lvl);
+        if (x >= TB) u |= bit;                      // quadrants c, d
+        if ((x >= TA && x < TB) || x >= TC) v |= bit;  // quadrants b, d
+      }
+      keys[k] = (u << 32) | v;
+    }
+  });
+  radix_sort_u64(keys, 32 + scale);
+  // drop self loops and duplicates
+  int64_t w = 0;
+  for (int64_t i = 0; i < M; ++i) {
+    uint64_t k = keys[i];
+    if ((k >> 32) == (k & 0xffffffffu)) continue;
+    if (w > 0 && keys[w - 1] == k) continue;
+    keys[w++] = k;
+  }
+  keys.resize((size_t)w);
+  keys_to_csr((int32_t)n, keys, cap_lo, cap_hi, seed, c);
+  // terminals: max out-degree and max in-degree (lowest id on ties)
+  std::vector<int32_t> indeg((size_t)n, 0);
+  for (int32_t v : c->dst) indeg[v]++;
+  int32_t s = 0, t = -1;
+  for (int32_t u = 1; u < (int32_t)n; ++u)
+    if (c->off[u + 1] - c->off[u] > c->off[s + 1] - c->off[s]) s = u;
+  for (int32_t u = 0; u < (int32_t)n; ++u)
+    if (u != s && (t < 0 || indeg[u] > indeg[t])) t = u;
+  c->s = s;
+  c->t = t;
+  return WBPR_OK;
+}
+
+wbpr_status gen_bipartite(int32_t L, int32_t R, double zs, int32_t dmax, uint64_t seed, Csr* c) {
+  if (L < 1 || R < 1 || dmax < 1 || zs <= 0) return WBPR_ERR_INVALID_ARG;
+  if ((int64_t)L + R + 2 > std::numeric_limits<int32_t>::max() / 2) return WBPR_ERR_OVERFLOW;
+  dmax = std::min(dmax, R);
+  // Zipf CDF over 1..dmax by plain sums (no libm beyond pow on exact ints)
+  std::vector<double> cdf((size_t)dmax);
+  double acc = 0;
+  for (int32_t k = 1; k <= dmax; ++k) {
+    double w = (zs == 2.0) ? 1.0 / ((double)k * (double)k) : 1.0 / std::pow((double)k, zs);
+    acc += w;
+    cdf[k - 1] = acc;
+  }
+  const int32_t n = L + R + 2, s = 0, t = L + R + 1;
+  std::vector<std::vector<int32_t>> rows((size_t)L);
+  parallel_for(L, [&](int64_t b, int64_t e, int) {
+    for (int64_t l = b; l < e; ++l) {
+      Stream r(seed, 0xB1ULL, (uint64_t)l);
+      double u = r.unit() * acc;
+      int32_t d = (int32_t)(std::upper_bound(cdf.begin(), cdf.end(), u) - cdf.begin()) + 1;
+      if (d > dmax) d = dmax;
+      auto& row = rows[l];
+      row.resize((size_t)d);
+      for (int32_t k = 0; k < d; ++k) row[k] = L + 1 + (int32_t)r.range(0, R - 1);
+      std::sort(row.begin(), row.end());
+      row.erase(std::unique(row.begin(), row.end()), row.end());
+    }
+  }, 4096);
+  c->n = n;
+  c->off.assign((size_t)n + 1, 0);
+  c->dst.clear();
+  c->cap.clear();
+  for (int32_t l = 1; l <= L; ++l) c->dst.push_back(l);
+  c->off[1] = L;
+  for (int32_t l = 0; l < L; ++l) {
+    for (int32_t v : rows[l]) c->dst.push_back(v);
+    c->off[l + 2] = (int32_t)c->dst.size();
+  }
+  for (int32_t r = 0; r < R; ++r) {
+    c->dst.push_back(t);
+    c->off[L + 2 + r] = (int32_t)c->dst.size();
+  }
+  c->off[n] = (int32_t)c->dst.size();
+  c->m = (int64_t)c->dst.size();
+  c->m_declared = c->m;
+  c->cap.assign(c->dst.size(), 1);
+  c->s = s;
+  c->t = t;
+  return WBPR_OK;
+}
+
+wbpr_status gen_layered(int32_t layers, int32_t width, int32_t dlo, int32_t dhi, int32_t clo,
+                        int32_t chi, uint64_t seed, Csr* c) {
+  if (layers < 1 || width < 1 || dlo < 1 || dhi < dlo || clo < 0 || chi < clo)
+    return WBPR_ERR_INVALID_ARG;
+  int64_t n64 = (int64_t)layers * width + 2;
+  if (n64 > std::numeric_limits<int32_t>::max() / 8) return WBPR_ERR_OVERFLOW;
+  const int32_t n = (int32_t)n64, s = 0, t = n - 1;
+  c->n = n;
+  c->off.assign((size_t)n + 1, 0);
+  c->dst.clear();
+  c->cap.clear();
+  Stream rs(seed, 0x1A0ULL, 0);
+  for (int32_t j = 0; j < width; ++j) {
+    c->dst.push_back(1 + j);
+    c->cap.push_back((int32_t)rs.range(clo, chi));
+  }
+  c->off[1] = (int32_t)c->dst.size();
+  std::vector<int32_t> tmp;
+  for (int32_t i = 0; i < layers; ++i)
+    for (int32_t j = 0; j < width; ++j) {
+      int32_t v = 1 + i * width + j;
+      Stream r(seed, 0x1A1ULL, (uint64_t)v);
+      if (i == layers - 1) {
+        c->dst.push_back(t);
+        c->cap.push_back((int32_t)r.range(clo, chi));
+      } else {
+        int32_t d = (int32_t)std::min<int64_t>(r.range(dlo, dhi), width);
+        tmp.clear();
+        for (int32_t k = 0; k < d; ++k) tmp.push_back(1 + (i + 1) * width + (int32_t)r.range(0, width - 1));
+        std::sort(tmp.begin(), tmp.end());
+        tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+        for (int32_t x : tmp) {
+          c->dst.push_back(x);
+          c->cap.push_back((int32_t)r.range(clo, chi));
+        }
+      }
+      c->off[(size_t)v + 1] = (int32_t)c->dst.size();
+    }
+  c->off[(size_t)n] = (int32_t)c->dst.size();
+  c->m = (int64_t)c->dst.size();
+  c->m_declared = c->m;
+  c->s = s;
+  c->t = t;
+  return WBPR_OK;
+}
+
+// Vision graph-cut grid.  field = seeded noise (Irwin-Hall sum of 12
+// uniforms, a unit-variance Gaussian stand-in) blurred with a sigma = 4
+// Gaussian and scaled to [0, 1].  n-link cap = round(1000 exp(-d^2 / 0.02)),
+// d = field difference; t-links round(1000 u), round(1000 (1 - u)),
+// u = clip(field + 0.2 * noise, 0, 1).
+wbpr_status gen_grid(int32_t w, int32_t h, uint64_t seed, Csr* c) {
+  if (w < 2 || h < 2) return WBPR_ERR_INVALID_ARG;
+  int64_t P = (int64_t)w * h;
+  if (P + 2 > std::numeric_limits<int32_t>::max() / 8) return WBPR_ERR_OVERFLOW;
+  auto gauss = [&](uint64_t tag, uint64_t i) {
+    Stream r(seed, tag, i);
+    double acc = 0;
+    for (int k = 0; k < 12; ++k) acc += r.unit();
+    return acc - 6.0;
+  };
+  std::vector<double> f((size_t)P), g((size_t)P);
+  for (int64_t i = 0; i < P; ++i) f[i] = gauss(0x6A1ULL, (uint64_t)i);
+  const int R = 12;
+  double kw[2 * R + 1], ks = 0;
+  for (int k = -R; k <= R; ++k) ks += (kw[k + R] = std::exp(-(double)(k * k) / (2.0 * 16.0)));
+  for (int k = 0; k <= 2 * R; ++k) kw[k] /= ks;
+  for (int32_t y = 0; y < h; ++y)
+    for (int32_t x = 0; x < w; ++x) {
+      double a = 0;
+      for (int k = -R; k <= R; ++k) {
+        int32_t xx = std::min(std::max(x + k, 0), w - 1);
+        a += kw[k + R] * f[(int64_t)y * w + xx];
+      }
+      g[(int64_t)y * w + x] = a;
+    }
+  for (int32_t y = 0; y < h; ++y)
+    for (int32_t x = 0; x < w; ++x) {
+      double a = 0;
+      for (int k = -R; k <= R; ++k) {
+        int32_t yy = std::min(std::max(y + k, 0), h - 1);
+        a += kw[k + R] * g[(int64_t)yy * w + x];
+      }
+      f[(int64_t)y * w + x] = a;
+    }
+  double lo = f[0], hi = f[0];
+  for (double v : f) { lo = std::min(lo, v); hi = std::max(hi, v); }
+  double span = hi > lo ? hi - lo : 1.0;
+  for (double& v : f) v = (v - lo) / span;
+  const int32_t n = (int32_t)(P + 2), s = (int32_t)P, t = (int32_t)P + 1;
+  auto ncap = [&](int64_t p, int64_t q) {
+    double d = f[p] - f[q];
+    return (int32_t)std::lround(1000.0 * std::exp(-d * d / 0.02));
+  };
+  // arc lists: pixel rows hold n-links (right, left, down, up) then p->t
+  c->n = n;
+  c->off.assign((size_t)n + 1, 0);
+  c->dst.clear();
+  c->cap.clear();
+  std::vector<int32_t> tcap((size_t)P), scap((size_t)P);
+  for (int64_t p = 0; p < P; ++p) {
+    double u = f[p] + 0.2 * gauss(0x6A2ULL, (uint64_t)p);
+    u = std::min(1.0, std::max(0.0, u));
+    scap[p] = (int32_t)std::lround(1000.0 * u);
+    tcap[p] = (int32_t)std::lround(1000.0 * (1.0 - u));
+  }
+  for (int32_t y = 0; y < h; ++y)
+    for (int32_t x = 0; x < w; ++x) {
+      int64_t p = (int64_t)y * w + x;
+      const int dx[4] = {1, -1, 0, 0}, dy[4] = {0, 0, 1, -1};
+      for (int k = 0; k < 4; ++k) {
+        int32_t nx = x + dx[k], ny = y + dy[k];
+        if (nx < 0 || ny < 0 || nx >= w || ny >= h) continue;
+        int64_t q = (int64_t)ny * w + nx;
+        c->dst.push_back((int32_t)q);
+        c->cap.push_back(ncap(p, q));
+      }
+      c->dst.push_back(t);
+      c->cap.push_back(tcap[p]);
+      c->off[(size_t)p + 1] = (int32_t)c->dst.size();
+    }
+  for (int64_t p = 0; p < P; ++p) {
+    c->dst.push_back((int32_t)p);
+    c->cap.push_back(scap[p]);
+  }
+  c->off[(size_t)s + 1] = (int32_t)c->dst.size();
+  c->off[(size_t)t + 1] = (int32_t)c->dst.size();
+  c->m = (int64_t)c->dst.size();
+  c->m_declared = c->m;
+  c->s = s;
+  c->t = t;
+  return WBPR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Residual builders.  Pairing is by construction (input arc i and its twin),
+// O(n + m), replacing the reference's first-match search, which costs
+// O(sum deg^2) and pairs antiparallel or parallel arcs with the wrong twin.
+wbpr_status build_bcsr16(const wbpr_csr* g, Bcsr16* out) {
+  const int32_t n = g->num_nodes;
+  const int64_t m = g->num_edges;
+  if (2 * m > std::numeric_limits<int32_t>::max()) return WBPR_ERR_OVERFLOW;
+  std::vector<int32_t> indeg((size_t)n, 0);
+  for (int64_t i = 0; i < m; ++i) indeg[g->destinations[i]]++;
+  out->row.assign((size_t)n + 1, 0);
+  for (int32_t u = 0; u < n; ++u)
+    out->row[u + 1] = out->row[u] + (g->offsets[u + 1] - g->offsets[u]) + indeg[u];
+  out->arc.resize((size_t)(4 * m));
+  out->arx.resize((size_t)(4 * m));
+  // reverse cursor of v starts after v's forward arcs
+  std::vector<int32_t> cur((size_t)n);
+  for (int32_t v = 0; v < n; ++v) cur[v] = out->row[v] + (g->offsets[v + 1] - g->offsets[v]);
+  for (int32_t u = 0; u < n; ++u) {
+    for (int32_t i = g->offsets[u]; i < g->offsets[u + 1]; ++i) {
+      int32_t v = g->destinations[i];
+      int32_t c = g->capacities ? g->capacities[i] : 1;
+      int32_t f = out->row[u] + (i - g->offsets[u]);
+      int32_t r = cur[v]++;
+      out->arc[2 * (size_t)f] = v;
+      out->arc[2 * (size_t)f + 1] = c;
+      out->arx[2 * (size_t)f] = r;
+      out->arx[2 * (size_t)f + 1] = c;
+      out->arc[2 * (size_t)r] = u;
+      out->arc[2 * (size_t)r + 1] = 0;
+      out->arx[2 * (size_t)r] = f;
+      out->arx[2 * (size_t)r + 1] = 0;
+    }
+  }
+  return WBPR_OK;
+}
+
+wbpr_status build_rcsr_dev(const wbpr_csr* g, Rcsr* out) {
+  const int32_t n = g->num_nodes;
+  const int64_t m = g->num_edges;
+  out->frow.assign(g->offsets, g->offsets + n + 1);
+  out->farc.resize((size_t)(2 * m));
+  out->fcap.resize((size_t)m);
+  out->rrow.assign((size_t)n + 1, 0);
+  out->rarc.resize((size_t)(2 * m));
+  for (int64_t i = 0; i < m; ++i) {
+    int32_t c = g->capacities ? g->capacities[i] : 1;
+    out->farc[2 * i] = g->destinations[i];
+    out->farc[2 * i + 1] = c;
+    out->fcap[i] = c;
+    out->rrow[(size_t)g->destinations[i] + 1]++;
+  }
+  for (int32_t v = 0; v < n; ++v) out->rrow[v + 1] += out->rrow[v];
+  std::vector<int32_t> cur(out->rrow.begin(), out->rrow.end() - 1);
+  for (int32_t u = 0; u < n; ++u)
+    for (int32_t i = g->offsets[u]; i < g->offsets[u + 1]; ++i) {
+      int32_t j = cur[g->destinations[i]]++;
+      out->rarc[2 * (size_t)j] = u;
+      out->rarc[2 * (size_t)j + 1] = i;
+    }
+  return WBPR_OK;
+}
+
+}  // namespace wbpr
+
+// ===========================================================================
+// C ABI
+using namespace wbpr;
+
+extern "C" {
+
+const char* wbpr_status_str(wbpr_status s) {
+  switch (s) {
+    case WBPR_OK: return "ok";
+    case WBPR_ERR_INVALID_ARG: return "invalid argument";
+    case WBPR_ERR_CUDA: return "CUDA error";
+    case WBPR_ERR_NO_CONVERGENCE: return "no convergence within the round/time budget";
+    case WBPR_ERR_OVERFLOW: return "int32 overflow of excess or arc index";
+    case WBPR_ERR_VERIFY: return "device verification failed";
+    case WBPR_ERR_IO: return "file missing, truncated or malformed";
+    case WBPR_ERR_NO_DEVICE: return "no CUDA device";
+    case WBPR_ERR_TIMEOUT: return "bounded grid-wide wait timed out";
+  }
+  return "unknown status";
+}
+
+int32_t wbpr_abi_version(void) { return WBPR_ABI_VERSION; }
+
+void wbpr_host_csr_free(wbpr_host_csr* g) {
+  if (!g) return;
+  std::free(g->offsets);
+  std::free(g->destinations);
+  std::free(g->capacities);
+  std::free(g);
+}
+
+wbpr_status wbpr_host_csr_copy(const wbpr_csr* in, wbpr_host_csr** out) {
+  wbpr_status st = check_csr(in);
+  if (st) return st;
+  Csr c;
+  c.n = in->num_nodes;
+  c.m = in->num_edges;
+  c.m_declared = in->num_edges;
+  c.off.assign(in->offsets, in->offsets + in->num_nodes + 1);
+  c.dst.assign(in->destinations, in->destinations + in->num_edges);
+  if (in->capacities) c.cap.assign(in->capacities, in->capacities + in->num_edges);
+  else c.cap.assign((size_t)in->num_edges, 1);
+  c.s = in->source;
+  c.t = in->sink;
+  return to_host_csr(std::move(c), out);
+}
+
+#define WBPR_READER(name, fn)                                 \
+  wbpr_status name(const char* path, wbpr_host_csr** out) {   \
+    if (!out) return WBPR_ERR_INVALID_ARG;                    \
+    *out = nullptr;                                           \
+    Csr c;                                                    \
+    wbpr_status st;                                           \
+    try {                                                     \
+      st = fn(path, &c);                                      \
+    } catch (const std::bad_alloc&) {                         \
+      return WBPR_ERR_IO;                                     \
+    }                                                         \
+    if (st) return st;                                        \
+    return to_host_csr(std::move(c), out);                    \
+  }
+WBPR_READER(wbpr_read_dimacs, read_dimacs)
+WBPR_READER(wbpr_read_snap_txt, read_snap_txt)
+WBPR_READER(wbpr_read_snap_bin, read_snap_bin)
+#undef WBPR_READER
+
+wbpr_status wbpr_write_snap_bin(const char* path, const wbpr_csr* g) {
+  wbpr_status st = check_csr(g);
+  if (st) return st;
+  FILE* f = path ? std::fopen(path, "wb") : nullptr;
+  if (!f) return WBPR_ERR_IO;
+  int32_t hdr[3] = {g->num_nodes, (int32_t)g->num_edges, (int32_t)g->num_edges};
+  bool ok = std::fwrite(hdr, 4, 3, f) == 3;
+  ok = ok && std::fwrite(g->destinations, 4, (size_t)g->num_edges, f) == (size_t)g->num_edges;
+  ok = ok && std::fwrite(g->offsets, 4, (size_t)g->num_nodes + 1, f) == (size_t)g->num_nodes + 1;
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? WBPR_OK : WBPR_ERR_IO;
+}
+
+wbpr_status wbpr_write_dimacs(const char* path, const wbpr_csr* g) {
+  wbpr_status st = check_csr(g);
+  if (st) return st;
+  FILE* f = path ? std::fopen(path, "w") : nullptr;
+  if (!f) return WBPR_ERR_IO;
+  std::fprintf(f, "p max %d %lld\n", g->num_nodes, (long long)g->num_edges);
+  if (g->source >= 0) std::fprintf(f, "n %d s\n", g->source + 1);
+  if (g->sink >= 0) std::fprintf(f, "n %d t\n", g->sink + 1);
+  for (int32_t u = 0; u < g->num_nodes; ++u)
+    for (int32_t i = g->offsets[u]; i < g->offsets[u + 1]; ++i)
+      std::fprintf(f, "a %d %d %d\n", u + 1, g->destinations[i] + 1,
+                   g->capacities ? g->capacities[i] : 1);
+  return std::fclose(f) == 0 ? WBPR_OK : WBPR_ERR_IO;
+}
+
+#define WBPR_GEN(call)                            \
+  if (!out) return WBPR_ERR_INVALID_ARG;          \
+  *out = nullptr;                                 \
+  Csr c;                                          \
+  wbpr_status st;                                 \
+  try {                                           \
+    st = call;                                    \
+  } catch (const std::bad_alloc&) {               \
+    return WBPR_ERR_OVERFLOW;                     \
+  }                                               \
+  if (st) return st;                              \
+  return to_host_csr(std::move(c), out);
+
+wbpr_status wbpr_gen_genrmf(int32_t a, int32_t b, int32_t c1, int32_t c2, uint64_t seed,
+                            wbpr_host_csr** out) {
+  WBPR_GEN(gen_genrmf(a, b, c1, c2, seed, &c))
+}
+wbpr_status wbpr_gen_rmat(int32_t scale, int32_t ef, double a, double b, double cc, int32_t lo,
+                          int32_t hi, uint64_t seed, wbpr_host_csr** out) {
+  WBPR_GEN(gen_rmat(scale, ef, a, b, cc, lo, hi, seed, &c))
+}
+wbpr_status wbpr_gen_bipartite(int32_t L, int32_t R, double zs, int32_t dmax, uint64_t seed,
+                               wbpr_host_csr** out) {
+  WBPR_GEN(gen_bipartite(L, R, zs, dmax, seed, &c))
+}
+wbpr_status wbpr_gen_layered(int32_t layers, int32_t width, int32_t dlo, int32_t dhi,
+                             int32_t clo, int32_t chi, uint64_t seed, wbpr_host_csr** out) {
+  WBPR_GEN(gen_layered(layers, width, dlo, dhi, clo, chi, seed, &c))
+}
+wbpr_status wbpr_gen_grid(int32_t w, int32_t h, uint64_t seed, wbpr_host_csr** out) {
+  WBPR_GEN(gen_grid(w, h, seed, &c))
+}
+#undef WBPR_GEN
+
+wbpr_status wbpr_build_rcsr(const wbpr_csr* g, int32_t* roffsets, int32_t* rdestinations,
+                            int32_t* flow_index) {
+  wbpr_status st = check_csr(g);
+  if (st) return st;
+  if (!roffsets || (g->num_edges && (!rdestinations || !flow_index))) return WBPR_ERR_INVALID_ARG;
+  Rcsr r;
+  st = build_rcsr_dev(g, &r);
+  if (st) return st;
+  std::memcpy(roffsets, r.rrow.data(), 4 * ((size_t)g->num_nodes + 1));
+  for (int64_t j = 0; j < g->num_edges; ++j) {
+    rdestinations[j] = r.rarc[2 * j];
+    flow_index[j] = r.rarc[2 * j + 1];
+  }
+  return WBPR_OK;
+}
+
+wbpr_status wbpr_build_bcsr(const wbpr_csr* g, int32_t* offsets, int32_t* destinations,
+                            int32_t* capacities, int32_t* backward_idx) {
+  wbpr_status st = check_csr(g);
+  if (st) return st;
+  if (!offsets || (g->num_edges && (!destinations || !capacities || !backward_idx)))
+    return WBPR_ERR_INVALID_ARG;
+  Bcsr16 b;
+  st = build_bcsr16(g, &b);
+  if (st) return st;
+  std::memcpy(offsets, b.row.data(), 4 * ((size_t)g->num_nodes + 1));
+  for (int64_t a = 0; a < 2 * g->num_edges; ++a) {
+    destinations[a] = b.arc[2 * a];
+    capacities[a] = b.arx[2 * a + 1];
+    backward_idx[a] = b.arx[2 * a];
+  }
+  return WBPR_OK;
+}
+
+wbpr_status wbpr_build_bcsr2(const wbpr_csr* g, int32_t* offsets, int32_t* destinations,
+                             int32_t* flows) {
+  wbpr_status st = check_csr(g);
+  if (st) return st;
+  if (!offsets || (g->num_edges && (!destinations || !flows))) return WBPR_ERR_INVALID_ARG;
+  Bcsr16 b;
+  st = build_bcsr16(g, &b);
+  if (st) return st;
+  std::memcpy(offsets, b.row.data(), 4 * ((size_t)g->num_nodes + 1));
+  for (int64_t a = 0; a < 2 * g->num_edges; ++a) {
+    destinations[a] = b.arc[2 * a];
+    flows[2 * a] = b.arc[2 * a + 1];
+    flows[2 * a + 1] = b.arx[2 * a];
+  }
+  return WBPR_OK;
+}
+
+}  // extern "C"
