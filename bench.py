@@ -221,7 +221,7 @@ def run_ours(args) -> None:
     d = Dist(world)
     if W.device_count() < 1:
         raise RuntimeError("bench needs a CUDA device")
-    w = WORKLOAD
+    w = dict(WORKLOAD, scale=args.scale)
     t0 = time.perf_counter()
     g = W.gen_rmat(w["scale"], w["edge_factor"], w["a"], w["b"], w["c"], w["cap_lo"], w["cap_hi"], w["seed"])
     gen_s = time.perf_counter() - t0
@@ -258,7 +258,7 @@ def run_ours(args) -> None:
     h2d = 32 * g.m + 8 * (g.n + 1)
     dg.close()
     # e2e through the C ABI from host buffers
-    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    e2e_steps = min(args.steps, args.e2e_steps)
     e2e_s = 0.0
     for _ in range(e2e_steps):
         t1 = time.perf_counter()
@@ -268,18 +268,21 @@ def run_ours(args) -> None:
         if r.flow != flow:
             raise AssertionError("e2e flow differs")
     e2e_s = d.max(e2e_s)
-    e2e = {"value": world * e2e_steps * g.m / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": 8 + 128, "steps": e2e_steps,
-           "path": "wbpr_graph_create (host BCSR build + H2D) + wbpr_solve + result read-back"}
+    e2e = None
+    if e2e_steps > 0:
+        e2e = {"value": world * e2e_steps * g.m / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": 8 + 128, "steps": e2e_steps,
+               "path": "wbpr_graph_create (host BCSR build + H2D) + wbpr_solve + result read-back"}
     if rank == 0:
-        cpu = cpu_baseline_once() if world == 1 else None
+        cpu = cpu_baseline_once() if world == 1 and not args.no_cpu_baseline else None
+        workload = "rmat22_ef16_cap1-100" if args.scale == 22 else f"rmat{args.scale}_ef16_cap1-100 (profiling size)"
         last = res[-1]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_s_max * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded R-MAT generator; the paper's SNAP graphs are not available)",
-            "config": {"workload": "rmat22_ef16_cap1-100", "n": g.n, "m": g.m, "s": g.s, "t": g.t,
+            "config": {"workload": workload, "n": g.n, "m": g.m, "s": g.s, "t": g.t,
                        "layout": args.layout, "algo": args.algo, "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (2.1 GB residual graph); no flush"},
             "flow": flow,
@@ -312,6 +315,9 @@ def main() -> None:
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--heavy-degree", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--scale", type=int, default=22, help="R-MAT scale (22 is the benchmark; smaller "
+                    "sizes are for profiling captures)")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU sample (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")

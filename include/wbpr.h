@@ -91,8 +91,10 @@ typedef struct wbpr_tuning {
   int32_t blocks_per_sm; /* resident blocks per SM for the persistent grid (0=max) */
   double gr_alpha;       /* global relabel after alpha*(n + arcs) units of work   */
   int64_t max_rounds;    /* push/relabel round budget (0 = unlimited)             */
-  double max_ms;         /* wall-clock budget of one solve in ms (0 = 600000)     */
+  double max_ms;         /* wall-clock budget of one solve in ms (0 = 120000)     */
   int32_t verify;        /* 1: run the device certificate check after the solve  */
+  int32_t trace;         /* 1: record a per-level / per-phase event trace         */
+  int32_t gr_rounds;     /* also relabel globally after this many rounds (0 = 48) */
   int32_t reserved;
 } wbpr_tuning;
 
@@ -112,6 +114,10 @@ typedef struct wbpr_result {
   int32_t global_relabels; /* BFS passes                                     */
   int32_t stranded;        /* vertices left with excess unable to reach t    */
   float launch_ms;         /* CUDA-event time of the persistent solver kernel */
+  float push_ms;           /* push phases of the rounds (rest: relabel)      */
+  int32_t bfs_levels;      /* BFS levels over all global relabels            */
+  int32_t bfs_bottom_up_levels; /* of which bottom-up                        */
+  uint64_t heavy_visits;   /* discharges of rows handled by a whole block    */
 } wbpr_result;
 
 typedef struct wbpr_verify_report {
@@ -120,7 +126,8 @@ typedef struct wbpr_verify_report {
   int32_t conservation_violations; /* vertices whose excess != in - out    */
   int32_t source_reaches_sink;/* 1 if a residual s->t path exists          */
   int32_t excess_reaches_sink;/* vertices with excess that reach t         */
-  int32_t reserved;
+  int32_t label_violations;   /* residual arcs u->v with h(u) > h(v) + 1 and
+                                 h(u) < n (solver labelling; informational) */
   int64_t cut_value;          /* capacity of the sink-side residual cut    */
   int64_t flow_value;         /* excess of the sink                        */
 } wbpr_verify_report;
@@ -208,6 +215,13 @@ wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo,
  * height[n], excess[n], and per input arc flow = cap - residual (m). */
 wbpr_status wbpr_read_state(wbpr_graph* g, int32_t* height, int32_t* excess,
                             int32_t* arc_flow);
+/* Event trace of the last solve run with tuning.trace = 1: the last `cap`
+ * records of 4 int64 {kind | aux << 32, ns since kernel start, v0, v1};
+ * kinds 1 BFS level (aux bottom-up, v0 frontier, v1 frontier arcs), 2 round
+ * start (aux round, v0 light list, v1 heavy entries << 32 | chunks), 3 pass A
+ * end, 4 push phase end, 5 relabel end (v0 next raw queue), 6 global relabel
+ * end.  Returns the number of records copied. */
+int32_t wbpr_read_trace(wbpr_graph* g, int64_t* out, int32_t cap);
 /* Certificate check on the device: capacities, conservation, and that no
  * residual path leads from s or from any excess vertex to t (so the value is
  * maximal), and cut value == flow value. */

@@ -32,6 +32,7 @@ def solve_all(g, combos=COMBOS, **kw):
                 r = d.solve(algo, g.s, g.t, tile=tile, **kw)
                 rep = d.verify()
                 assert rep["ok"], (layout, algo, tile, rep)
+                assert rep["label_violations"] == 0, (layout, algo, tile, rep)
                 out[(layout, algo, tile)] = r.flow
     return out
 
@@ -172,6 +173,35 @@ def test_budget_exhaustion_is_reported():
         assert ei.value.status == 3
         # the handle stays usable
         assert d.solve("vc", g.s, g.t).flow == oracle.fifo_pr(g.n, g.off, g.dst, g.cap, g.s, g.t)
+
+
+@pytest.mark.parametrize("tune", [
+    dict(heavy_degree=64), dict(heavy_degree=256, gr_alpha=2.0), dict(heavy_degree=256, gr_alpha=8.0),
+    dict(gr_alpha=0.05), dict(tile=8, heavy_degree=2048, gr_alpha=4.0), dict(blocks_per_sm=1, tile=16),
+    dict(block=128, heavy_degree=128, gr_alpha=3.0)])
+def test_tuning_space_exact_and_valid(tune):
+    """Every tuning gives the exact value, a valid final labelling and the
+    certificate, within a bounded time (a livelock would hit max_ms)."""
+    for g in (W.gen_rmat(16, 16, seed=5), W.gen_genrmf(12, 12, 1, 10000, 2)):
+        expected = oracle.fifo_pr(g.n, g.off, g.dst, g.cap, g.s, g.t)
+        for layout in ("bcsr", "rcsr"):
+            with W.DeviceGraph(g, layout) as d:
+                for algo in ("vc", "tc"):
+                    r = d.solve(algo, g.s, g.t, max_ms=20000.0, **tune)
+                    rep = d.verify()
+                    assert r.flow == expected, (layout, algo, tune)
+                    assert rep["ok"] and rep["label_violations"] == 0, (layout, algo, tune, rep)
+
+
+def test_sparse_work_tail_terminates():
+    """Rounds that do little work still lead to global relabels (a large
+    work threshold alone once left ping-ponging vertices climbing to n)."""
+    g = W.gen_rmat(20, 16, seed=1)
+    expected = oracle.fifo_pr(g.n, g.off, g.dst, g.cap, g.s, g.t)
+    with W.DeviceGraph(g, "bcsr") as d:
+        for tune in (dict(heavy_degree=256, gr_alpha=2.0), dict(gr_alpha=50.0)):
+            r = d.solve("vc", g.s, g.t, max_ms=30000.0, **tune)
+            assert r.flow == expected, tune
 
 
 def test_rmat20_certificate():

@@ -47,7 +47,8 @@ class HostCsr(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("tile", C.c_int32), ("block", C.c_int32), ("heavy_degree", C.c_int32),
                 ("blocks_per_sm", C.c_int32), ("gr_alpha", C.c_double), ("max_rounds", C.c_int64),
-                ("max_ms", C.c_double), ("verify", C.c_int32), ("reserved", C.c_int32)]
+                ("max_ms", C.c_double), ("verify", C.c_int32), ("trace", C.c_int32),
+                ("gr_rounds", C.c_int32), ("reserved", C.c_int32)]
 
 
 class Result(C.Structure):
@@ -55,7 +56,9 @@ class Result(C.Structure):
                 ("gr_ms", C.c_float), ("arcs_scanned", C.c_uint64), ("pushes", C.c_uint64),
                 ("relabels", C.c_uint64), ("vertex_visits", C.c_uint64), ("bfs_arcs", C.c_uint64),
                 ("bfs_vertices", C.c_uint64), ("alg_bytes", C.c_uint64), ("rounds", C.c_int32),
-                ("global_relabels", C.c_int32), ("stranded", C.c_int32), ("launch_ms", C.c_float)]
+                ("global_relabels", C.c_int32), ("stranded", C.c_int32), ("launch_ms", C.c_float),
+                ("push_ms", C.c_float), ("bfs_levels", C.c_int32), ("bfs_bottom_up_levels", C.c_int32),
+                ("heavy_visits", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -64,11 +67,11 @@ class Result(C.Structure):
 class VerifyReport(C.Structure):
     _fields_ = [("ok", C.c_int32), ("capacity_violations", C.c_int32),
                 ("conservation_violations", C.c_int32), ("source_reaches_sink", C.c_int32),
-                ("excess_reaches_sink", C.c_int32), ("reserved", C.c_int32),
+                ("excess_reaches_sink", C.c_int32), ("label_violations", C.c_int32),
                 ("cut_value", C.c_int64), ("flow_value", C.c_int64)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 LAYOUTS = {"rcsr": 0, "bcsr": 1, "bcsr2": 2}
@@ -83,6 +86,7 @@ EXPORTED = [
     "wbpr_build_rcsr", "wbpr_build_bcsr", "wbpr_build_bcsr2", "wbpr_graph_create",
     "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_solve", "wbpr_read_state",
     "wbpr_verify", "wbpr_mincut_adjoint", "wbpr_rcsr_preflow", "wbpr_rcsr_push_relabel",
+    "wbpr_read_trace",
 ]
 
 _lib = None
@@ -127,6 +131,7 @@ def lib() -> C.CDLL:
         "wbpr_graph_device_bytes": (C.c_int64, [vp]),
         "wbpr_solve": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int, C.POINTER(Tuning), C.POINTER(Result)]),
         "wbpr_read_state": (C.c_int, [vp, _i32p, _i32p, _i32p]),
+        "wbpr_read_trace": (C.c_int32, [vp, C.POINTER(C.c_int64), C.c_int32]),
         "wbpr_verify": (C.c_int, [vp, C.POINTER(VerifyReport)]),
         "wbpr_mincut_adjoint": (C.c_int, [vp, C.c_int32, _i8p, C.POINTER(C.c_float)]),
         "wbpr_rcsr_preflow": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, _i32p, _i32p, _i32p, _i32p,
@@ -349,6 +354,14 @@ class DeviceGraph:
         if t is not None:
             self.t = t
         return r
+
+    def trace(self, cap: int = 1 << 14) -> np.ndarray:
+        """Event records of the last solve run with trace=1: rows of
+        (kind, aux, t_ns, v0, v1)."""
+        buf = np.zeros((cap, 4), np.int64)
+        n = lib().wbpr_read_trace(self._h, buf.ctypes.data_as(C.POINTER(C.c_int64)), cap)
+        b = buf[:n]
+        return np.stack([b[:, 0] & 0xffffffff, b[:, 0] >> 32, b[:, 1], b[:, 2], b[:, 3]], axis=1)
 
     def verify(self) -> dict:
         rep = VerifyReport()

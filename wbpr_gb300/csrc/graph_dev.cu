@@ -54,13 +54,29 @@ struct wbpr_graph {
   int* rl_left = nullptr;
   int* lq[2] = {nullptr, nullptr};
   int* hq[2] = {nullptr, nullptr};
+  int* esnap = nullptr;
+  int* dq = nullptr;
+  int* dbase = nullptr;
+  int* dE = nullptr;
+  int* derem = nullptr;
+  int* dmin0 = nullptr;
+  int* hown = nullptr;
+  int* hsum = nullptr;
+  int* hmin = nullptr;
+  int4* bch = nullptr;
+  int n_bch = 0;
+  int n_td_heavy = 0;
   int* qraw = nullptr;
   int* fr[3] = {nullptr, nullptr, nullptr};
-  int* frh[3] = {nullptr, nullptr, nullptr};
+  int2* frh[3] = {nullptr, nullptr, nullptr};
+  int64_t n_td_items = 0;
   int* cls = nullptr;
   int* vlab = nullptr;
   int8_t* ind = nullptr;
   int* flow_tmp = nullptr;
+  long long* trace = nullptr;
+  int trace_cap = 0;
+  int trace_n = 0;
   int n_light = 0, n_medium = 0, n_heavy = 0;
   long long total_deg = 0;
   double avg_deg = 0;
@@ -119,33 +135,37 @@ struct VerifyAcc {
   int cap_viol;
   int cons_viol;
   int excess_reach;
-  int pad;
+  int label_viol;
   long long cut;
 };
 
 // warp per vertex: capacity pair invariant, conservation, cut of the sink side
 __global__ void verify_bcsr(const int* row, const int2* arc, const int2* arx, const int* e,
-                            const int* lab, int n, int s, int t, VerifyAcc* out) {
+                            const int* lab, const int* h, int n, int s, int t, VerifyAcc* out) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   for (int v = gw; v < n; v += nw) {
     long long net = 0, cut = 0;
-    int bad = 0;
+    int bad = 0, lv = 0;
     const bool vin = lab[v] < n;
+    const int hv = h[v];
     for (int a = row[v] + lane; a < row[v + 1]; a += 32) {
       const int2 r = arc[a], x = arx[a];
       const int2 rr = arc[x.x], xr = arx[x.x];
       if (r.y < 0 || (long long)r.y + rr.y != (long long)x.y + xr.y) ++bad;
       net += (long long)r.y - x.y;
       if (!vin && x.y > 0 && lab[r.x] < n) cut += x.y;
+      if (r.y > 0 && v != s && hv < n && hv > h[r.x] + 1) ++lv;
     }
     for (int o = 16; o > 0; o >>= 1) {
       net += __shfl_down_sync(0xffffffffu, net, o);
       cut += __shfl_down_sync(0xffffffffu, cut, o);
       bad += __shfl_down_sync(0xffffffffu, bad, o);
+      lv += __shfl_down_sync(0xffffffffu, lv, o);
     }
     if (lane == 0) {
       if (bad) atomicAdd(&out->cap_viol, bad);
+      if (lv) atomicAdd(&out->label_viol, lv);
       if (v != s && net != (long long)e[v]) atomicAdd(&out->cons_viol, 1);
       if (cut) atomicAdd((unsigned long long*)&out->cut, (unsigned long long)cut);
       if (v != s && v != t && e[v] > 0 && vin) atomicAdd(&out->excess_reach, 1);
@@ -154,29 +174,38 @@ __global__ void verify_bcsr(const int* row, const int2* arc, const int2* arx, co
 }
 
 __global__ void verify_rcsr(const int* frow, const int2* farc, const int* fcb, const int* fcap,
-                            const int* rrow, const int2* rarc, const int* e, const int* lab, int n,
-                            int s, int t, VerifyAcc* out) {
+                            const int* rrow, const int2* rarc, const int* e, const int* lab, const int* h,
+                            int n, int s, int t, VerifyAcc* out) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   for (int v = gw; v < n; v += nw) {
     long long net = 0, cut = 0;
-    int bad = 0;
+    int bad = 0, lv = 0;
     const bool vin = lab[v] < n;
+    const int hv = h[v];
     for (int i = frow[v] + lane; i < frow[v + 1]; i += 32) {
       const int2 r = farc[i];
       const int b = fcb[i], c = fcap[i];
       if (r.y < 0 || b < 0 || (long long)r.y + b != c) ++bad;
       net -= b;
       if (!vin && c > 0 && lab[r.x] < n) cut += c;
+      if (r.y > 0 && v != s && hv < n && hv > h[r.x] + 1) ++lv;
     }
-    for (int j = rrow[v] + lane; j < rrow[v + 1]; j += 32) net += fcb[rarc[j].y];
+    for (int j = rrow[v] + lane; j < rrow[v + 1]; j += 32) {
+      const int2 q = rarc[j];
+      const int f = fcb[q.y];
+      net += f;
+      if (f > 0 && v != s && hv < n && hv > h[q.x] + 1) ++lv;
+    }
     for (int o = 16; o > 0; o >>= 1) {
       net += __shfl_down_sync(0xffffffffu, net, o);
       cut += __shfl_down_sync(0xffffffffu, cut, o);
       bad += __shfl_down_sync(0xffffffffu, bad, o);
+      lv += __shfl_down_sync(0xffffffffu, lv, o);
     }
     if (lane == 0) {
       if (bad) atomicAdd(&out->cap_viol, bad);
+      if (lv) atomicAdd(&out->label_viol, lv);
       if (v != s && net != (long long)e[v]) atomicAdd(&out->cons_viol, 1);
       if (cut) atomicAdd((unsigned long long*)&out->cut, (unsigned long long)cut);
       if (v != s && v != t && e[v] > 0 && vin) atomicAdd(&out->excess_reach, 1);
@@ -267,6 +296,7 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   const int n = g->n;
   const int64_t m = g->m;
   std::vector<int32_t> deg((size_t)n);
+  std::vector<int32_t> row_host, rrow_host;
   if (g->layout == WBPR_LAYOUT_BCSR) {
     wbpr::Bcsr16 b;
     TRY(wbpr::build_bcsr16(in, &b));
@@ -279,6 +309,7 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
       TRYC(cudaMemcpy(g->arx, b.arx.data(), 16 * (size_t)m, cudaMemcpyHostToDevice));
     }
     for (int u = 0; u < n; ++u) deg[u] = b.row[u + 1] - b.row[u];
+    row_host.swap(b.row);
   } else {
     wbpr::Rcsr r;
     TRY(wbpr::build_rcsr_dev(in, &r));
@@ -297,6 +328,7 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
       TRYC(cudaMemset(g->fcb, 0, 4 * (size_t)m));
     }
     for (int u = 0; u < n; ++u) deg[u] = (r.frow[u + 1] - r.frow[u]) + (r.rrow[u + 1] - r.rrow[u]);
+    rrow_host.swap(r.rrow);
   }
   TRY(dalloc(g, &g->ioff, (size_t)n + 1));
   TRYC(cudaMemcpy(g->ioff, in->offsets, 4 * ((size_t)n + 1), cudaMemcpyHostToDevice));
@@ -321,10 +353,47 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   g->avg_deg = n ? (double)g->total_deg / std::max<int64_t>(1, g->n_light + g->n_medium + g->n_heavy) : 0;
   TRY(dalloc(g, &g->cls, cls.size()));
   if (!cls.empty()) TRYC(cudaMemcpy(g->cls, cls.data(), 4 * cls.size(), cudaMemcpyHostToDevice));
+  // static chunks of the long rows for the bottom-up BFS, and the bound on
+  // the chunk items of the push phase (every row cut into kChunk pieces)
+  {
+    std::vector<int4> bch;
+    int64_t max_chunks = 1;
+    std::vector<int32_t> seg_b(2), seg_e(2);
+    for (int u = 0; u < n; ++u) {
+      const int d = deg[u];
+      max_chunks += (d + kChunk - 1) / kChunk;
+      if (d > kTdHeavy) {
+        ++g->n_td_heavy;
+        g->n_td_items += (d + kTdChunk - 1) / kTdChunk;
+      }
+      if (d <= kHeavyDeg) continue;
+      int nseg = 1;
+      if (g->layout == WBPR_LAYOUT_BCSR) {
+        seg_b[0] = row_host[u];
+        seg_e[0] = row_host[u] + d;
+      } else {
+        nseg = 2;
+        seg_b[0] = in->offsets[u];
+        seg_e[0] = in->offsets[u + 1];
+        seg_b[1] = rrow_host[u];
+        seg_e[1] = rrow_host[u + 1];
+      }
+      for (int k = 0; k < nseg; ++k)
+        for (int b = seg_b[k]; b < seg_e[k]; b += kChunk)
+          bch.push_back(make_int4(u, k, b, std::min(seg_e[k], b + kChunk)));
+    }
+    g->n_bch = (int)bch.size();
+    TRY(dalloc(g, &g->bch, bch.size()));
+    if (!bch.empty()) TRYC(cudaMemcpy(g->bch, bch.data(), sizeof(int4) * bch.size(), cudaMemcpyHostToDevice));
+    TRY(dalloc(g, &g->hown, (size_t)max_chunks));
+    TRY(dalloc(g, &g->hsum, (size_t)max_chunks));
+    TRY(dalloc(g, &g->hmin, (size_t)max_chunks));
+  }
   int** vec[] = {&g->h, &g->e, &g->rl_min, &g->rl_left, &g->lq[0], &g->lq[1], &g->hq[0], &g->hq[1],
+                 &g->esnap, &g->dq, &g->dbase, &g->dE, &g->derem, &g->dmin0,
                  &g->qraw, &g->fr[0], &g->fr[1], &g->fr[2], &g->vlab};
   for (int** p : vec) TRY(dalloc(g, p, (size_t)n));
-  for (int k = 0; k < 3; ++k) TRY(dalloc(g, &g->frh[k], (size_t)g->n_heavy + 1));
+  for (int k = 0; k < 3; ++k) TRY(dalloc(g, &g->frh[k], (size_t)g->n_td_items + 1));
   TRY(dalloc(g, &g->ctl, 1));
   TRY(dalloc(g, &g->st, 1));
   TRYC(cudaMemset(g->h, 0, 4 * (size_t)n));
@@ -346,6 +415,17 @@ void fill_common(wbpr_graph* g, Params<Topo>& p) {
     p.lq[k] = g->lq[k];
     p.hq[k] = g->hq[k];
   }
+  p.esnap = g->esnap;
+  p.dq = g->dq;
+  p.dbase = g->dbase;
+  p.dE = g->dE;
+  p.derem = g->derem;
+  p.dmin0 = g->dmin0;
+  p.hown = g->hown;
+  p.hsum = g->hsum;
+  p.hmin = g->hmin;
+  p.bch = g->bch;
+  p.n_bch = g->n_bch;
   p.qraw = g->qraw;
   for (int k = 0; k < 3; ++k) {
     p.fr[k] = g->fr[k];
@@ -385,10 +465,12 @@ struct RunCfg {
   int blocks_per_sm;
   int heavy_deg;
   unsigned long long gr_threshold;
+  int gr_rounds;
   long long max_rounds;
   unsigned long long budget_ns;
   int bfs_dir, bfs_root, bfs_excl;
   int* lab;
+  bool trace;
 };
 
 template <class Topo>
@@ -402,12 +484,22 @@ wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch
   p.mode = rc.mode;
   p.heavy_deg = rc.heavy_deg;
   p.gr_threshold = rc.gr_threshold;
+  p.gr_rounds = rc.gr_rounds;
   p.max_rounds = rc.max_rounds;
   p.budget_ns = rc.budget_ns;
   p.bfs_dir = rc.bfs_dir;
   p.bfs_root = rc.bfs_root;
   p.bfs_excl = rc.bfs_excl;
   if (rc.lab) p.lab = rc.lab;
+  if (rc.trace) {
+    if (!g->trace) {
+      g->trace_cap = 1 << 14;
+      wbpr_status st = dalloc(g, &g->trace, 4 * (size_t)g->trace_cap);
+      if (st) return st;
+    }
+    p.trace = g->trace;
+    p.trace_cap = g->trace_cap;
+  }
   const int occ = occupancy_pr(&p, rc.tile, rc.threads);
   if (occ <= 0) {
     g_last_error = "persistent kernel does not fit on an SM";
@@ -425,6 +517,7 @@ wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch
   CK(cudaMemcpyAsync(hs, g->st, sizeof(Stats), cudaMemcpyDeviceToHost, g->stream));
   CK(cudaStreamSynchronize(g->stream));
   if (launch_ms) CK(cudaEventElapsedTime(launch_ms, g->ev2, g->ev3));
+  g->trace_n = rc.trace ? hs->trace_n : 0;
   if (hc.err) return (wbpr_status)hc.err;
   return WBPR_OK;
 }
@@ -437,7 +530,7 @@ wbpr_status run(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch_ms = n
 void tuning_defaults(wbpr_tuning* t) {
   std::memset(t, 0, sizeof(*t));
   t->gr_alpha = 1.0;
-  t->max_ms = 600000.0;
+  t->max_ms = 120000.0;
 }
 
 wbpr_status make_cfg(wbpr_graph* g, int s, int t, wbpr_algo algo, const wbpr_tuning* tu, RunCfg* rc) {
@@ -456,12 +549,14 @@ wbpr_status make_cfg(wbpr_graph* g, int s, int t, wbpr_algo algo, const wbpr_tun
   int threads = tu->block ? tu->block : 256;
   if (threads < 64 || threads > 256 || threads % 32) return WBPR_ERR_INVALID_ARG;
   rc->threads = threads;
-  rc->blocks_per_sm = tu->blocks_per_sm > 0 ? tu->blocks_per_sm : 2;
+  rc->blocks_per_sm = tu->blocks_per_sm > 0 ? tu->blocks_per_sm : 0;
   rc->heavy_deg = tu->heavy_degree > 0 ? tu->heavy_degree : (algo == WBPR_ALGO_TC ? 128 : 1024);
   const double alpha = tu->gr_alpha > 0 ? tu->gr_alpha : 1.0;
   rc->gr_threshold = (unsigned long long)(alpha * ((double)g->n + (double)g->total_deg)) + 1;
+  rc->gr_rounds = tu->gr_rounds > 0 ? tu->gr_rounds : 48;
   rc->max_rounds = tu->max_rounds;
-  const double ms = tu->max_ms > 0 ? tu->max_ms : 600000.0;
+  rc->trace = tu->trace != 0;
+  const double ms = tu->max_ms > 0 ? tu->max_ms : 120000.0;
   rc->budget_ns = (unsigned long long)(ms * 1e6);
   rc->bfs_excl = -1;
   return WBPR_OK;
@@ -557,6 +652,10 @@ wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, cons
     out->stranded = hs.stranded;
     out->alg_bytes = alg_bytes(g, hs);
     out->launch_ms = launch_ms;
+    out->push_ms = (float)(hs.push_ns * 1e-6);
+    out->bfs_levels = hs.bfs_levels;
+    out->bfs_bottom_up_levels = hs.bu_levels;
+    out->heavy_visits = hs.heavy_visits;
   }
   g->s = s;
   g->t = t;
@@ -567,6 +666,22 @@ wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, cons
     if (!rep.ok) return WBPR_ERR_VERIFY;
   }
   return WBPR_OK;
+}
+
+int32_t wbpr_read_trace(wbpr_graph* g, int64_t* out, int32_t cap) {
+  if (!g || !out || cap <= 0 || !g->trace) return 0;
+  // the device keeps the last trace_cap records in a ring
+  const int total = g->trace_n, kept = std::min(total, g->trace_cap);
+  std::vector<long long> ring(4 * (size_t)g->trace_cap);
+  if (kept > 0 && cudaMemcpy(ring.data(), g->trace, 32 * (size_t)g->trace_cap, cudaMemcpyDeviceToHost) !=
+                      cudaSuccess)
+    return 0;
+  const int n = std::min(cap, kept);
+  for (int i = 0; i < n; ++i) {
+    const int src = (total - n + i) % g->trace_cap;
+    std::memcpy(out + 4 * (size_t)i, ring.data() + 4 * (size_t)src, 32);
+  }
+  return n;
 }
 
 wbpr_status wbpr_read_state(wbpr_graph* g, int32_t* height, int32_t* excess, int32_t* arc_flow) {
@@ -614,9 +729,9 @@ wbpr_status wbpr_verify(wbpr_graph* g, wbpr_verify_report* rep) {
   cudaMemsetAsync(dacc, 0, sizeof(VerifyAcc), g->stream);
   if (g->layout == WBPR_LAYOUT_RCSR)
     verify_rcsr<<<g->sms * 4, 256, 0, g->stream>>>(g->frow, g->farc, g->fcb, g->fcap, g->rrow, g->rarc,
-                                                   g->e, g->vlab, g->n, g->s, g->t, dacc);
+                                                   g->e, g->vlab, g->h, g->n, g->s, g->t, dacc);
   else
-    verify_bcsr<<<g->sms * 4, 256, 0, g->stream>>>(g->row, g->arc, g->arx, g->e, g->vlab, g->n, g->s,
+    verify_bcsr<<<g->sms * 4, 256, 0, g->stream>>>(g->row, g->arc, g->arx, g->e, g->vlab, g->h, g->n, g->s,
                                                    g->t, dacc);
   VerifyAcc h;
   int ls = 0, et = 0;
@@ -633,6 +748,7 @@ wbpr_status wbpr_verify(wbpr_graph* g, wbpr_verify_report* rep) {
   rep->capacity_violations = h.cap_viol;
   rep->conservation_violations = h.cons_viol;
   rep->excess_reaches_sink = h.excess_reach;
+  rep->label_violations = h.label_viol;
   rep->source_reaches_sink = ls < g->n ? 1 : 0;
   rep->cut_value = h.cut;
   rep->flow_value = et;

@@ -189,11 +189,6 @@ bool parse_word(const char** p, const char* e, const char** wb, const char** we)
   *p = q;
   return true;
 }
-bool only_space(const char* p, const char* e) {
-  for (; p < e; ++p)
-    if (*p != ' ' && *p != '\t') return false;
-  return true;
-}
 
 // Group (u, v, c) triples into CSR, keeping per-row order of appearance
 // (the reference's adjacency-list append order).

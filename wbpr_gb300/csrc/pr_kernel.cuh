@@ -64,12 +64,15 @@ struct Ctl {
   int qraw_count[2];
   int light_next;
   int heavy_next;
+  int deep_next_a;
+  int deep_next_b;
   int fcount[3];
   int fhcount[3];
   long long fdeg[3];
   unsigned long long work[2];  // work done in rounds of even / odd parity
+  unsigned long long dpack;    // deep list of the round: (entries << 32) | chunk items
   int bfs_heavy_next[3];
-  int pad[5];
+  int pad[1];
 };
 
 struct Stats {
@@ -81,10 +84,17 @@ struct Stats {
   unsigned long long bfs_vertices;
   unsigned long long gr_ns;
   unsigned long long round_ns;
+  unsigned long long push_ns;
+  unsigned long long heavy_visits;
   int rounds;
   int grs;
   int stranded;
   int status;
+  int bfs_levels;
+  int bu_levels;
+  int trace_n;
+  int pad2;
+  unsigned long long t0;
 };
 
 __device__ __forceinline__ unsigned long long gtime() {
@@ -93,6 +103,20 @@ __device__ __forceinline__ unsigned long long gtime() {
   return t;
 }
 __device__ __forceinline__ int ldv(const int* p) { return *(const volatile int*)p; }
+
+__device__ __forceinline__ void trace_rec(long long* tr, int cap, int* n, unsigned long long t0, int kind,
+                                          int aux, long long v0, long long v1) {
+  if (!tr) return;
+  const int i = *n;
+  *n = i + 1;
+  long long* r = tr + 4 * (long long)(i % cap);
+  r[0] = (long long)kind | ((long long)aux << 32);
+  r[1] = (long long)(gtime() - t0);
+  r[2] = v0;
+  r[3] = v1;
+}
+#define TRACE(p, kind, aux, v0, v1) \
+  trace_rec((p).trace, (p).trace_cap, &(p).st->trace_n, (p).st->t0, (kind), (aux), (v0), (v1))
 __device__ __forceinline__ long long ldv64(const long long* p) { return *(const volatile long long*)p; }
 
 // ---------------------------------------------------------------------------
@@ -184,18 +208,30 @@ struct Params {
   int* rl_min;
   int* rl_left;
   int* lq[2];
-  int* hq[2];
+  int* hq[2];      // heavy active vertices (rows longer than heavy_deg)
+  int* esnap;      // excess of each active vertex when it was filed for the round
+  int* dq;         // deep entries: heavy vertices with excess left after chunk 0
+  int* dbase;      //   first chunk item of the entry
+  int* dE;         //   excess snapshot of the round
+  int* derem;      //   excess left after chunk 0
+  int* dmin0;      //   min label over chunk 0's remaining residual arcs
+  int* hown;       // chunk item -> deep entry
+  int* hsum;       // chunk item -> admissible residual (saturated)
+  int* hmin;       // chunk item -> min label over other residual arcs
   int* qraw;
   int* fr[3];
-  int* frh[3];
+  int2* frh[3];    // long frontier rows as chunk items {vertex, chunk index}
   const int* cls;  // vertex ids: [0, n_light) light, then medium, then heavy
   int n_light;
   int n_medium;
   int n_heavy;
+  const int4* bch; // static 2048-arc chunks {v, segment, begin, end} of heavy rows
+  int n_bch;
   Ctl* ctl;
   Stats* st;
   long long total_deg;
   unsigned long long gr_threshold;
+  int gr_rounds;  // global relabel at the latest after this many rounds
   long long max_rounds;
   unsigned long long budget_ns;
   unsigned long long bar_timeout_ns;
@@ -204,7 +240,12 @@ struct Params {
   int bfs_dir;   // 0: vertices that reach the root (to sink); 1: reached from the root
   int bfs_root;
   int bfs_excl;  // vertex the BFS never labels (the source during a solve), or -1
+  long long* trace;  // optional event records {kind | aux << 32, t_ns, v0, v1}
+  int trace_cap;
 };
+
+// Optional event trace (written by global thread 0 only; count in Stats).
+enum TraceKind : int { kTrLevel = 1, kTrRound = 2, kTrPassA = 3, kTrPassB = 4, kTrRelabel = 5, kTrGrEnd = 6 };
 
 // Per-block counters, flushed to Stats once per phase.
 struct BlockAcc {
@@ -355,8 +396,11 @@ __device__ __forceinline__ void discharge_tile(const Params<Topo>& p, int u, int
     bool self = true;
     if (D > 0) self = (atomicSub(p.e + u, D) - D) > 0;
     if (erem > 0) {
+      // Pushes into u during this phase open arcs u->w with label(w) =
+      // label(u) + 1 that the scan may not have seen; the relabel phase
+      // detects them by comparing excess with (filing snapshot - pushed).
       p.rl_min[u] = minh;
-      p.rl_left[u] = (int)erem;
+      p.rl_left[u] = __ldcg(p.esnap + u) - D;
     }
     if (self) append(p.qraw, rawcnt, u);
     atomicAdd(&acc.scanned, scanned);
@@ -364,143 +408,353 @@ __device__ __forceinline__ void discharge_tile(const Params<Topo>& p, int u, int
   }
 }
 
-// Push phase for one heavy row: the whole block walks the row in slabs of
-// blockDim * kItems arcs (loads issued together), block-wide saturating scan.
-constexpr int kItems = 4;
+// ---------------------------------------------------------------------------
+// Heavy rows (longer than heavy_deg) are cut into chunks of kChunk arcs that
+// different blocks process in two passes of the push phase:
+//   pass A  every chunk sums the residual capacity of its admissible arcs
+//           (saturated at the vertex's excess) and takes the min label over
+//           its other residual arcs;
+//   -- grid barrier --
+//   pass B  chunk c of u receives allot = min(sum_c, E - sum of earlier
+//           chunks) and pushes it along its admissible arcs in arc order;
+//           the last chunk settles excess(u) and the relabel record.
+// Total pushed = min(E, sum of all chunks), in arc order: the same pushes a
+// single thread walking the row would make.  Labels are frozen across both
+// passes, and admissible residuals of u change only by u's own pushes, so the
+// two passes see the same admissible set.
+constexpr int kItems = 8;
+constexpr int kChunk = 2048;
+
+struct VRow {  // a row as one virtual range [0, deg): segment 0 then segment 1
+  int b0, d0, b1, deg;
+};
 
 template <class Topo>
-__device__ void discharge_block(const Params<Topo>& p, int u, int* rawcnt, BlockAcc& acc) {
-  __shared__ unsigned s_wsum[32];
-  __shared__ unsigned s_tot;
-  __shared__ int s_eu;
-  __shared__ int s_min[32];
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
-  const int hu = __ldcg(p.lab + u);
-  if (tid == 0) s_eu = ldv(p.e + u);
-  __syncthreads();
-  const int eu = s_eu;
-  __syncthreads();
-  if (eu <= 0 || hu >= p.n) return;
-  unsigned erem = (unsigned)eu;
-  const int th = hu - 1;
-  int minh = kBig;
-  int npush = 0;
-  unsigned long long scanned = 0;
-  for (int k = 0; k < Topo::kSeg && erem > 0; ++k) {
-    int b, e;
-    p.g.seg(u, k, b, e);
-    for (int base = b; base < e && erem > 0; base += blockDim.x * kItems) {
-      int dst[kItems], cf[kItems], hv[kItems];
+__device__ __forceinline__ VRow vrow(const Topo& g, int u) {
+  VRow r;
+  int e0, b1 = 0, e1 = 0;
+  g.seg(u, 0, r.b0, e0);
+  if (Topo::kSeg > 1) g.seg(u, 1, b1, e1);
+  r.d0 = e0 - r.b0;
+  r.b1 = b1;
+  r.deg = r.d0 + (e1 - b1);
+  return r;
+}
+__device__ __forceinline__ void vidx(const VRow& r, int vi, int& k, int& a) {
+  if (vi < r.d0) {
+    k = 0;
+    a = r.b0 + vi;
+  } else {
+    k = 1;
+    a = r.b1 + (vi - r.d0);
+  }
+}
+
+// Block-wide inclusive scan of x (saturated at cap); returns the inclusive
+// value of this thread and writes the exclusive one to *excl, the total to
+// *total.  All threads of the block must call it.
+__device__ __forceinline__ unsigned block_scan_sat(unsigned x, unsigned cap, unsigned* excl,
+                                                   unsigned* total) {
+  __shared__ unsigned s_w[32];
+  __shared__ unsigned s_t;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned incl = x > cap ? cap : x;
 #pragma unroll
-      for (int j = 0; j < kItems; ++j) {
-        const int a = base + j * blockDim.x + tid;
-        dst[j] = 0;
-        cf[j] = 0;
-        if (a < e) p.g.load(k, a, dst[j], cf[j]);
+  for (int d = 1; d < 32; d <<= 1) {
+    unsigned y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) {
+      incl += y;
+      if (incl > cap) incl = cap;
+    }
+  }
+  unsigned prevw = __shfl_up_sync(0xffffffffu, incl, 1);
+  if (lane == 0) prevw = 0;
+  if (lane == 31) s_w[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    unsigned v = lane < nw ? s_w[lane] : 0u;
+    unsigned inc2 = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      unsigned y = __shfl_up_sync(0xffffffffu, inc2, d);
+      if (lane >= d) {
+        inc2 += y;
+        if (inc2 > cap) inc2 = cap;
       }
+    }
+    unsigned exc2 = __shfl_up_sync(0xffffffffu, inc2, 1);
+    if (lane == 0) exc2 = 0;
+    if (lane < nw) s_w[lane] = exc2;
+    if (lane == nw - 1) s_t = inc2;
+  }
+  __syncthreads();
+  const unsigned wpre = s_w[wid];
+  unsigned ib = wpre + incl, pb = wpre + prevw;
+  if (ib > cap) ib = cap;
+  if (pb > cap) pb = cap;
+  *excl = pb;
+  *total = s_t;
+  __syncthreads();
+  return ib;
+}
+
+// Settle a heavy vertex: subtract what it pushed, re-file it when it still
+// has excess, record the relabel candidate when some of its own excess was
+// left over.
+template <class Topo>
+__device__ __forceinline__ void settle(const Params<Topo>& p, int u, int E, int erem, int mn, int* rawcnt,
+                                       BlockAcc& acc) {
+  const int D = E - erem;
+  bool self = true;
+  if (D > 0) self = (atomicSub(p.e + u, D) - D) > 0;
+  if (erem > 0) {
+    p.rl_min[u] = mn;
+    p.rl_left[u] = erem;
+  }
+  if (self) append(p.qraw, rawcnt, u);
+  atomicAdd(&acc.visits, 1ull);
+  atomicAdd(&p.st->heavy_visits, 1ull);
+}
+
+__device__ __forceinline__ int block_min(int v) {
+  __shared__ int s_mn[32];
+  v = __reduce_min_sync(0xffffffffu, v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) s_mn[wid] = v;
+  __syncthreads();
+  int m = kBig;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = min(m, s_mn[w]);
+  __syncthreads();
+  return m;
+}
+
+// Ordered discharge of the arcs [lo, hi) of the virtual row r by the whole
+// block: pushes at most erem units along admissible arcs in arc order.
+// Returns the units left; *mn gets this thread's min label over arcs still
+// residual after the pushes.
+template <class Topo>
+__device__ __forceinline__ unsigned ordered_push(const Params<Topo>& p, const VRow& r, int lo, int hi, int hu,
+                                                 unsigned erem, int* mn, int* rawcnt, BlockAcc& acc) {
+  const int th = hu - 1;
+  int npush = 0, mloc = kBig;
+  unsigned long long scanned = 0;
+  for (int vb = lo; vb < hi && erem > 0; vb += blockDim.x * kItems) {
+    int dst[kItems], cf[kItems], hv[kItems], kk[kItems], aa[kItems];
 #pragma unroll
-      for (int j = 0; j < kItems; ++j) hv[j] = cf[j] > 0 ? __ldcg(p.lab + dst[j]) : kBig;
-      if (tid == 0) scanned += (unsigned long long)min(blockDim.x * kItems, e - base);
+    for (int it = 0; it < kItems; ++it) {
+      const int vi = vb + it * blockDim.x + threadIdx.x;
+      dst[it] = 0;
+      cf[it] = 0;
+      kk[it] = 0;
+      aa[it] = 0;
+      if (vi < hi) {
+        vidx(r, vi, kk[it], aa[it]);
+        p.g.load(kk[it], aa[it], dst[it], cf[it]);
+      }
+    }
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) hv[it] = cf[it] > 0 ? __ldcg(p.lab + dst[it]) : kBig;
+    scanned += (unsigned long long)min(blockDim.x * kItems, hi - vb);
 #pragma unroll 1
-      for (int j = 0; j < kItems; ++j) {
-        const int a = base + j * blockDim.x + tid;
-        const bool adm = cf[j] > 0 && hv[j] == th;
-        int pushed = 0;
-        if (__syncthreads_or(adm)) {
-          unsigned incl = adm ? (unsigned)cf[j] : 0u;
-          if (incl > erem) incl = erem;
-#pragma unroll
-          for (int d = 1; d < 32; d <<= 1) {
-            unsigned y = __shfl_up_sync(0xffffffffu, incl, d);
-            if (lane >= d) {
-              incl += y;
-              if (incl > erem) incl = erem;
-            }
-          }
-          unsigned prevw = __shfl_up_sync(0xffffffffu, incl, 1);
-          if (lane == 0) prevw = 0;
-          if (lane == 31) s_wsum[wid] = incl;
-          __syncthreads();
-          if (wid == 0) {
-            unsigned v = lane < nw ? s_wsum[lane] : 0u;
-            unsigned inc2 = v;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-              unsigned y = __shfl_up_sync(0xffffffffu, inc2, d);
-              if (lane >= d) {
-                inc2 += y;
-                if (inc2 > erem) inc2 = erem;
-              }
-            }
-            unsigned exc2 = __shfl_up_sync(0xffffffffu, inc2, 1);
-            if (lane == 0) exc2 = 0;
-            if (lane < nw) s_wsum[lane] = exc2;
-            if (lane == nw - 1) s_tot = inc2;
-          }
-          __syncthreads();
-          const unsigned wpre = s_wsum[wid];
-          unsigned ib = wpre + incl, pb = wpre + prevw;
-          if (ib > erem) ib = erem;
-          if (pb > erem) pb = erem;
-          pushed = (int)(ib - pb);
-          const unsigned total = s_tot;
-          __syncthreads();
-          erem -= total;
-          if (pushed > 0) {
-            p.g.push(k, a, cf[j], pushed);
-            ++npush;
-            if (dst[j] == p.t) {
-              atomicAdd(&acc.sink, pushed);
-            } else {
-              int old = atomicAdd(p.e + dst[j], pushed);
-              if (old == 0) append(p.qraw, rawcnt, dst[j]);
-            }
+    for (int it = 0; it < kItems; ++it) {
+      const bool adm = cf[it] > 0 && hv[it] == th;
+      int pushed = 0;
+      if (erem > 0 && __syncthreads_or(adm)) {
+        unsigned ex, total;
+        const unsigned inc = block_scan_sat(adm ? (unsigned)cf[it] : 0u, erem, &ex, &total);
+        pushed = (int)(inc - ex);
+        erem -= total;
+        if (pushed > 0) {
+          p.g.push(kk[it], aa[it], cf[it], pushed);
+          ++npush;
+          if (dst[it] == p.t) {
+            atomicAdd(&acc.sink, pushed);
+          } else {
+            int old = atomicAdd(p.e + dst[it], pushed);
+            if (old == 0) append(p.qraw, rawcnt, dst[it]);
           }
         }
-        if (cf[j] - pushed > 0 && hv[j] < minh) minh = hv[j];
-        if (erem == 0) break;
       }
+      if (cf[it] - pushed > 0 && hv[it] < mloc) mloc = hv[it];
     }
-  }
-  // block min over remaining residual arcs
-  minh = __reduce_min_sync(0xffffffffu, minh);
-  if (lane == 0) s_min[wid] = minh;
-  __syncthreads();
-  if (tid == 0) {
-    int mh = kBig;
-    for (int w = 0; w < nw; ++w) mh = min(mh, s_min[w]);
-    const int D = eu - (int)erem;
-    bool self = true;
-    if (D > 0) self = (atomicSub(p.e + u, D) - D) > 0;
-    if (erem > 0) {
-      p.rl_min[u] = mh;
-      p.rl_left[u] = (int)erem;
-    }
-    if (self) append(p.qraw, rawcnt, u);
-    atomicAdd(&acc.scanned, scanned);
-    atomicAdd(&acc.visits, 1ull);
   }
   if (npush) atomicAdd(&acc.pushes, (unsigned long long)npush);
+  if (threadIdx.x == 0) atomicAdd(&acc.scanned, scanned);
+  *mn = mloc;
+  return erem;
+}
+
+// Heavy vertex, stage 1: one block discharges chunk 0 (the first kChunk arcs)
+// in order.  Most heavy vertices place all their excess there; the others
+// become deep entries whose remaining chunks are handled in parallel.
+template <class Topo>
+__device__ void heavy_first(const Params<Topo>& p, int idx, int cur, int* rawcnt, BlockAcc& acc) {
+  __shared__ int s_u, s_E, s_hu;
+  __shared__ VRow s_r;
+  if (threadIdx.x == 0) {
+    s_u = __ldcg(p.hq[cur] + idx);
+    s_E = __ldcg(p.esnap + s_u);
+    s_hu = __ldcg(p.lab + s_u);
+    s_r = vrow(p.g, s_u);
+  }
+  __syncthreads();
+  const int u = s_u, E = s_E, hu = s_hu;
+  const VRow r = s_r;
+  __syncthreads();
+  if (E <= 0 || hu >= p.n) return;
+  int mloc;
+  const unsigned erem = ordered_push(p, r, 0, min(r.deg, kChunk), hu, (unsigned)E, &mloc, rawcnt, acc);
+  const int mn = block_min(mloc);
+  if (threadIdx.x == 0) {
+    if (erem == 0 || r.deg <= kChunk) {
+      settle(p, u, E, (int)erem, mn, rawcnt, acc);
+    } else {
+      Ctl* c = p.ctl;
+      const int nch = (r.deg - kChunk + kChunk - 1) / kChunk;
+      const unsigned long long old = atomicAdd(&c->dpack, (1ull << 32) | (unsigned long long)nch);
+      const int di = (int)(old >> 32), base = (int)(old & 0xffffffffu);
+      p.dq[di] = u;
+      p.dbase[di] = base;
+      p.dE[di] = E;
+      p.derem[di] = (int)erem;
+      p.dmin0[di] = mn;
+      for (int j = 0; j < nch; ++j) p.hown[base + j] = di;
+    }
+  }
   __syncthreads();
 }
 
-template <class Topo, int W>
-__device__ void push_phase(const Params<Topo>& p, int cur, int raw, BlockAcc& acc) {
+struct DeepMeta {
+  int u, di, base, E, Er, hu, j, nch;
+  VRow r;
+};
+
+template <class Topo>
+__device__ __forceinline__ void deep_meta(const Params<Topo>& p, int k, DeepMeta* m) {
+  __shared__ DeepMeta s_m;
+  if (threadIdx.x == 0) {
+    s_m.di = __ldcg(p.hown + k);
+    s_m.u = __ldcg(p.dq + s_m.di);
+    s_m.base = __ldcg(p.dbase + s_m.di);
+    s_m.E = __ldcg(p.dE + s_m.di);
+    s_m.Er = __ldcg(p.derem + s_m.di);
+    s_m.hu = __ldcg(p.lab + s_m.u);
+    s_m.j = k - s_m.base;
+    s_m.r = vrow(p.g, s_m.u);
+    s_m.nch = (s_m.r.deg - kChunk + kChunk - 1) / kChunk;
+  }
+  __syncthreads();
+  *m = s_m;
+  __syncthreads();
+}
+
+// Deep entry, pass A: admissible capacity (saturated at the excess left) and
+// min label over the other residual arcs of chunk j + 1.
+template <class Topo>
+__device__ void deep_pass_a(const Params<Topo>& p, int k, BlockAcc& acc) {
+  DeepMeta m;
+  deep_meta(p, k, &m);
+  const int lo = (m.j + 1) * kChunk, hi = min(m.r.deg, lo + kChunk);
+  const int th = m.hu - 1;
+  unsigned long long sum = 0;
+  int mn = kBig;
+  for (int vb = lo; vb < hi; vb += blockDim.x * kItems) {
+    int dst[kItems], cf[kItems];
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {
+      const int vi = vb + it * blockDim.x + threadIdx.x;
+      dst[it] = 0;
+      cf[it] = 0;
+      if (vi < hi) {
+        int kk, a;
+        vidx(m.r, vi, kk, a);
+        p.g.load(kk, a, dst[it], cf[it]);
+      }
+    }
+#pragma unroll
+    for (int it = 0; it < kItems; ++it) {
+      if (cf[it] > 0) {
+        const int hv = __ldcg(p.lab + dst[it]);
+        if (hv == th) sum += (unsigned)cf[it];
+        else if (hv < mn) mn = hv;
+      }
+    }
+  }
+  __shared__ unsigned long long s_sum[32];
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = sum;
+  const int mm = block_min(mn);
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_sum[w];
+    p.hsum[k] = (int)(t > (unsigned long long)m.Er ? (unsigned long long)m.Er : t);
+    p.hmin[k] = mm;
+    atomicAdd(&acc.scanned, (unsigned long long)(hi - lo));
+  }
+  __syncthreads();
+}
+
+// Deep entry, pass B: chunk takes min(sum, Er - earlier chunks) and pushes it
+// in order; the last chunk settles the vertex.
+template <class Topo>
+__device__ void deep_pass_b(const Params<Topo>& p, int k, int* rawcnt, BlockAcc& acc) {
+  DeepMeta m;
+  deep_meta(p, k, &m);
+  __shared__ int s_allot;
+  __shared__ long long s_prev;
+  if (threadIdx.x == 0) {
+    long long prev = 0;
+    for (int i = m.base; i < k && prev < m.Er; ++i) prev += __ldcg(p.hsum + i);
+    const int S = __ldcg(p.hsum + k);
+    s_prev = prev;
+    s_allot = prev >= m.Er ? 0 : (int)min((long long)S, (long long)m.Er - prev);
+  }
+  __syncthreads();
+  const unsigned allot = (unsigned)s_allot;
+  const long long prev = s_prev;
+  __syncthreads();
+  if (allot > 0) {
+    const int lo = (m.j + 1) * kChunk, hi = min(m.r.deg, lo + kChunk);
+    int unused;
+    ordered_push(p, m.r, lo, hi, m.hu, allot, &unused, rawcnt, acc);
+  }
+  if (threadIdx.x == 0 && m.j == m.nch - 1) {
+    const long long all = prev + __ldcg(p.hsum + k);
+    const int Dd = (int)min((long long)m.Er, all);
+    const int erest = m.Er - Dd;
+    int mn = __ldcg(p.dmin0 + m.di);
+    if (erest > 0)
+      for (int i = m.base; i < m.base + m.nch; ++i) mn = min(mn, __ldcg(p.hmin + i));
+    settle(p, m.u, m.E, erest, mn, rawcnt, acc);
+  }
+  __syncthreads();
+}
+
+// File u as active for the next round (light list or heavy list).
+template <class Topo>
+__device__ __forceinline__ void file_active(const Params<Topo>& p, int nxt, int u, int eu) {
   Ctl* c = p.ctl;
-  const int nH = ldv(&c->hcount[cur]);
+  p.esnap[u] = eu;
+  if (p.g.deg(u) <= p.heavy_deg) append(p.lq[nxt], &c->lcount[nxt], u);
+  else append(p.hq[nxt], &c->hcount[nxt], u);
+}
+
+// Push phase, stage 1: heavy vertices' chunk 0 (block each) and light rows.
+template <class Topo, int W>
+__device__ void push_first(const Params<Topo>& p, int cur, int raw, BlockAcc& acc) {
+  Ctl* c = p.ctl;
   const int nL = ldv(&c->lcount[cur]);
+  const int nH = ldv(&c->hcount[cur]);
   int* rawcnt = &c->qraw_count[raw];
   __shared__ int s_item;
-  // heavy rows first (whole block each), dynamically claimed
   for (;;) {
     if (threadIdx.x == 0) s_item = nH > 0 ? atomicAdd(&c->heavy_next, 1) : nH;
     __syncthreads();
     const int it = s_item;
     __syncthreads();
     if (it >= nH) break;
-    discharge_block<Topo>(p, __ldcg(p.hq[cur] + it), rawcnt, acc);
+    heavy_first<Topo>(p, it, cur, rawcnt, acc);
   }
-  // light rows: each warp claims 2 entries per tile at a time
   constexpr int kTpw = 32 / W;
   constexpr int kGrab = 2 * kTpw;
   const int lane = threadIdx.x & 31;
@@ -516,9 +770,29 @@ __device__ void push_phase(const Params<Topo>& p, int cur, int raw, BlockAcc& ac
     }
     __syncwarp();
   }
+}
+
+template <class Topo>
+__device__ void push_deep(const Params<Topo>& p, int pass, int nD, int raw, BlockAcc& acc) {
+  Ctl* c = p.ctl;
+  int* rawcnt = &c->qraw_count[raw];
+  int* ctr = pass == 0 ? &c->deep_next_a : &c->deep_next_b;
+  __shared__ int s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(ctr, 1);
+    __syncthreads();
+    const int it = s_item;
+    __syncthreads();
+    if (it >= nD) break;
+    if (pass == 0) deep_pass_a<Topo>(p, it, acc);
+    else deep_pass_b<Topo>(p, it, rawcnt, acc);
+  }
+}
+
+__device__ __forceinline__ void flush_sink(int* et, BlockAcc& acc) {
   __syncthreads();
   if (threadIdx.x == 0 && acc.sink) {
-    atomicAdd(p.e + p.t, acc.sink);
+    atomicAdd(et, acc.sink);
     acc.sink = 0;
   }
 }
@@ -546,19 +820,19 @@ __device__ void relabel_phase(const Params<Topo>& p, int cur, int nxt, int raw, 
       hu = nh;
       ++rl;
     }
-    if (eu > 0 && hu < p.n) {
-      if (p.g.deg(u) > p.heavy_deg) append(p.hq[nxt], &c->hcount[nxt], u);
-      else append(p.lq[nxt], &c->lcount[nxt], u);
-    }
+    if (eu > 0 && hu < p.n) file_active(p, nxt, u, eu);
   }
   if (rl) atomicAdd(&acc.relabels, rl);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     c->lcount[cur] = 0;
     c->hcount[cur] = 0;
+    c->dpack = 0;
     c->qraw_count[raw ^ 1] = 0;
     c->work[raw ^ 1] = 0;
     c->light_next = 0;
     c->heavy_next = 0;
+    c->deep_next_a = 0;
+    c->deep_next_b = 0;
   }
 }
 
@@ -567,49 +841,62 @@ __device__ void relabel_phase(const Params<Topo>& p, int cur, int nxt, int raw, 
 // DIR 0 labels every vertex with its residual distance TO the root (the
 // reference's backward BFS from the sink); DIR 1 with its distance FROM the
 // root.  Unreached vertices keep label n.  Top-down expands the frontier
-// (warp per light row, all warps of the grid per heavy row); bottom-up lets
-// every unvisited vertex look for a frontier neighbour (thread / warp / block
-// per row by length class).
-template <class Topo, int DIR>
-__device__ __forceinline__ bool bfs_edge(const Params<Topo>& p, int k, int a, int& dst) {
-  // true when the arc a (in the row of x, head dst) links dst to the row
-  // owner in the BFS direction: DIR 0 needs residual dst -> x, DIR 1 x -> dst.
-  int cf;
-  if (DIR == 0) {
-    dst = p.g.head(k, a);
-    (void)cf;
-    return true;
-  } else {
-    p.g.load(k, a, dst, cf);
-    return cf > 0;
-  }
-}
+// (warp per row; all warps of the grid share each row longer than kTdHeavy);
+// bottom-up lets every unvisited vertex look for a frontier neighbour
+// (8-lane tile per short row, warp per medium row, blocks over 2048-arc
+// chunks of long rows).
+constexpr int kTdHeavy = 256;
+constexpr int kTdChunk = 1024;
 
 template <class Topo>
-__device__ __forceinline__ void bfs_discover(const Params<Topo>& p, int v, int level, int fn,
-                                             BlockAcc& acc) {
+__device__ __forceinline__ void bfs_discover(const Params<Topo>& p, int v, int fn, BlockAcc& acc) {
   const int d = p.g.deg(v);
-  if (d > kHeavyDeg) append(p.frh[fn], &p.ctl->fhcount[fn], v);
-  else append(p.fr[fn], &p.ctl->fcount[fn], v);
+  if (d > kTdHeavy) {
+    // a long row enters the frontier as ceil(d / kTdChunk) chunk items
+    const int nch = (d + kTdChunk - 1) / kTdChunk;
+    const int base = atomicAdd(&p.ctl->fhcount[fn], nch);
+    for (int j = 0; j < nch; ++j) p.frh[fn][base + j] = make_int2(v, j);
+  } else {
+    append(p.fr[fn], &p.ctl->fcount[fn], v);
+  }
   atomicAdd((unsigned long long*)&acc.fdeg, (unsigned long long)d);
 }
 
+// Top-down on a batch of up to 4 arcs per lane: heads, then labels, then the
+// twin residual of the still-unvisited heads, then the claims.
 template <class Topo, int DIR>
-__device__ __forceinline__ void td_arc(const Params<Topo>& p, int k, int a, int level, int fn,
-                                       BlockAcc& acc, unsigned long long& arcs) {
-  int dst, cf;
-  bool ok;
-  if (DIR == 0) {
-    dst = p.g.head(k, a);
-    ok = true;
-  } else {
-    p.g.load(k, a, dst, cf);
-    ok = cf > 0;
+__device__ __forceinline__ void td_batch(const Params<Topo>& p, const VRow& r, int v0, int vend, int stride,
+                                         int level, int fn, BlockAcc& acc, unsigned long long& arcs) {
+  int kk[4], aa[4], dst[4];
+  bool ok[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int vi = v0 + q * stride;
+    ok[q] = vi < vend;
+    dst[q] = -1;
+    if (ok[q]) {
+      vidx(r, vi, kk[q], aa[q]);
+      if (DIR == 0) {
+        dst[q] = p.g.head(kk[q], aa[q]);
+      } else {
+        int cf;
+        p.g.load(kk[q], aa[q], dst[q], cf);
+        ok[q] = cf > 0;
+      }
+      ++arcs;
+    }
   }
-  ++arcs;
-  if (!ok || dst == p.bfs_excl || __ldcg(p.lab + dst) != p.n) return;
-  if (DIR == 0 && p.g.twin_cf(k, a) <= 0) return;
-  if (atomicCAS(p.lab + dst, p.n, level + 1) == p.n) bfs_discover(p, dst, level, fn, acc);
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (ok[q]) ok[q] = dst[q] != p.bfs_excl && __ldcg(p.lab + dst[q]) == p.n;
+  if (DIR == 0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (ok[q]) ok[q] = p.g.twin_cf(kk[q], aa[q]) > 0;
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (ok[q] && atomicCAS(p.lab + dst[q], p.n, level + 1) == p.n) bfs_discover(p, dst[q], fn, acc);
 }
 
 // does the arc a of row x make x adjacent to a vertex labelled `level`?
@@ -635,23 +922,18 @@ __device__ void bfs_top_down(const Params<Topo>& p, int level, int fc, int fn, B
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   unsigned long long arcs = 0;
-  // heavy frontier rows: every warp of the grid takes 32-arc chunks
-  for (int i = 0; i < nfh; ++i) {
-    const int x = __ldcg(p.frh[fc] + i);
-    for (int k = 0; k < Topo::kSeg; ++k) {
-      int b, e;
-      p.g.seg(x, k, b, e);
-      for (int a = b + gw * 32 + lane; a < e; a += nwarps * 32) td_arc<Topo, DIR>(p, k, a, level, fn, acc, arcs);
-    }
+  // chunk items of long rows: a warp per 1024-arc chunk, 128 arcs in flight
+  for (int i = gw; i < nfh; i += nwarps) {
+    const int2 it = __ldcg(p.frh[fc] + i);
+    const VRow r = vrow(p.g, it.x);
+    const int lo = it.y * kTdChunk, hi = min(r.deg, lo + kTdChunk);
+    for (int v0 = lo + lane; v0 < hi; v0 += 128) td_batch<Topo, DIR>(p, r, v0, hi, 32, level, fn, acc, arcs);
   }
-  // light frontier rows: warp per row
+  // short rows (<= kTdHeavy arcs): a warp per row
   for (int i = gw; i < nf; i += nwarps) {
     const int x = __ldcg(p.fr[fc] + i);
-    for (int k = 0; k < Topo::kSeg; ++k) {
-      int b, e;
-      p.g.seg(x, k, b, e);
-      for (int a = b + lane; a < e; a += 32) td_arc<Topo, DIR>(p, k, a, level, fn, acc, arcs);
-    }
+    const VRow r = vrow(p.g, x);
+    for (int v0 = lane; v0 < r.deg; v0 += 128) td_batch<Topo, DIR>(p, r, v0, r.deg, 32, level, fn, acc, arcs);
   }
   if (arcs) atomicAdd(&acc.bfs_arcs, arcs);
 }
@@ -663,26 +945,54 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, int fn, BlockAcc
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   const int gw = gt >> 5, nwarps = gs >> 5;
   unsigned long long arcs = 0, verts = 0;
-  // light rows: one thread each
-  for (int i = gt; i < p.n_light; i += gs) {
-    const int x = __ldg(p.cls + i);
-    ++verts;
-    if (x == p.bfs_excl || __ldcg(p.lab + x) != p.n) continue;
-    bool hit = false;
-    for (int k = 0; k < Topo::kSeg && !hit; ++k) {
-      int b, e;
-      p.g.seg(x, k, b, e);
-      for (int a = b; a < e; ++a) {
-        ++arcs;
-        if (bu_arc<Topo, DIR>(p, k, a, level)) { hit = true; break; }
+  // short rows (<= kLightDeg): a thread each, 4 rows and 4 arcs in flight
+  for (int i0 = gt; i0 < p.n_light; i0 += 4 * gs) {
+    int xs[4];
+    bool todo[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = i0 + q * gs;
+      xs[q] = i < p.n_light ? __ldg(p.cls + i) : -1;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      todo[q] = xs[q] >= 0 && xs[q] != p.bfs_excl && __ldcg(p.lab + xs[q]) == p.n;
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+      if (xs[q] >= 0) ++verts;
+      if (!todo[q]) continue;
+      const int x = xs[q];
+      const VRow r = vrow(p.g, x);
+      bool hit = false;
+      for (int v0 = 0; v0 < r.deg && !hit; v0 += 4) {
+        int kk[4], aa[4], dst[4], cf[4];
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+          cf[w] = 0;
+          dst[w] = 0;
+          if (v0 + w < r.deg) {
+            vidx(r, v0 + w, kk[w], aa[w]);
+            p.g.load(kk[w], aa[w], dst[w], cf[w]);
+            ++arcs;
+          }
+        }
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+          if (v0 + w >= r.deg) continue;
+          if (DIR == 0) {
+            if (cf[w] > 0 && __ldcg(p.lab + dst[w]) == level) hit = true;
+          } else {
+            if (__ldcg(p.lab + dst[w]) == level && p.g.twin_cf(kk[w], aa[w]) > 0) hit = true;
+          }
+        }
+      }
+      if (hit) {
+        p.lab[x] = level + 1;
+        bfs_discover(p, x, fn, acc);
       }
     }
-    if (hit) {
-      p.lab[x] = level + 1;
-      bfs_discover(p, x, level, fn, acc);
-    }
   }
-  // medium rows: one warp each
+  // medium rows: a warp each, 4 arcs per lane in flight
   for (int i = gw; i < p.n_medium; i += nwarps) {
     const int x = __ldg(p.cls + p.n_light + i);
     if (lane == 0) ++verts;
@@ -691,54 +1001,71 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, int fn, BlockAcc
     for (int k = 0; k < Topo::kSeg && !hit; ++k) {
       int b, e;
       p.g.seg(x, k, b, e);
-      for (int base = b; base < e; base += 32) {
-        const int a = base + lane;
+      for (int base = b; base < e; base += 128) {
         bool h = false;
-        if (a < e) { ++arcs; h = bu_arc<Topo, DIR>(p, k, a, level); }
-        if (__any_sync(0xffffffffu, h)) { hit = true; break; }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int a = base + q * 32 + lane;
+          if (a < e) {
+            ++arcs;
+            h |= bu_arc<Topo, DIR>(p, k, a, level);
+          }
+        }
+        if (__any_sync(0xffffffffu, h)) {
+          hit = true;
+          break;
+        }
       }
     }
     if (hit && lane == 0) {
       p.lab[x] = level + 1;
-      bfs_discover(p, x, level, fn, acc);
+      bfs_discover(p, x, fn, acc);
     }
   }
   if (arcs) atomicAdd(&acc.bfs_arcs, arcs);
   if (verts) atomicAdd(&acc.bfs_vertices, verts);
-  // heavy rows: one block each, claimed dynamically
+  // long rows: blocks over static 2048-arc chunks; first chunk to hit wins
   __shared__ int s_item;
-  const int cur3 = (level) % 3;
+  __shared__ int s_skip;
+  const int cur3 = level % 3;
+  unsigned long long ha = 0;
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(&c->bfs_heavy_next[cur3], 1);
     __syncthreads();
     const int it = s_item;
+    if (it >= p.n_bch) {
+      __syncthreads();
+      break;
+    }
+    const int4 ch = __ldg(p.bch + it);  // {vertex, segment, begin, end}
+    if (threadIdx.x == 0) s_skip = (ch.x == p.bfs_excl || __ldcg(p.lab + ch.x) != p.n);
     __syncthreads();
-    if (it >= p.n_heavy) break;
-    const int x = __ldg(p.cls + p.n_light + p.n_medium + it);
-    if (x == p.bfs_excl || __ldcg(p.lab + x) != p.n) continue;  // uniform per block
+    if (s_skip) continue;
     bool hit = false;
-    unsigned long long ha = 0;
-    for (int k = 0; k < Topo::kSeg && !hit; ++k) {
-      int b, e;
-      p.g.seg(x, k, b, e);
-      for (int base = b; base < e; base += blockDim.x) {
-        const int a = base + threadIdx.x;
-        bool h = false;
-        if (a < e) { ++ha; h = bu_arc<Topo, DIR>(p, k, a, level); }
-        if (__syncthreads_or(h)) { hit = true; break; }
+    for (int base = ch.z; base < ch.w; base += blockDim.x * 4) {
+      bool h = false;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int a = base + q * blockDim.x + threadIdx.x;
+        if (a < ch.w) {
+          ++ha;
+          h |= bu_arc<Topo, DIR>(p, ch.y, a, level);
+        }
+      }
+      if (__syncthreads_or(h)) {
+        hit = true;
+        break;
       }
     }
-    if (ha) atomicAdd(&acc.bfs_arcs, ha);
-    if (hit && threadIdx.x == 0) {
-      p.lab[x] = level + 1;
-      bfs_discover(p, x, level, fn, acc);
-    }
+    if (hit && threadIdx.x == 0 && atomicCAS(p.lab + ch.x, p.n, level + 1) == p.n)
+      bfs_discover(p, ch.x, fn, acc);
   }
+  if (ha) atomicAdd(&acc.bfs_arcs, ha);
 }
 
 // Full BFS; on return every block has passed the closing barrier.  When
-// `queues` is set, the light/heavy active lists `cur` are rebuilt from the new
-// labels (vertices with excess and label < n, other than s and t).
+// `queues` is set, the active lists `cur` are rebuilt from the new labels
+// (vertices with excess and label < n, other than s and t).
 template <class Topo, int DIR>
 __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, BlockAcc& acc) {
   Ctl* c = p.ctl;
@@ -746,9 +1073,10 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
   for (int v = gt; v < p.n; v += gs) p.lab[v] = (v == root) ? 0 : p.n;
   if (gt == 0) {
     const int d = p.g.deg(root);
-    if (d > kHeavyDeg) {
-      p.frh[0][0] = root;
-      c->fhcount[0] = 1;
+    if (d > kTdHeavy) {
+      const int nch = (d + kTdChunk - 1) / kTdChunk;
+      for (int j = 0; j < nch; ++j) p.frh[0][j] = make_int2(root, j);
+      c->fhcount[0] = nch;
       c->fcount[0] = 0;
     } else {
       p.fr[0][0] = root;
@@ -763,8 +1091,11 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
     if (queues) {
       c->lcount[cur] = 0;
       c->hcount[cur] = 0;
+      c->dpack = 0;
       c->light_next = 0;
       c->heavy_next = 0;
+      c->deep_next_a = 0;
+      c->deep_next_b = 0;
     }
   }
   if (!grid_sync(c, p.bar_timeout_ns)) return false;
@@ -786,6 +1117,9 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
       c->fhcount[fr] = 0;
       c->fdeg[fr] = 0;
       c->bfs_heavy_next[fn] = 0;
+      atomicAdd(&p.st->bfs_levels, 1);
+      if (bu) atomicAdd(&p.st->bu_levels, 1);
+      TRACE(p, kTrLevel, bu ? 1 : 0, nf, fdeg);
     }
     if (threadIdx.x == 0) acc.fdeg = 0;
     __syncthreads();
@@ -801,10 +1135,8 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
     for (int i = gt; i < nall; i += gs) {
       const int v = __ldg(p.cls + i);
       if (v == p.s || v == p.t) continue;
-      if (ldv(p.e + v) > 0 && __ldcg(p.lab + v) < p.n) {
-        if (p.g.deg(v) > p.heavy_deg) append(p.hq[cur], &c->hcount[cur], v);
-        else append(p.lq[cur], &c->lcount[cur], v);
-      }
+      const int ev = ldv(p.e + v);
+      if (ev > 0 && __ldcg(p.lab + v) < p.n) file_active(p, cur, v, ev);
     }
     if (!grid_sync(c, p.bar_timeout_ns)) return false;
   }
@@ -813,7 +1145,7 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
 
 // ---------------------------------------------------------------------------
 template <class Topo, int W>
-__global__ void __launch_bounds__(256, 2) pr_persistent(Params<Topo> p) {
+__global__ void __launch_bounds__(256, 3) pr_persistent(Params<Topo> p) {
   __shared__ BlockAcc acc;
   Ctl* c = p.ctl;
   if (threadIdx.x == 0) {
@@ -824,6 +1156,7 @@ __global__ void __launch_bounds__(256, 2) pr_persistent(Params<Topo> p) {
   __syncthreads();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   const unsigned long long t_start = gtime();
+  if (gt == 0) p.st->t0 = t_start;
 
   if (p.mode == kModeBfsOnly) {
     if (p.bfs_dir == 0) bfs<Topo, 0>(p, p.bfs_root, false, 0, acc);
@@ -865,7 +1198,8 @@ __global__ void __launch_bounds__(256, 2) pr_persistent(Params<Topo> p) {
   // work since the last global relabel: every block adds the per-round
   // counter of the finished round (final at the barrier), so all agree
   unsigned long long work = 0;
-  unsigned long long gr_ns = 0, round_ns = 0;
+  int since_gr = 0;
+  unsigned long long gr_ns = 0, round_ns = 0, push_ns = 0;
   for (;;) {
     if (need_gr) {
       const unsigned long long t0 = gtime();
@@ -873,20 +1207,40 @@ __global__ void __launch_bounds__(256, 2) pr_persistent(Params<Topo> p) {
       if (threadIdx.x == 0 && blockIdx.x == 0) {
         gr_ns += gtime() - t0;
         atomicAdd(&p.st->grs, 1);
+        TRACE(p, kTrGrEnd, 0, 0, 0);
       }
       need_gr = false;
       work = 0;
+      since_gr = 0;
     }
-    const int nact = ldv(&c->lcount[cur]) + ldv(&c->hcount[cur]);
+    const int nL = ldv(&c->lcount[cur]), nH = ldv(&c->hcount[cur]);
+    const int nact = nL + nH;
     if (nact == 0) break;
     if (ldv(&c->stop)) {
       if (gt == 0) atomicCAS(&c->err, 0, (int)WBPR_ERR_NO_CONVERGENCE);
       break;
     }
     const unsigned long long t0 = gtime();
-    push_phase<Topo, W>(p, cur, raw, acc);
+    if (gt == 0) TRACE(p, kTrRound, rounds, nL, nH);
+    push_first<Topo, W>(p, cur, raw, acc);
+    if (nH > 0) {
+      if (!grid_sync(c, p.bar_timeout_ns)) break;
+      const unsigned long long dp = *(volatile unsigned long long*)&c->dpack;
+      const int nD = (int)(dp & 0xffffffffu);
+      if (gt == 0) TRACE(p, kTrPassA, rounds, (long long)(dp >> 32), nD);
+      if (nD > 0) {
+        push_deep<Topo>(p, 0, nD, raw, acc);
+        if (!grid_sync(c, p.bar_timeout_ns)) break;
+        push_deep<Topo>(p, 1, nD, raw, acc);
+      }
+    }
+    flush_sink(p.e + p.t, acc);
     flush_acc(acc, p.st, &c->work[raw]);
     if (!grid_sync(c, p.bar_timeout_ns)) break;
+    if (gt == 0) {
+      push_ns += gtime() - t0;
+      TRACE(p, kTrPassB, rounds, 0, 0);
+    }
     relabel_phase<Topo>(p, cur, cur ^ 1, raw, acc);
     flush_acc(acc, p.st, &c->work[raw]);
     if (gt == 0) {
@@ -895,17 +1249,23 @@ __global__ void __launch_bounds__(256, 2) pr_persistent(Params<Topo> p) {
         c->stop = 1;
     }
     if (!grid_sync(c, p.bar_timeout_ns)) break;
+    if (gt == 0) TRACE(p, kTrRelabel, rounds, ldv(&c->qraw_count[raw]), 0);
     work += *(volatile unsigned long long*)&c->work[raw];
     ++rounds;
+    ++since_gr;
     cur ^= 1;
     raw ^= 1;
-    if (work > p.gr_threshold) need_gr = true;
+    // Work-based trigger (Cherkassky-Goldberg) plus a round cap: tails where
+    // a few stranded vertices ping-pong excess do little work per round
+    // while their labels climb towards n two at a time.
+    if (work > p.gr_threshold || since_gr >= p.gr_rounds) need_gr = true;
   }
   flush_acc(acc, p.st);
   if (gt == 0) {
     p.st->rounds = rounds;
     p.st->gr_ns = gr_ns;
     p.st->round_ns = round_ns;
+    p.st->push_ns = push_ns;
   }
 }
 
