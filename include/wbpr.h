@@ -234,6 +234,26 @@ wbpr_status wbpr_verify(wbpr_graph* g, wbpr_verify_report* rep);
 wbpr_status wbpr_mincut_adjoint(wbpr_graph* g, int32_t side, int8_t* indicator,
                                 float* adjoint_ms);
 
+/* ---- solve without any device allocation --------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory (code running inside a caller-owned memory pool or arena, or a
+ * framework that forbids cudaMalloc on its hot path): the caller passes the
+ * BCSR residual graph in device buffers it owns -- d_row[n+1], d_arc (2 ints
+ * per residual arc: head, residual; the residual is reset to the capacity and
+ * holds the final residual on return), d_arx (2 ints per residual arc: twin
+ * arc, capacity), as produced by wbpr_build_bcsr -- and receives the maximum
+ * flow in *flow (host).  All solver scratch lives in one fixed file-scope
+ * device array (about 7.4 MB per device, held until exit), so no allocation
+ * happens.  Limits: n <= 65536 vertices and num_residual_arcs <= 1048576;
+ * larger inputs return WBPR_ERR_INVALID_ARG (see wbpr_last_error).  The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race and
+ * must be serialised by the caller.  `stream` is a cudaStream_t or NULL; the
+ * call synchronises it before returning. */
+wbpr_status wbpr_solve_bcsr_noalloc(int32_t n, int64_t num_residual_arcs, const int32_t* d_row,
+                                    int32_t* d_arc, const int32_t* d_arx, int32_t s, int32_t t,
+                                    int32_t algo, void* stream, int64_t* flow);
+
 /* ---- drop-ins for the reference host functions (RCSR arrays, in place) --- */
 /* Same arguments and meaning as preflow() in maxflow-cuda/src/preflow.cu:3-31,
  * except that excess is accumulated (+=) so parallel source arcs are not lost.

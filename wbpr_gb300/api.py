@@ -86,7 +86,7 @@ EXPORTED = [
     "wbpr_build_rcsr", "wbpr_build_bcsr", "wbpr_build_bcsr2", "wbpr_graph_create",
     "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_solve", "wbpr_read_state",
     "wbpr_verify", "wbpr_mincut_adjoint", "wbpr_rcsr_preflow", "wbpr_rcsr_push_relabel",
-    "wbpr_read_trace",
+    "wbpr_read_trace", "wbpr_solve_bcsr_noalloc",
 ]
 
 _lib = None
@@ -132,6 +132,9 @@ def lib() -> C.CDLL:
         "wbpr_solve": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int, C.POINTER(Tuning), C.POINTER(Result)]),
         "wbpr_read_state": (C.c_int, [vp, _i32p, _i32p, _i32p]),
         "wbpr_read_trace": (C.c_int32, [vp, C.POINTER(C.c_int64), C.c_int32]),
+        "wbpr_solve_bcsr_noalloc": (C.c_int, [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                              C.POINTER(C.c_int64)]),
         "wbpr_verify": (C.c_int, [vp, C.POINTER(VerifyReport)]),
         "wbpr_mincut_adjoint": (C.c_int, [vp, C.c_int32, _i8p, C.POINTER(C.c_float)]),
         "wbpr_rcsr_preflow": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, _i32p, _i32p, _i32p, _i32p,

@@ -16,6 +16,10 @@ using namespace wbpr_dev;
 
 static thread_local std::string g_last_error;
 
+namespace wbpr {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace wbpr
+
 #define CK(call)                                                            \
   do {                                                                      \
     cudaError_t e_ = (call);                                                \

@@ -55,4 +55,7 @@ wbpr_status build_rcsr_dev(const wbpr_csr* g, Rcsr* out);
 // Hardware threads to use for host loops.
 int host_threads();
 
+// Record the text that wbpr_last_error() returns on this host thread.
+void set_last_error(const std::string& msg);
+
 }  // namespace wbpr
