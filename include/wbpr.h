@@ -234,6 +234,28 @@ wbpr_status wbpr_verify(wbpr_graph* g, wbpr_verify_report* rep);
 wbpr_status wbpr_mincut_adjoint(wbpr_graph* g, int32_t side, int8_t* indicator,
                                 float* adjoint_ms);
 
+/* ---- batched solver ---------------------------------------------------------- */
+/* No counterpart in the reference (its CLI solves one graph per process).
+ * Many independent instances, each with its own source and sink, solved in one
+ * launch: every thread block claims a whole instance (largest first) and runs
+ * preflow, global relabels and push/relabel rounds with block-level barriers
+ * only, scheduling its own global relabels.  The launch is captured into a
+ * CUDA graph on the first solve with a given tuning and replayed afterwards. */
+typedef struct wbpr_batch wbpr_batch;
+wbpr_status wbpr_batch_create(const wbpr_csr* graphs, int32_t count, wbpr_batch** out);
+wbpr_status wbpr_batch_destroy(wbpr_batch* b);
+int64_t wbpr_batch_device_bytes(const wbpr_batch* b);
+/* flows (host, count entries, may be NULL): maximum-flow values, -1 for an
+ * instance that hit its budget (then WBPR_ERR_NO_CONVERGENCE).  Uses
+ * tuning.tile (8/16/32), .block (64..512), .gr_alpha, .gr_rounds, .max_rounds,
+ * .max_ms (per instance). */
+wbpr_status wbpr_batch_solve(wbpr_batch* b, const wbpr_tuning* tuning, int64_t* flows, float* solve_ms);
+/* Per-instance device time (ms) and rounds of the last solve (either may be NULL). */
+wbpr_status wbpr_batch_instance_stats(wbpr_batch* b, float* inst_ms, int32_t* inst_rounds);
+/* Try tile widths, block sizes and global-relabel frequencies on this batch;
+ * return the fastest tuning and its time. */
+wbpr_status wbpr_batch_autotune(wbpr_batch* b, wbpr_tuning* best, float* best_ms);
+
 /* ---- solve without any device allocation --------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory (code running inside a caller-owned memory pool or arena, or a

@@ -86,7 +86,8 @@ EXPORTED = [
     "wbpr_build_rcsr", "wbpr_build_bcsr", "wbpr_build_bcsr2", "wbpr_graph_create",
     "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_solve", "wbpr_read_state",
     "wbpr_verify", "wbpr_mincut_adjoint", "wbpr_rcsr_preflow", "wbpr_rcsr_push_relabel",
-    "wbpr_read_trace", "wbpr_solve_bcsr_noalloc",
+    "wbpr_read_trace", "wbpr_solve_bcsr_noalloc", "wbpr_batch_create", "wbpr_batch_destroy",
+    "wbpr_batch_device_bytes", "wbpr_batch_solve", "wbpr_batch_instance_stats", "wbpr_batch_autotune",
 ]
 
 _lib = None
@@ -132,6 +133,12 @@ def lib() -> C.CDLL:
         "wbpr_solve": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int, C.POINTER(Tuning), C.POINTER(Result)]),
         "wbpr_read_state": (C.c_int, [vp, _i32p, _i32p, _i32p]),
         "wbpr_read_trace": (C.c_int32, [vp, C.POINTER(C.c_int64), C.c_int32]),
+        "wbpr_batch_create": (C.c_int, [C.POINTER(CsrView), C.c_int32, C.POINTER(vp)]),
+        "wbpr_batch_destroy": (C.c_int, [vp]),
+        "wbpr_batch_device_bytes": (C.c_int64, [vp]),
+        "wbpr_batch_solve": (C.c_int, [vp, C.POINTER(Tuning), C.POINTER(C.c_int64), C.POINTER(C.c_float)]),
+        "wbpr_batch_instance_stats": (C.c_int, [vp, C.POINTER(C.c_float), _i32p]),
+        "wbpr_batch_autotune": (C.c_int, [vp, C.POINTER(Tuning), C.POINTER(C.c_float)]),
         "wbpr_solve_bcsr_noalloc": (C.c_int, [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                               C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                                               C.POINTER(C.c_int64)]),
@@ -384,6 +391,60 @@ class DeviceGraph:
         _check(lib().wbpr_mincut_adjoint(self._h, side, ind.ctypes.data_as(_i8p), C.byref(ms)),
                "wbpr_mincut_adjoint")
         return ind[:self.m], float(ms.value)
+
+
+class Batch:
+    """Many independent instances solved in one launch (wbpr_batch_*)."""
+
+    def __init__(self, graphs: list):
+        self._h = None
+        views = (CsrView * len(graphs))()
+        self._graphs = list(graphs)
+        for i, g in enumerate(self._graphs):
+            views[i] = g.view()
+        h = C.c_void_p()
+        _check(lib().wbpr_batch_create(views, len(graphs), C.byref(h)), "wbpr_batch_create")
+        self._h = h
+        self.count = len(graphs)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().wbpr_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().wbpr_batch_device_bytes(self._h))
+
+    def solve(self, tuning: Tuning | None = None, **kw):
+        """Returns (flows array, device ms)."""
+        tu = tuning if tuning is not None else default_tuning(**kw)
+        flows = np.zeros(self.count, np.int64)
+        ms = C.c_float(0)
+        _check(lib().wbpr_batch_solve(self._h, C.byref(tu), flows.ctypes.data_as(C.POINTER(C.c_int64)),
+                                      C.byref(ms)), "wbpr_batch_solve")
+        return flows, float(ms.value)
+
+    def instance_stats(self):
+        ms = np.zeros(self.count, np.float32)
+        rounds = np.zeros(self.count, np.int32)
+        _check(lib().wbpr_batch_instance_stats(self._h, ms.ctypes.data_as(C.POINTER(C.c_float)), _p(rounds)),
+               "wbpr_batch_instance_stats")
+        return ms, rounds
+
+    def autotune(self):
+        t = Tuning()
+        ms = C.c_float(0)
+        _check(lib().wbpr_batch_autotune(self._h, C.byref(t), C.byref(ms)), "wbpr_batch_autotune")
+        return t, float(ms.value)
 
 
 def maxflow(g: Graph, algo="vc", layout="bcsr", **tuning) -> int:

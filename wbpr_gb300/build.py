@@ -24,7 +24,7 @@ LIB = os.path.join(OUT, "libwbpr.so")
 CLI = os.path.join(OUT, "maxflow")
 
 ARCH = ["-gencode=arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["pr_bcsr.cu", "pr_rcsr.cu", "graph_dev.cu", "noalloc.cu"]
+CU_SOURCES = ["pr_bcsr.cu", "pr_rcsr.cu", "graph_dev.cu", "noalloc.cu", "batch.cu"]
 CPP_SOURCES = ["host_graph.cpp"]
 HEADERS = ["pr_kernel.cuh", "pr_launch.h", "wbpr_internal.h"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]

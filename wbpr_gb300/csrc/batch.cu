@@ -1,0 +1,585 @@
+// Batched solver: many independent, uneven max-flow instances in one launch.
+//
+// All instances live in one concatenated BCSR16 graph (global vertex and arc
+// ids).  Each thread block claims a whole instance from a work list sorted by
+// size (largest first) and solves it alone: preflow, then global relabels
+// (block-level BFS from the sink) and synchronous push/relabel rounds with
+// __syncthreads as the only barrier, each instance scheduling its own global
+// relabels by its own work and round counts.  Blocks never wait for each
+// other, so the launch needs no grid barrier.  Per-instance device
+// timestamps give the latency distribution.  The launch (and the memset of
+// its work counter) is captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "pr_kernel.cuh"
+#include "wbpr_internal.h"
+
+using namespace wbpr_dev;
+
+struct BatchInst {
+  int vbase;  // first global vertex id
+  int n;      // vertices
+  int s, t;   // global ids
+};
+
+struct wbpr_batch {
+  int device = 0, sms = 0, count = 0;
+  int64_t total_n = 0, total_arcs = 0, bytes = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int* row = nullptr;
+  int2* arc = nullptr;
+  int2* arx = nullptr;
+  BatchInst* inst = nullptr;
+  int* order = nullptr;  // instance ids, largest first
+  int* h = nullptr;
+  int* e = nullptr;
+  int* rl_min = nullptr;
+  int* rl_left = nullptr;
+  int* esnap = nullptr;
+  int* lq[2] = {nullptr, nullptr};
+  int* qraw = nullptr;
+  int* fr[2] = {nullptr, nullptr};
+  long long* flows = nullptr;
+  unsigned long long* inst_ns = nullptr;
+  int* inst_rounds = nullptr;
+  int* next = nullptr;  // work-list cursor
+  std::vector<void*> allocs;
+  // captured launch
+  cudaGraphExec_t exec = nullptr;
+  int cap_tile = 0, cap_block = 0;
+  double cap_alpha = 0;
+  int cap_grr = 0;
+  std::vector<long long> host_flows;
+};
+
+namespace {
+
+
+struct BatchParams {
+  const int* row;
+  int2* arc;
+  const int2* arx;
+  const BatchInst* inst;
+  const int* order;
+  int count;
+  int* h;
+  int* e;
+  int* rl_min;
+  int* rl_left;
+  int* esnap;
+  int* lq0;
+  int* lq1;
+  int* qraw;
+  int* fr0;
+  int* fr1;
+  long long* flows;
+  unsigned long long* inst_ns;
+  int* inst_rounds;
+  int* next;
+  double gr_alpha;
+  int gr_rounds;
+  int max_rounds;
+  unsigned long long budget_ns;
+};
+
+struct BlockCtl {
+  int lcount[2];
+  int qraw_count[2];
+  int fcount[2];
+  int item;
+  int stop;  // budget exhausted (decided by thread 0, read after a barrier)
+};
+
+// Block-level BFS from t over residual arcs (top-down, warp per frontier
+// row); unreached vertices of the instance keep label n.
+__device__ void batch_bfs(const Params<TopoB>& p, int vbase, int* fr0, int* fr1, BlockCtl& bc,
+                          BlockAcc& acc) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int v = vbase + (int)threadIdx.x; v < vbase + p.n; v += blockDim.x) p.lab[v] = (v == p.t) ? 0 : p.n;
+  if (threadIdx.x == 0) {
+    fr0[0] = p.t;
+    bc.fcount[0] = 1;
+    bc.fcount[1] = 0;
+  }
+  __syncthreads();
+  unsigned long long arcs = 0;
+  for (int level = 0;; ++level) {
+    int* cur = (level & 1) ? fr1 : fr0;
+    int* nxt = (level & 1) ? fr0 : fr1;
+    const int nf = bc.fcount[level & 1];
+    if (nf == 0) break;
+    for (int i = wid; i < nf; i += nw) {
+      const int x = __ldcg(cur + i);
+      const int b = __ldg(p.g.row + x), e = __ldg(p.g.row + x + 1);
+      for (int a = b + lane; a < e; a += 32) {
+        ++arcs;
+        const int dst = p.g.head(0, a);
+        if (dst == p.s || __ldcg(p.lab + dst) != p.n) continue;
+        if (p.g.twin_cf(0, a) <= 0) continue;
+        if (atomicCAS(p.lab + dst, p.n, level + 1) == p.n) append(nxt, &bc.fcount[(level + 1) & 1], dst);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) bc.fcount[level & 1] = 0;
+    __syncthreads();
+  }
+  if (arcs) atomicAdd(&acc.bfs_arcs, arcs);
+  // rebuild the active list of the instance
+  if (threadIdx.x == 0) bc.lcount[0] = 0;
+  __syncthreads();
+  for (int v = vbase + (int)threadIdx.x; v < vbase + p.n; v += blockDim.x) {
+    if (v == p.s || v == p.t) continue;
+    const int ev = ldv(p.e + v);
+    if (ev > 0 && __ldcg(p.lab + v) < p.n) {
+      p.esnap[v] = ev;
+      append(p.lq[0], &bc.lcount[0], v);
+    }
+  }
+  __syncthreads();
+}
+
+template <int W>
+__global__ void __launch_bounds__(512) pr_batch(BatchParams bp) {
+  __shared__ BlockAcc acc;
+  __shared__ BlockCtl bc;
+  for (;;) {
+    if (threadIdx.x == 0) bc.item = atomicAdd(bp.next, 1);
+    __syncthreads();
+    const int item = bc.item;
+    __syncthreads();
+    if (item >= bp.count) return;
+    const int id = bp.order[item];
+    const BatchInst in = bp.inst[id];
+    const unsigned long long t_start = gtime();
+    Params<TopoB> p;
+    p.g.row = bp.row;
+    p.g.arc = bp.arc;
+    p.g.arx = bp.arx;
+    p.n = in.n;
+    p.s = in.s;
+    p.t = in.t;
+    p.lab = bp.h;
+    p.e = bp.e;
+    p.rl_min = bp.rl_min;
+    p.rl_left = bp.rl_left;
+    p.esnap = bp.esnap;
+    p.lq[0] = bp.lq0 + in.vbase;
+    p.lq[1] = bp.lq1 + in.vbase;
+    p.qraw = bp.qraw + in.vbase;
+    int* fr0 = bp.fr0 + in.vbase;
+    int* fr1 = bp.fr1 + in.vbase;
+    const int abeg = __ldg(bp.row + in.vbase), aend = __ldg(bp.row + in.vbase + in.n);
+    if (threadIdx.x == 0) {
+      acc.scanned = acc.pushes = acc.relabels = acc.visits = acc.bfs_arcs = acc.bfs_vertices = 0;
+      acc.fdeg = 0;
+      acc.sink = 0;
+      bc.lcount[0] = bc.lcount[1] = 0;
+      bc.qraw_count[0] = bc.qraw_count[1] = 0;
+    }
+    // reset residuals and state of this instance, then preflow from s
+    for (int a = abeg + (int)threadIdx.x; a < aend; a += blockDim.x) bp.arc[a].y = __ldg(&bp.arx[a].y);
+    for (int v = in.vbase + (int)threadIdx.x; v < in.vbase + in.n; v += blockDim.x) {
+      bp.h[v] = 0;
+      bp.e[v] = 0;
+      bp.rl_min[v] = kNone;
+    }
+    __syncthreads();
+    {
+      const int b = __ldg(bp.row + in.s), e = __ldg(bp.row + in.s + 1);
+      for (int a = b + (int)threadIdx.x; a < e; a += blockDim.x) {
+        int dst, cf;
+        p.g.load(0, a, dst, cf);
+        if (cf > 0 && dst != in.s) {
+          p.g.push(0, a, cf, cf);
+          atomicAdd(bp.e + dst, cf);
+        }
+      }
+    }
+    __syncthreads();
+    const unsigned long long gr_thr =
+        (unsigned long long)(bp.gr_alpha * ((double)in.n + (double)(aend - abeg))) + 1;
+    int cur = 0, raw = 0, rounds = 0, since = 0;
+    unsigned long long work = 0;
+    bool need_gr = true, failed = false;
+    for (;;) {
+      if (need_gr) {
+        batch_bfs(p, in.vbase, fr0, fr1, bc, acc);
+        if (threadIdx.x == 0) {
+          bc.lcount[1] = 0;
+          bc.qraw_count[0] = bc.qraw_count[1] = 0;
+        }
+        __syncthreads();
+        cur = 0;
+        raw = 0;
+        need_gr = false;
+        work = 0;
+        since = 0;
+      }
+      if (threadIdx.x == 0)
+        bc.stop = (bp.max_rounds > 0 && rounds >= bp.max_rounds) || gtime() - t_start > bp.budget_ns;
+      __syncthreads();
+      const int nL = bc.lcount[cur];
+      if (nL == 0) break;
+      if (bc.stop) {
+        failed = true;
+        break;
+      }
+      // push phase: tiles over the active list
+      const unsigned long long w0 = acc.scanned + acc.visits;
+      {
+        const int ntiles = blockDim.x / W, tile = threadIdx.x / W;
+        int* rawcnt = &bc.qraw_count[raw];
+        const int* lq = p.lq[cur];
+        for (int i = tile; i < nL; i += ntiles) discharge_tile<TopoB, W>(p, __ldcg(lq + i), rawcnt, acc);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        if (acc.sink) {
+          atomicAdd(bp.e + in.t, acc.sink);
+          acc.sink = 0;
+        }
+        bc.lcount[cur ^ 1] = 0;
+      }
+      __syncthreads();
+      // relabel phase: threads over the raw next list
+      {
+        const int nq = bc.qraw_count[raw];
+        unsigned long long rl = 0;
+        for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+          const int u = __ldcg(p.qraw + i);
+          int m = __ldcg(p.rl_min + u);
+          int hu = __ldcg(p.lab + u);
+          const int eu = ldv(p.e + u);
+          if (m != kNone) {
+            p.rl_min[u] = kNone;
+            if (eu > __ldcg(p.rl_left + u) && hu + 1 < m) m = hu + 1;
+            int nh = (m >= p.n - 1) ? p.n : m + 1;
+            if (nh <= hu) nh = hu + 1;
+            if (nh > p.n) nh = p.n;
+            p.lab[u] = nh;
+            hu = nh;
+            ++rl;
+          }
+          if (eu > 0 && hu < p.n) {
+            p.esnap[u] = eu;
+            append(p.lq[cur ^ 1], &bc.lcount[cur ^ 1], u);
+          }
+        }
+        if (rl) atomicAdd(&acc.relabels, rl);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) bc.qraw_count[raw] = 0;
+      work += acc.scanned + acc.visits - w0;
+      __syncthreads();
+      ++rounds;
+      ++since;
+      cur ^= 1;
+      raw ^= 1;
+      if (work > gr_thr || since >= bp.gr_rounds) need_gr = true;
+    }
+    if (threadIdx.x == 0) {
+      bp.flows[id] = failed ? -1 : (long long)ldv(bp.e + in.t);
+      bp.inst_ns[id] = gtime() - t_start;
+      bp.inst_rounds[id] = rounds;
+    }
+    __syncthreads();
+  }
+}
+
+template <class T>
+wbpr_status balloc(wbpr_batch* b, T** p, size_t count) {
+  void* q = nullptr;
+  size_t bytes = sizeof(T) * std::max<size_t>(count, 1);
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) {
+    wbpr::set_last_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return WBPR_ERR_CUDA;
+  }
+  b->allocs.push_back(q);
+  b->bytes += (int64_t)bytes;
+  *p = (T*)q;
+  return WBPR_OK;
+}
+
+void batch_release(wbpr_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (void* q : b->allocs) cudaFree(q);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+#define BCK(call)                                                                 \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess) {                                                      \
+      wbpr::set_last_error(std::string(#call) + ": " + cudaGetErrorString(e_));   \
+      return WBPR_ERR_CUDA;                                                       \
+    }                                                                             \
+  } while (0)
+
+const void* kernel_for(int tile) {
+  switch (tile) {
+    case 8: return (const void*)pr_batch<8>;
+    case 16: return (const void*)pr_batch<16>;
+    case 32: return (const void*)pr_batch<32>;
+  }
+  return nullptr;
+}
+
+wbpr_status capture(wbpr_batch* b, int tile, int block, double alpha, int grr, long long max_rounds,
+                    double max_ms) {
+  if (b->exec && b->cap_tile == tile && b->cap_block == block && b->cap_alpha == alpha && b->cap_grr == grr)
+    return WBPR_OK;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  const void* fn = kernel_for(tile);
+  int occ = 0;
+  BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, block, 0));
+  if (occ <= 0) {
+    wbpr::set_last_error("batch kernel does not fit on an SM");
+    return WBPR_ERR_CUDA;
+  }
+  const int grid = std::min<int64_t>((int64_t)b->sms * occ, std::max(1, b->count));
+  BatchParams bp;
+  std::memset(&bp, 0, sizeof(bp));
+  bp.row = b->row;
+  bp.arc = b->arc;
+  bp.arx = b->arx;
+  bp.inst = b->inst;
+  bp.order = b->order;
+  bp.count = b->count;
+  bp.h = b->h;
+  bp.e = b->e;
+  bp.rl_min = b->rl_min;
+  bp.rl_left = b->rl_left;
+  bp.esnap = b->esnap;
+  bp.lq0 = b->lq[0];
+  bp.lq1 = b->lq[1];
+  bp.qraw = b->qraw;
+  bp.fr0 = b->fr[0];
+  bp.fr1 = b->fr[1];
+  bp.flows = b->flows;
+  bp.inst_ns = b->inst_ns;
+  bp.inst_rounds = b->inst_rounds;
+  bp.next = b->next;
+  bp.gr_alpha = alpha;
+  bp.gr_rounds = grr;
+  bp.max_rounds = (int)std::min<long long>(max_rounds, 1 << 30);
+  bp.budget_ns = (unsigned long long)(max_ms * 1e6);
+  cudaGraph_t graph = nullptr;
+  BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  cudaMemsetAsync(b->next, 0, sizeof(int), b->stream);
+  void* args[] = {&bp};
+  cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, b->stream);
+  BCK(cudaStreamEndCapture(b->stream, &graph));
+  cudaError_t e = cudaGraphInstantiate(&b->exec, graph, 0);
+  cudaGraphDestroy(graph);
+  BCK(e);
+  b->cap_tile = tile;
+  b->cap_block = block;
+  b->cap_alpha = alpha;
+  b->cap_grr = grr;
+  return WBPR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+wbpr_status wbpr_batch_create(const wbpr_csr* graphs, int32_t count, wbpr_batch** out) {
+  if (!out || !graphs || count < 1) return WBPR_ERR_INVALID_ARG;
+  *out = nullptr;
+  int64_t tn = 0, tm = 0;
+  for (int i = 0; i < count; ++i) {
+    const wbpr_csr* g = graphs + i;
+    wbpr_status st = wbpr::check_csr(g);
+    if (st) return st;
+    if (g->num_nodes < 2 || g->source < 0 || g->sink < 0 || g->source >= g->num_nodes ||
+        g->sink >= g->num_nodes || g->source == g->sink)
+      return WBPR_ERR_INVALID_ARG;
+    if (wbpr::max_in_capacity(g) > 0x7fffffff) return WBPR_ERR_OVERFLOW;
+    tn += g->num_nodes;
+    tm += 2 * g->num_edges;
+  }
+  if (tn >= 0x7fffffff || tm >= 0x7fffffff) return WBPR_ERR_OVERFLOW;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return WBPR_ERR_NO_DEVICE;
+  }
+  wbpr_batch* b = new wbpr_batch();
+  b->count = count;
+  b->total_n = tn;
+  b->total_arcs = tm;
+  auto fail = [&](wbpr_status s) {
+    batch_release(b);
+    return s;
+  };
+#define TRYB(x)               \
+  do {                        \
+    wbpr_status s_ = (x);     \
+    if (s_) return fail(s_);  \
+  } while (0)
+#define TRYBC(x)                                                                    \
+  do {                                                                              \
+    cudaError_t e_ = (x);                                                           \
+    if (e_ != cudaSuccess) {                                                        \
+      wbpr::set_last_error(std::string(#x) + ": " + cudaGetErrorString(e_));        \
+      return fail(WBPR_ERR_CUDA);                                                   \
+    }                                                                               \
+  } while (0)
+  TRYBC(cudaGetDevice(&b->device));
+  TRYBC(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device));
+  TRYBC(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  TRYBC(cudaEventCreate(&b->ev0));
+  TRYBC(cudaEventCreate(&b->ev1));
+  // concatenate the instances' BCSR16 rows with global ids
+  std::vector<int32_t> row((size_t)tn + 1);
+  std::vector<int32_t> arc(2 * (size_t)tm), arx(2 * (size_t)tm);
+  std::vector<BatchInst> inst((size_t)count);
+  std::vector<int64_t> size((size_t)count);
+  int64_t vb = 0, ab = 0;
+  for (int i = 0; i < count; ++i) {
+    wbpr::Bcsr16 r;
+    TRYB(wbpr::build_bcsr16(graphs + i, &r));
+    const int n = graphs[i].num_nodes;
+    const int64_t na = 2 * graphs[i].num_edges;
+    for (int u = 0; u < n; ++u) row[vb + u] = (int32_t)(ab + r.row[u]);
+    for (int64_t a = 0; a < na; ++a) {
+      arc[2 * (ab + a)] = (int32_t)(r.arc[2 * a] + vb);
+      arc[2 * (ab + a) + 1] = r.arc[2 * a + 1];
+      arx[2 * (ab + a)] = (int32_t)(r.arx[2 * a] + ab);
+      arx[2 * (ab + a) + 1] = r.arx[2 * a + 1];
+    }
+    inst[i] = BatchInst{(int)vb, n, (int)(vb + graphs[i].source), (int)(vb + graphs[i].sink)};
+    size[i] = n + na;
+    vb += n;
+    ab += na;
+  }
+  row[(size_t)tn] = (int32_t)ab;
+  std::vector<int32_t> order((size_t)count);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return size[a] > size[c]; });
+  TRYB(balloc(b, &b->row, (size_t)tn + 1));
+  TRYB(balloc(b, &b->arc, (size_t)tm));
+  TRYB(balloc(b, &b->arx, (size_t)tm));
+  TRYB(balloc(b, &b->inst, (size_t)count));
+  TRYB(balloc(b, &b->order, (size_t)count));
+  TRYBC(cudaMemcpy(b->row, row.data(), 4 * row.size(), cudaMemcpyHostToDevice));
+  if (tm) {
+    TRYBC(cudaMemcpy(b->arc, arc.data(), 4 * arc.size(), cudaMemcpyHostToDevice));
+    TRYBC(cudaMemcpy(b->arx, arx.data(), 4 * arx.size(), cudaMemcpyHostToDevice));
+  }
+  TRYBC(cudaMemcpy(b->inst, inst.data(), sizeof(BatchInst) * inst.size(), cudaMemcpyHostToDevice));
+  TRYBC(cudaMemcpy(b->order, order.data(), 4 * order.size(), cudaMemcpyHostToDevice));
+  int** vec[] = {&b->h, &b->e, &b->rl_min, &b->rl_left, &b->esnap, &b->lq[0], &b->lq[1], &b->qraw,
+                 &b->fr[0], &b->fr[1]};
+  for (int** p : vec) TRYB(balloc(b, p, (size_t)tn));
+  TRYB(balloc(b, &b->flows, (size_t)count));
+  TRYB(balloc(b, &b->inst_ns, (size_t)count));
+  TRYB(balloc(b, &b->inst_rounds, (size_t)count));
+  TRYB(balloc(b, &b->next, 1));
+  b->host_flows.resize((size_t)count);
+#undef TRYB
+#undef TRYBC
+  *out = b;
+  return WBPR_OK;
+}
+
+wbpr_status wbpr_batch_destroy(wbpr_batch* b) {
+  if (!b) return WBPR_ERR_INVALID_ARG;
+  batch_release(b);
+  return WBPR_OK;
+}
+
+int64_t wbpr_batch_device_bytes(const wbpr_batch* b) { return b ? b->bytes : 0; }
+
+wbpr_status wbpr_batch_solve(wbpr_batch* b, const wbpr_tuning* tu, int64_t* flows, float* solve_ms) {
+  if (!b) return WBPR_ERR_INVALID_ARG;
+  wbpr_tuning d;
+  wbpr_default_tuning(&d);
+  if (!tu) tu = &d;
+  int tile = tu->tile ? tu->tile : 8;
+  int block = tu->block ? tu->block : 512;
+  if ((tile != 8 && tile != 16 && tile != 32) || block < 64 || block > 512 || block % 32)
+    return WBPR_ERR_INVALID_ARG;
+  const double alpha = tu->gr_alpha > 0 ? tu->gr_alpha : 1.0;
+  const int grr = tu->gr_rounds > 0 ? tu->gr_rounds : 48;
+  const double max_ms = tu->max_ms > 0 ? tu->max_ms : 120000.0;
+  BCK(cudaSetDevice(b->device));
+  wbpr_status st = capture(b, tile, block, alpha, grr, tu->max_rounds, max_ms);
+  if (st) return st;
+  BCK(cudaEventRecord(b->ev0, b->stream));
+  BCK(cudaGraphLaunch(b->exec, b->stream));
+  BCK(cudaEventRecord(b->ev1, b->stream));
+  BCK(cudaMemcpyAsync(b->host_flows.data(), b->flows, 8 * (size_t)b->count, cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  if (solve_ms) BCK(cudaEventElapsedTime(solve_ms, b->ev0, b->ev1));
+  bool failed = false;
+  for (int i = 0; i < b->count; ++i) {
+    if (b->host_flows[i] < 0) failed = true;
+    if (flows) flows[i] = b->host_flows[i];
+  }
+  return failed ? WBPR_ERR_NO_CONVERGENCE : WBPR_OK;
+}
+
+wbpr_status wbpr_batch_instance_stats(wbpr_batch* b, float* inst_ms, int32_t* inst_rounds) {
+  if (!b) return WBPR_ERR_INVALID_ARG;
+  BCK(cudaSetDevice(b->device));
+  if (inst_ms) {
+    std::vector<unsigned long long> ns((size_t)b->count);
+    BCK(cudaMemcpy(ns.data(), b->inst_ns, 8 * ns.size(), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < b->count; ++i) inst_ms[i] = (float)(ns[i] * 1e-6);
+  }
+  if (inst_rounds) BCK(cudaMemcpy(inst_rounds, b->inst_rounds, 4 * (size_t)b->count, cudaMemcpyDeviceToHost));
+  return WBPR_OK;
+}
+
+wbpr_status wbpr_batch_autotune(wbpr_batch* b, wbpr_tuning* best, float* best_ms) {
+  if (!b || !best) return WBPR_ERR_INVALID_ARG;
+  const int tiles[] = {8, 16, 32};
+  const int blocks[] = {256, 512};
+  const double alphas[] = {0.5, 1.0, 2.0};
+  float bms = 1e30f;
+  wbpr_tuning bt;
+  wbpr_default_tuning(&bt);
+  for (int ti : tiles)
+    for (int bl : blocks)
+      for (double al : alphas) {
+        wbpr_tuning t;
+        wbpr_default_tuning(&t);
+        t.tile = ti;
+        t.block = bl;
+        t.gr_alpha = al;
+        float ms = 0;
+        wbpr_status st = wbpr_batch_solve(b, &t, nullptr, &ms);
+        if (st == WBPR_ERR_NO_CONVERGENCE) continue;
+        if (st) return st;
+        // second run: the first replay of a new capture includes its upload
+        st = wbpr_batch_solve(b, &t, nullptr, &ms);
+        if (st) continue;
+        if (ms < bms) {
+          bms = ms;
+          bt = t;
+        }
+      }
+  *best = bt;
+  if (best_ms) *best_ms = bms;
+  return bms < 1e29f ? WBPR_OK : WBPR_ERR_NO_CONVERGENCE;
+}
+
+}  // extern "C"
