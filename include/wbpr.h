@@ -86,10 +86,11 @@ typedef struct wbpr_host_csr {
 typedef struct wbpr_tuning {
   int32_t tile;          /* VC tile width: 8, 16 or 32 (0 = auto)                 */
   int32_t block;         /* threads per block: 128..1024, multiple of 32 (0=auto) */
-  int32_t heavy_degree;  /* rows longer than this are discharged by a whole      */
-                         /* block (0 = auto)                                      */
+  int32_t heavy_degree;  /* rows longer than this are discharged by a whole warp  */
+                         /* (128 arcs in flight) instead of a tile (0 = 32)       */
   int32_t blocks_per_sm; /* resident blocks per SM for the persistent grid (0=max) */
   double gr_alpha;       /* global relabel after alpha*(n + arcs) units of work   */
+                         /* (0 = 0.75)                                            */
   int64_t max_rounds;    /* push/relabel round budget (0 = unlimited)             */
   double max_ms;         /* wall-clock budget of one solve in ms (0 = 120000)     */
   int32_t verify;        /* 1: run the device certificate check after the solve  */
@@ -216,7 +217,8 @@ wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo,
 wbpr_status wbpr_read_state(wbpr_graph* g, int32_t* height, int32_t* excess,
                             int32_t* arc_flow);
 /* Event trace of the last solve run with tuning.trace = 1: the last `cap`
- * records of 4 int64 {kind | aux << 32, ns since kernel start, v0, v1};
+ * records of 6 int64 {kind | aux << 32, ns since kernel start, v0, v1, longest
+ * and shortest block work time (ns) of the phase that the record closes};
  * kinds 1 BFS level (aux bottom-up, v0 frontier, v1 frontier arcs), 2 round
  * start (aux round, v0 light list, v1 heavy entries << 32 | chunks), 3 pass A
  * end, 4 push phase end, 5 relabel end (v0 next raw queue), 6 global relabel

@@ -367,11 +367,12 @@ class DeviceGraph:
 
     def trace(self, cap: int = 1 << 14) -> np.ndarray:
         """Event records of the last solve run with trace=1: rows of
-        (kind, aux, t_ns, v0, v1)."""
-        buf = np.zeros((cap, 4), np.int64)
+        (kind, aux, t_ns, v0, v1, max_block_ns, min_block_ns)."""
+        buf = np.zeros((cap, 6), np.int64)
         n = lib().wbpr_read_trace(self._h, buf.ctypes.data_as(C.POINTER(C.c_int64)), cap)
         b = buf[:n]
-        return np.stack([b[:, 0] & 0xffffffff, b[:, 0] >> 32, b[:, 1], b[:, 2], b[:, 3]], axis=1)
+        return np.stack([b[:, 0] & 0xffffffff, b[:, 0] >> 32, b[:, 1], b[:, 2], b[:, 3], b[:, 4], b[:, 5]],
+                        axis=1)
 
     def verify(self) -> dict:
         rep = VerifyReport()

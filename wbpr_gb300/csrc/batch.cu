@@ -146,7 +146,7 @@ __device__ void batch_bfs(const Params<TopoB>& p, int vbase, int* fr0, int* fr1,
 }
 
 template <int W>
-__global__ void __launch_bounds__(512) pr_batch(BatchParams bp) {
+__global__ void __launch_bounds__(512, 2) pr_batch(BatchParams bp) {
   __shared__ BlockAcc acc;
   __shared__ BlockCtl bc;
   for (;;) {
@@ -235,9 +235,9 @@ __global__ void __launch_bounds__(512) pr_batch(BatchParams bp) {
       const unsigned long long w0 = acc.scanned + acc.visits;
       {
         const int ntiles = blockDim.x / W, tile = threadIdx.x / W;
-        int* rawcnt = &bc.qraw_count[raw];
-        const int* lq = p.lq[cur];
-        for (int i = tile; i < nL; i += ntiles) discharge_tile<TopoB, W>(p, __ldcg(lq + i), rawcnt, acc);
+        int* rawcnt = raw ? &bc.qraw_count[1] : &bc.qraw_count[0];
+        const int* lq = cur ? p.lq[1] : p.lq[0];
+        for (int i = tile; i < nL; i += ntiles) tile_discharge<TopoB, W, 4>(p, __ldcg(lq + i), 0x7fffffff, rawcnt, acc);
       }
       __syncthreads();
       if (threadIdx.x == 0) {
@@ -269,7 +269,8 @@ __global__ void __launch_bounds__(512) pr_batch(BatchParams bp) {
           }
           if (eu > 0 && hu < p.n) {
             p.esnap[u] = eu;
-            append(p.lq[cur ^ 1], &bc.lcount[cur ^ 1], u);
+            if (cur) append(p.lq[0], &bc.lcount[0], u);
+            else append(p.lq[1], &bc.lcount[1], u);
           }
         }
         if (rl) atomicAdd(&acc.relabels, rl);

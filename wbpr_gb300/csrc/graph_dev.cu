@@ -79,6 +79,8 @@ struct wbpr_graph {
   int8_t* ind = nullptr;
   int* flow_tmp = nullptr;
   long long* trace = nullptr;
+  unsigned long long* bt = nullptr;
+  unsigned long long* bt2 = nullptr;
   int trace_cap = 0;
   int trace_n = 0;
   int n_light = 0, n_medium = 0, n_heavy = 0;
@@ -498,10 +500,18 @@ wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch
   if (rc.trace) {
     if (!g->trace) {
       g->trace_cap = 1 << 14;
-      wbpr_status st = dalloc(g, &g->trace, 4 * (size_t)g->trace_cap);
+      wbpr_status st = dalloc(g, &g->trace, 6 * (size_t)g->trace_cap);
       if (st) return st;
+      st = dalloc(g, &g->bt, 4096);
+      if (st) return st;
+      st = dalloc(g, &g->bt2, 8192);
+      if (st) return st;
+      CK(cudaMemset(g->bt, 0, 8 * 4096));
+      CK(cudaMemset(g->bt2, 0, 8 * 8192));
     }
     p.trace = g->trace;
+    p.bt = g->bt;
+    p.bt2 = g->bt2;
     p.trace_cap = g->trace_cap;
   }
   const int occ = occupancy_pr(&p, rc.tile, rc.threads);
@@ -533,7 +543,7 @@ wbpr_status run(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch_ms = n
 
 void tuning_defaults(wbpr_tuning* t) {
   std::memset(t, 0, sizeof(*t));
-  t->gr_alpha = 1.0;
+  t->gr_alpha = 0.75;
   t->max_ms = 120000.0;
 }
 
@@ -554,8 +564,8 @@ wbpr_status make_cfg(wbpr_graph* g, int s, int t, wbpr_algo algo, const wbpr_tun
   if (threads < 64 || threads > 256 || threads % 32) return WBPR_ERR_INVALID_ARG;
   rc->threads = threads;
   rc->blocks_per_sm = tu->blocks_per_sm > 0 ? tu->blocks_per_sm : 0;
-  rc->heavy_deg = tu->heavy_degree > 0 ? tu->heavy_degree : (algo == WBPR_ALGO_TC ? 128 : 1024);
-  const double alpha = tu->gr_alpha > 0 ? tu->gr_alpha : 1.0;
+  rc->heavy_deg = tu->heavy_degree > 0 ? tu->heavy_degree : 32;
+  const double alpha = tu->gr_alpha > 0 ? tu->gr_alpha : 0.75;
   rc->gr_threshold = (unsigned long long)(alpha * ((double)g->n + (double)g->total_deg)) + 1;
   rc->gr_rounds = tu->gr_rounds > 0 ? tu->gr_rounds : 48;
   rc->max_rounds = tu->max_rounds;
@@ -676,14 +686,14 @@ int32_t wbpr_read_trace(wbpr_graph* g, int64_t* out, int32_t cap) {
   if (!g || !out || cap <= 0 || !g->trace) return 0;
   // the device keeps the last trace_cap records in a ring
   const int total = g->trace_n, kept = std::min(total, g->trace_cap);
-  std::vector<long long> ring(4 * (size_t)g->trace_cap);
-  if (kept > 0 && cudaMemcpy(ring.data(), g->trace, 32 * (size_t)g->trace_cap, cudaMemcpyDeviceToHost) !=
+  std::vector<long long> ring(6 * (size_t)g->trace_cap);
+  if (kept > 0 && cudaMemcpy(ring.data(), g->trace, 48 * (size_t)g->trace_cap, cudaMemcpyDeviceToHost) !=
                       cudaSuccess)
     return 0;
   const int n = std::min(cap, kept);
   for (int i = 0; i < n; ++i) {
     const int src = (total - n + i) % g->trace_cap;
-    std::memcpy(out + 4 * (size_t)i, ring.data() + 4 * (size_t)src, 32);
+    std::memcpy(out + 6 * (size_t)i, ring.data() + 6 * (size_t)src, 48);
   }
   return n;
 }

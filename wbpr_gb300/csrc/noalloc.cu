@@ -197,11 +197,11 @@ extern "C" wbpr_status wbpr_solve_bcsr_noalloc(int32_t n, int64_t num_residual_a
   p.ctl = ctl;
   p.st = stats;
   p.total_deg = num_residual_arcs;
-  p.gr_threshold = (unsigned long long)((double)n + (double)num_residual_arcs) + 1;
+  p.gr_threshold = (unsigned long long)(0.75 * ((double)n + (double)num_residual_arcs)) + 1;
   p.gr_rounds = 48;
   p.budget_ns = 120ull * 1000 * 1000 * 1000;
   p.bar_timeout_ns = 10ull * 1000 * 1000 * 1000;
-  p.heavy_deg = algo == WBPR_ALGO_TC ? 128 : 1024;
+  p.heavy_deg = 32;
   p.mode = kModeFresh;
   p.bfs_excl = s;
   const int tile = algo == WBPR_ALGO_TC ? 1 : 32;

@@ -72,7 +72,9 @@ struct Ctl {
   unsigned long long work[2];  // work done in rounds of even / odd parity
   unsigned long long dpack;    // deep list of the round: (entries << 32) | chunk items
   int bfs_heavy_next[3];
-  int pad[1];
+  int bu_found[3];  // vertices labelled by a bottom-up level, by level % 3
+  int mcount;       // materialised frontier: short rows
+  int mhcount;      //   long-row chunk items
 };
 
 struct Stats {
@@ -105,18 +107,41 @@ __device__ __forceinline__ unsigned long long gtime() {
 __device__ __forceinline__ int ldv(const int* p) { return *(const volatile int*)p; }
 
 __device__ __forceinline__ void trace_rec(long long* tr, int cap, int* n, unsigned long long t0, int kind,
-                                          int aux, long long v0, long long v1) {
+                                          int aux, long long v0, long long v1, long long v2, long long v3) {
   if (!tr) return;
   const int i = *n;
   *n = i + 1;
-  long long* r = tr + 4 * (long long)(i % cap);
+  long long* r = tr + 6 * (long long)(i % cap);
   r[0] = (long long)kind | ((long long)aux << 32);
   r[1] = (long long)(gtime() - t0);
   r[2] = v0;
   r[3] = v1;
+  r[4] = v2;
+  r[5] = v3;
 }
-#define TRACE(p, kind, aux, v0, v1) \
-  trace_rec((p).trace, (p).trace_cap, &(p).st->trace_n, (p).st->t0, (kind), (aux), (v0), (v1))
+// Record an event; v2 / v3 = longest / shortest work time of any block in
+// the phase that just ended (each block stores it in bt[] before the barrier).
+#define TRACE(p, kind, aux, v0, v1)                                                           \
+  do {                                                                                        \
+    if ((p).trace) {                                                                          \
+      unsigned long long mx_ = 0, mn_ = ~0ull;                                                \
+      for (int b_ = 0; b_ < (int)gridDim.x; ++b_) {                                           \
+        const unsigned long long d_ = *(volatile unsigned long long*)((p).bt + b_);           \
+        mx_ = d_ > mx_ ? d_ : mx_;                                                            \
+        mn_ = d_ < mn_ ? d_ : mn_;                                                            \
+      }                                                                                       \
+      trace_rec((p).trace, (p).trace_cap, &(p).st->trace_n, (p).st->t0, (kind), (aux), (v0), \
+                (v1), (long long)mx_, (long long)mn_);                                        \
+    }                                                                                         \
+  } while (0)
+// each block stores how long its share of the current phase took
+#define TRACE_BLOCK(p, tb)                                            \
+  do {                                                                \
+    if ((p).trace) {                                                  \
+      __syncthreads();                                                \
+      if (threadIdx.x == 0) (p).bt[blockIdx.x] = gtime() - (tb);      \
+    }                                                                 \
+  } while (0)
 __device__ __forceinline__ long long ldv64(const long long* p) { return *(const volatile long long*)p; }
 
 // ---------------------------------------------------------------------------
@@ -240,12 +265,16 @@ struct Params {
   int bfs_dir;   // 0: vertices that reach the root (to sink); 1: reached from the root
   int bfs_root;
   int bfs_excl;  // vertex the BFS never labels (the source during a solve), or -1
-  long long* trace;  // optional event records {kind | aux << 32, t_ns, v0, v1}
+  long long* trace;  // optional event records {kind | aux << 32, t_ns, v0, v1, max, min}
+  unsigned long long* bt;  // per-block work time of the current phase (trace only)
+  unsigned long long* bt2; // per-block time of the heavy part of the push phase (trace only)
   int trace_cap;
 };
 
 // Optional event trace (written by global thread 0 only; count in Stats).
-enum TraceKind : int { kTrLevel = 1, kTrRound = 2, kTrPassA = 3, kTrPassB = 4, kTrRelabel = 5, kTrGrEnd = 6 };
+enum TraceKind : int {
+  kTrLevel = 1, kTrRound = 2, kTrPassA = 3, kTrPassB = 4, kTrRelabel = 5, kTrGrEnd = 6, kTrSplit = 7
+};
 
 // Per-block counters, flushed to Stats once per phase.
 struct BlockAcc {
@@ -320,111 +349,6 @@ __device__ __forceinline__ void flush_acc(BlockAcc& a, Stats* st,
 }
 
 // ---------------------------------------------------------------------------
-// Push phase: one tile of W lanes (W = 1 is the thread-centric form).
-template <class Topo, int W>
-__device__ __forceinline__ void discharge_tile(const Params<Topo>& p, int u, int* rawcnt,
-                                               BlockAcc& acc) {
-  const unsigned lw = threadIdx.x & 31u;
-  const int lane = (W == 1) ? 0 : (int)(lw & (W - 1));
-  const unsigned mask =
-      (W == 32) ? 0xffffffffu : (W == 1 ? (1u << lw) : (((1u << W) - 1u) << (lw & ~(unsigned)(W - 1))));
-  const int hu = __ldcg(p.lab + u);
-  int eu = 0;
-  if (lane == 0) eu = ldv(p.e + u);
-  if (W > 1) eu = __shfl_sync(mask, eu, 0, W);
-  if (eu <= 0 || hu >= p.n) return;
-  unsigned erem = (unsigned)eu;
-  const int th = hu - 1;
-  int minh = kBig;
-  int npush = 0;
-  unsigned long long scanned = 0;
-#pragma unroll 1
-  for (int k = 0; k < Topo::kSeg; ++k) {
-    int b, e;
-    p.g.seg(u, k, b, e);
-#pragma unroll 1
-    for (int base = b; base < e; base += W) {
-      const int a = base + lane;
-      int dst = 0, cf = 0, hv = kBig;
-      if (a < e) {
-        p.g.load(k, a, dst, cf);
-        if (cf > 0) hv = __ldcg(p.lab + dst);
-      }
-      const bool adm = (cf > 0) && (hv == th);
-      const unsigned am = (W == 1) ? (unsigned)adm : __ballot_sync(mask, adm);
-      int pushed = 0;
-      if (am) {
-        unsigned incl = adm ? (unsigned)cf : 0u;
-        if (incl > erem) incl = erem;
-        unsigned prev = 0, total = incl;
-        if (W > 1) {
-#pragma unroll
-          for (int d = 1; d < W; d <<= 1) {
-            unsigned y = __shfl_up_sync(mask, incl, d, W);
-            if (lane >= d) {
-              incl += y;
-              if (incl > erem) incl = erem;
-            }
-          }
-          prev = __shfl_up_sync(mask, incl, 1, W);
-          if (lane == 0) prev = 0;
-          total = __shfl_sync(mask, incl, W - 1, W);
-        }
-        pushed = (int)(incl - prev);
-        erem -= total;
-        if (pushed > 0) {
-          p.g.push(k, a, cf, pushed);
-          ++npush;
-          if (dst == p.t) {
-            atomicAdd(&acc.sink, pushed);
-          } else {
-            int old = atomicAdd(p.e + dst, pushed);
-            if (old == 0) append(p.qraw, rawcnt, dst);
-          }
-        }
-      }
-      if (cf - pushed > 0 && hv < minh) minh = hv;
-      if (lane == 0) scanned += (unsigned long long)min(W, e - base);
-      if (erem == 0) break;
-    }
-    if (erem == 0) break;
-  }
-  if (W > 1) minh = __reduce_min_sync(mask, minh);
-  if (npush) atomicAdd(&acc.pushes, (unsigned long long)npush);
-  if (lane == 0) {
-    const int D = eu - (int)erem;
-    bool self = true;
-    if (D > 0) self = (atomicSub(p.e + u, D) - D) > 0;
-    if (erem > 0) {
-      // Pushes into u during this phase open arcs u->w with label(w) =
-      // label(u) + 1 that the scan may not have seen; the relabel phase
-      // detects them by comparing excess with (filing snapshot - pushed).
-      p.rl_min[u] = minh;
-      p.rl_left[u] = __ldcg(p.esnap + u) - D;
-    }
-    if (self) append(p.qraw, rawcnt, u);
-    atomicAdd(&acc.scanned, scanned);
-    atomicAdd(&acc.visits, 1ull);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Heavy rows (longer than heavy_deg) are cut into chunks of kChunk arcs that
-// different blocks process in two passes of the push phase:
-//   pass A  every chunk sums the residual capacity of its admissible arcs
-//           (saturated at the vertex's excess) and takes the min label over
-//           its other residual arcs;
-//   -- grid barrier --
-//   pass B  chunk c of u receives allot = min(sum_c, E - sum of earlier
-//           chunks) and pushes it along its admissible arcs in arc order;
-//           the last chunk settles excess(u) and the relabel record.
-// Total pushed = min(E, sum of all chunks), in arc order: the same pushes a
-// single thread walking the row would make.  Labels are frozen across both
-// passes, and admissible residuals of u change only by u's own pushes, so the
-// two passes see the same admissible set.
-constexpr int kItems = 8;
-constexpr int kChunk = 2048;
-
 struct VRow {  // a row as one virtual range [0, deg): segment 0 then segment 1
   int b0, d0, b1, deg;
 };
@@ -449,6 +373,132 @@ __device__ __forceinline__ void vidx(const VRow& r, int vi, int& k, int& a) {
     a = r.b1 + (vi - r.d0);
   }
 }
+
+// Push phase for one vertex: a tile of W lanes (W = 1 is the thread-centric
+// form) with Q arcs per lane in flight walks the row in order from its start,
+// with early exit, over at most `limit` arcs.  A vertex whose row is longer
+// than `limit` and that keeps excess becomes a deep entry: its remaining
+// chunks are processed by whole blocks (deep passes A and B).
+template <class Topo>
+__device__ __forceinline__ void make_deep(const Params<Topo>& p, int u, int E, int erem, int mn, int from,
+                                          int deg);
+
+template <class Topo, int W, int Q>
+__device__ __forceinline__ void tile_discharge(const Params<Topo>& p, int u, int limit, int* rawcnt,
+                                               BlockAcc& acc) {
+  const unsigned lw = threadIdx.x & 31u;
+  const int lane = (W == 1) ? 0 : (int)(lw & (W - 1));
+  const unsigned mask =
+      (W == 32) ? 0xffffffffu : (W == 1 ? (1u << lw) : (((1u << W) - 1u) << (lw & ~(unsigned)(W - 1))));
+  const int hu = __ldcg(p.lab + u);
+  int eu = 0;
+  if (lane == 0) eu = ldv(p.e + u);
+  if (W > 1) eu = __shfl_sync(mask, eu, 0, W);
+  if (eu <= 0 || hu >= p.n) return;
+  const VRow r = vrow(p.g, u);
+  const int hi = min(r.deg, limit);
+  unsigned erem = (unsigned)eu;
+  const int th = hu - 1;
+  int minh = kBig;
+  int npush = 0;
+  unsigned long long scanned = 0;
+#pragma unroll 1
+  for (int base = 0; base < hi; base += W * Q) {
+    int dst[Q], cf[Q], hv[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int vi = base + q * W + lane;
+      dst[q] = 0;
+      cf[q] = 0;
+      if (vi < hi) {
+        int kk, aa;
+        vidx(r, vi, kk, aa);
+        p.g.load(kk, aa, dst[q], cf[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) hv[q] = cf[q] > 0 ? __ldcg(p.lab + dst[q]) : kBig;
+    if (lane == 0) scanned += (unsigned long long)min(W * Q, hi - base);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const bool adm = (cf[q] > 0) && (hv[q] == th);
+      const unsigned am = (W == 1) ? (unsigned)adm : __ballot_sync(mask, adm);
+      int pushed = 0;
+      if (am && erem > 0) {
+        unsigned incl = adm ? (unsigned)cf[q] : 0u;
+        if (incl > erem) incl = erem;
+        unsigned prev = 0, total = incl;
+        if (W > 1) {
+#pragma unroll
+          for (int d = 1; d < W; d <<= 1) {
+            unsigned y = __shfl_up_sync(mask, incl, d, W);
+            if (lane >= d) {
+              incl += y;
+              if (incl > erem) incl = erem;
+            }
+          }
+          prev = __shfl_up_sync(mask, incl, 1, W);
+          if (lane == 0) prev = 0;
+          total = __shfl_sync(mask, incl, W - 1, W);
+        }
+        pushed = (int)(incl - prev);
+        erem -= total;
+        if (pushed > 0) {
+          int kk, aa;
+          vidx(r, base + q * W + lane, kk, aa);
+          p.g.push(kk, aa, cf[q], pushed);
+          ++npush;
+          if (dst[q] == p.t) {
+            atomicAdd(&acc.sink, pushed);
+          } else {
+            int old = atomicAdd(p.e + dst[q], pushed);
+            if (old == 0) append(p.qraw, rawcnt, dst[q]);
+          }
+        }
+      }
+      if (cf[q] - pushed > 0 && hv[q] < minh) minh = hv[q];
+    }
+    if (erem == 0) break;
+  }
+  if (W > 1) minh = __reduce_min_sync(mask, minh);
+  if (npush) atomicAdd(&acc.pushes, (unsigned long long)npush);
+  if (lane == 0) {
+    atomicAdd(&acc.scanned, scanned);
+    if (erem > 0 && r.deg > hi) {
+      make_deep(p, u, eu, (int)erem, minh, hi, r.deg);
+    } else {
+      const int D = eu - (int)erem;
+      bool self = true;
+      if (D > 0) self = (atomicSub(p.e + u, D) - D) > 0;
+      if (erem > 0) {
+        // Pushes into u during this phase open arcs u->w with label(w) =
+        // label(u) + 1 that the scan may not have seen; the relabel phase
+        // detects them by comparing excess with (filing snapshot - pushed).
+        p.rl_min[u] = minh;
+        p.rl_left[u] = __ldcg(p.esnap + u) - D;
+      }
+      if (self) append(p.qraw, rawcnt, u);
+      atomicAdd(&acc.visits, 1ull);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Heavy rows (longer than heavy_deg) are cut into chunks of kChunk arcs that
+// different blocks process in two passes of the push phase:
+//   pass A  every chunk sums the residual capacity of its admissible arcs
+//           (saturated at the vertex's excess) and takes the min label over
+//           its other residual arcs;
+//   -- grid barrier --
+//   pass B  chunk c of u receives allot = min(sum_c, E - sum of earlier
+//           chunks) and pushes it along its admissible arcs in arc order;
+//           the last chunk settles excess(u) and the relabel record.
+// Total pushed = min(E, sum of all chunks), in arc order: the same pushes a
+// single thread walking the row would make.  Labels are frozen across both
+// passes, and admissible residuals of u change only by u's own pushes, so the
+// two passes see the same admissible set.
+constexpr int kItems = 8;
+constexpr int kChunk = 2048;
 
 // Block-wide inclusive scan of x (saturated at cap); returns the inclusive
 // value of this thread and writes the exclusive one to *excl, the total to
@@ -509,7 +559,7 @@ __device__ __forceinline__ void settle(const Params<Topo>& p, int u, int E, int 
   if (D > 0) self = (atomicSub(p.e + u, D) - D) > 0;
   if (erem > 0) {
     p.rl_min[u] = mn;
-    p.rl_left[u] = erem;
+    p.rl_left[u] = __ldcg(p.esnap + u) - D;
   }
   if (self) append(p.qraw, rawcnt, u);
   atomicAdd(&acc.visits, 1ull);
@@ -538,25 +588,28 @@ __device__ __forceinline__ unsigned ordered_push(const Params<Topo>& p, const VR
   const int th = hu - 1;
   int npush = 0, mloc = kBig;
   unsigned long long scanned = 0;
-  for (int vb = lo; vb < hi && erem > 0; vb += blockDim.x * kItems) {
-    int dst[kItems], cf[kItems], hv[kItems], kk[kItems], aa[kItems];
+  // slabs of blockDim x ni arcs with ni = 1, 2, 4, 8, 8, ...: a vertex that
+  // places its excess early reads only the first few hundred arcs
+  int ni = 1;
+  for (int vb = lo; vb < hi && erem > 0; vb += blockDim.x * ni, ni = ni < kItems ? 2 * ni : kItems) {
+    int dst[kItems], cf[kItems], hv[kItems];
 #pragma unroll
     for (int it = 0; it < kItems; ++it) {
       const int vi = vb + it * blockDim.x + threadIdx.x;
       dst[it] = 0;
       cf[it] = 0;
-      kk[it] = 0;
-      aa[it] = 0;
-      if (vi < hi) {
-        vidx(r, vi, kk[it], aa[it]);
-        p.g.load(kk[it], aa[it], dst[it], cf[it]);
+      if (it < ni && vi < hi) {
+        int kk, aa;
+        vidx(r, vi, kk, aa);
+        p.g.load(kk, aa, dst[it], cf[it]);
       }
     }
 #pragma unroll
     for (int it = 0; it < kItems; ++it) hv[it] = cf[it] > 0 ? __ldcg(p.lab + dst[it]) : kBig;
-    scanned += (unsigned long long)min(blockDim.x * kItems, hi - vb);
-#pragma unroll 1
+    scanned += (unsigned long long)min((int)blockDim.x * ni, hi - vb);
+#pragma unroll
     for (int it = 0; it < kItems; ++it) {
+      if (it >= ni) break;  // uniform: ni is the same in every thread
       const bool adm = cf[it] > 0 && hv[it] == th;
       int pushed = 0;
       if (erem > 0 && __syncthreads_or(adm)) {
@@ -565,7 +618,9 @@ __device__ __forceinline__ unsigned ordered_push(const Params<Topo>& p, const VR
         pushed = (int)(inc - ex);
         erem -= total;
         if (pushed > 0) {
-          p.g.push(kk[it], aa[it], cf[it], pushed);
+          int kk, aa;
+          vidx(r, vb + it * blockDim.x + threadIdx.x, kk, aa);
+          p.g.push(kk, aa, cf[it], pushed);
           ++npush;
           if (dst[it] == p.t) {
             atomicAdd(&acc.sink, pushed);
@@ -584,44 +639,21 @@ __device__ __forceinline__ unsigned ordered_push(const Params<Topo>& p, const VR
   return erem;
 }
 
-// Heavy vertex, stage 1: one block discharges chunk 0 (the first kChunk arcs)
-// in order.  Most heavy vertices place all their excess there; the others
-// become deep entries whose remaining chunks are handled in parallel.
+// A vertex that kept excess after the first `from` arcs of its row: its
+// remaining arcs are cut into kChunk chunks for the deep passes.
 template <class Topo>
-__device__ void heavy_first(const Params<Topo>& p, int idx, int cur, int* rawcnt, BlockAcc& acc) {
-  __shared__ int s_u, s_E, s_hu;
-  __shared__ VRow s_r;
-  if (threadIdx.x == 0) {
-    s_u = __ldcg(p.hq[cur] + idx);
-    s_E = __ldcg(p.esnap + s_u);
-    s_hu = __ldcg(p.lab + s_u);
-    s_r = vrow(p.g, s_u);
-  }
-  __syncthreads();
-  const int u = s_u, E = s_E, hu = s_hu;
-  const VRow r = s_r;
-  __syncthreads();
-  if (E <= 0 || hu >= p.n) return;
-  int mloc;
-  const unsigned erem = ordered_push(p, r, 0, min(r.deg, kChunk), hu, (unsigned)E, &mloc, rawcnt, acc);
-  const int mn = block_min(mloc);
-  if (threadIdx.x == 0) {
-    if (erem == 0 || r.deg <= kChunk) {
-      settle(p, u, E, (int)erem, mn, rawcnt, acc);
-    } else {
-      Ctl* c = p.ctl;
-      const int nch = (r.deg - kChunk + kChunk - 1) / kChunk;
-      const unsigned long long old = atomicAdd(&c->dpack, (1ull << 32) | (unsigned long long)nch);
-      const int di = (int)(old >> 32), base = (int)(old & 0xffffffffu);
-      p.dq[di] = u;
-      p.dbase[di] = base;
-      p.dE[di] = E;
-      p.derem[di] = (int)erem;
-      p.dmin0[di] = mn;
-      for (int j = 0; j < nch; ++j) p.hown[base + j] = di;
-    }
-  }
-  __syncthreads();
+__device__ __forceinline__ void make_deep(const Params<Topo>& p, int u, int E, int erem, int mn, int from,
+                                          int deg) {
+  Ctl* c = p.ctl;
+  const int nch = (deg - from + kChunk - 1) / kChunk;
+  const unsigned long long old = atomicAdd(&c->dpack, (1ull << 32) | (unsigned long long)nch);
+  const int di = (int)(old >> 32), base = (int)(old & 0xffffffffu);
+  p.dq[di] = u;
+  p.dbase[di] = base;
+  p.dE[di] = E;
+  p.derem[di] = erem;
+  p.dmin0[di] = mn;
+  for (int j = 0; j < nch; ++j) p.hown[base + j] = di;
 }
 
 struct DeepMeta {
@@ -730,34 +762,25 @@ __device__ void deep_pass_b(const Params<Topo>& p, int k, int* rawcnt, BlockAcc&
   __syncthreads();
 }
 
-// File u as active for the next round (light list or heavy list).
-template <class Topo>
-__device__ __forceinline__ void file_active(const Params<Topo>& p, int nxt, int u, int eu) {
-  Ctl* c = p.ctl;
-  p.esnap[u] = eu;
-  if (p.g.deg(u) <= p.heavy_deg) append(p.lq[nxt], &c->lcount[nxt], u);
-  else append(p.hq[nxt], &c->hcount[nxt], u);
-}
-
-// Push phase, stage 1: heavy vertices' chunk 0 (block each) and light rows.
+// Push phase, stage 1: rows longer than heavy_deg by a warp each (128 arcs in
+// flight), shorter rows by W-lane tiles; both with early exit.
 template <class Topo, int W>
 __device__ void push_first(const Params<Topo>& p, int cur, int raw, BlockAcc& acc) {
   Ctl* c = p.ctl;
   const int nL = ldv(&c->lcount[cur]);
   const int nH = ldv(&c->hcount[cur]);
   int* rawcnt = &c->qraw_count[raw];
-  __shared__ int s_item;
+  const int lane = threadIdx.x & 31;
   for (;;) {
-    if (threadIdx.x == 0) s_item = nH > 0 ? atomicAdd(&c->heavy_next, 1) : nH;
-    __syncthreads();
-    const int it = s_item;
-    __syncthreads();
-    if (it >= nH) break;
-    heavy_first<Topo>(p, it, cur, rawcnt, acc);
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(&c->heavy_next, 1);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= nH) break;
+    tile_discharge<Topo, 32, 4>(p, __ldcg(p.hq[cur] + idx), kChunk, rawcnt, acc);
   }
+  if (p.trace && threadIdx.x == 0) p.bt2[blockIdx.x] = gtime();
   constexpr int kTpw = 32 / W;
   constexpr int kGrab = 2 * kTpw;
-  const int lane = threadIdx.x & 31;
   for (;;) {
     int base = 0;
     if (lane == 0) base = atomicAdd(&c->light_next, kGrab);
@@ -766,7 +789,7 @@ __device__ void push_first(const Params<Topo>& p, int cur, int raw, BlockAcc& ac
 #pragma unroll 1
     for (int r = 0; r < 2; ++r) {
       const int idx = base + r * kTpw + lane / W;
-      if (idx < nL) discharge_tile<Topo, W>(p, __ldcg(p.lq[cur] + idx), rawcnt, acc);
+      if (idx < nL) tile_discharge<Topo, W, 4>(p, __ldcg(p.lq[cur] + idx), kChunk, rawcnt, acc);
     }
     __syncwarp();
   }
@@ -797,30 +820,61 @@ __device__ __forceinline__ void flush_sink(int* et, BlockAcc& acc) {
   }
 }
 
+// Warp-aggregated append: all 32 lanes call it; lanes with `pred` append v.
+// One atomic per warp instead of one per element (a single frontier or queue
+// counter otherwise serialises hundreds of thousands of atomics).
+__device__ __forceinline__ void warp_append(int* q, int* cnt, int v, bool pred) {
+  const unsigned m = __ballot_sync(0xffffffffu, pred);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(cnt, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = v;
+}
+
+// Warp-level filing of active vertices (all 32 lanes call it).
+template <class Topo>
+__device__ __forceinline__ void warp_file(const Params<Topo>& p, int nxt, int u, int eu, bool pred) {
+  Ctl* c = p.ctl;
+  bool light = false;
+  if (pred) {
+    p.esnap[u] = eu;
+    light = p.g.deg(u) <= p.heavy_deg;
+  }
+  warp_append(p.lq[nxt], &c->lcount[nxt], u, pred && light);
+  warp_append(p.hq[nxt], &c->hcount[nxt], u, pred && !light);
+}
+
 // Relabel phase over the raw next queue; also files the survivors into the
 // light / heavy lists of the next round.
 template <class Topo>
 __device__ void relabel_phase(const Params<Topo>& p, int cur, int nxt, int raw, BlockAcc& acc) {
   Ctl* c = p.ctl;
   const int nq = ldv(&c->qraw_count[raw]);
+  const int lane = threadIdx.x & 31;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   unsigned long long rl = 0;
-  for (int i = gt; i < nq; i += gs) {
-    const int u = __ldcg(p.qraw + i);
-    int m = __ldcg(p.rl_min + u);
-    int hu = __ldcg(p.lab + u);
-    const int eu = ldv(p.e + u);
-    if (m != kNone) {
-      p.rl_min[u] = kNone;
-      if (eu > __ldcg(p.rl_left + u) && hu + 1 < m) m = hu + 1;
-      int nh = (m >= p.n - 1) ? p.n : m + 1;
-      if (nh <= hu) nh = hu + 1;
-      if (nh > p.n) nh = p.n;
-      p.lab[u] = nh;
-      hu = nh;
-      ++rl;
+  for (int base = gt - lane; base < nq; base += gs) {
+    const int i = base + lane;
+    int u = -1, eu = 0, hu = p.n;
+    if (i < nq) {
+      u = __ldcg(p.qraw + i);
+      int m = __ldcg(p.rl_min + u);
+      hu = __ldcg(p.lab + u);
+      eu = ldv(p.e + u);
+      if (m != kNone) {
+        p.rl_min[u] = kNone;
+        if (eu > __ldcg(p.rl_left + u) && hu + 1 < m) m = hu + 1;
+        int nh = (m >= p.n - 1) ? p.n : m + 1;
+        if (nh <= hu) nh = hu + 1;
+        if (nh > p.n) nh = p.n;
+        p.lab[u] = nh;
+        hu = nh;
+        ++rl;
+      }
     }
-    if (eu > 0 && hu < p.n) file_active(p, nxt, u, eu);
+    warp_file(p, nxt, u, eu, u >= 0 && eu > 0 && hu < p.n);
   }
   if (rl) atomicAdd(&acc.relabels, rl);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -840,38 +894,46 @@ __device__ void relabel_phase(const Params<Topo>& p, int cur, int nxt, int raw, 
 // Global relabel: level-synchronous BFS over residual arcs from `root`.
 // DIR 0 labels every vertex with its residual distance TO the root (the
 // reference's backward BFS from the sink); DIR 1 with its distance FROM the
-// root.  Unreached vertices keep label n.  Top-down expands the frontier
-// (warp per row; all warps of the grid share each row longer than kTdHeavy);
-// bottom-up lets every unvisited vertex look for a frontier neighbour
-// (8-lane tile per short row, warp per medium row, blocks over 2048-arc
-// chunks of long rows).
+// root.  Unreached vertices keep label n.  Top-down expands a frontier list
+// (warp per short row; long rows as 1024-arc chunk items shared by all warps;
+// warp-aggregated appends).  Bottom-up lets every unvisited vertex look for a
+// neighbour labelled `level` (thread / warp / block per row by length class)
+// and keeps no list: it only counts the vertices it labels and their arcs
+// (one atomic per block); if the next level goes top-down, its frontier is
+// materialised by a scan of the labels.
 constexpr int kTdHeavy = 256;
 constexpr int kTdChunk = 1024;
 
+// Frontier entry of a vertex found top-down or by a label scan: short rows
+// into fr, long rows as chunk items into frh.  All lanes call it.
 template <class Topo>
-__device__ __forceinline__ void bfs_discover(const Params<Topo>& p, int v, int fn, BlockAcc& acc) {
-  const int d = p.g.deg(v);
-  if (d > kTdHeavy) {
-    // a long row enters the frontier as ceil(d / kTdChunk) chunk items
+__device__ __forceinline__ void warp_frontier(const Params<Topo>& p, int* fcnt, int* fhcnt, int fn, int v,
+                                              bool pred, BlockAcc& acc) {
+  int d = 0;
+  if (pred) d = p.g.deg(v);
+  const bool lng = pred && d > kTdHeavy;
+  warp_append(p.fr[fn], fcnt, v, pred && !lng);
+  if (lng) {
     const int nch = (d + kTdChunk - 1) / kTdChunk;
-    const int base = atomicAdd(&p.ctl->fhcount[fn], nch);
+    const int base = atomicAdd(fhcnt, nch);
     for (int j = 0; j < nch; ++j) p.frh[fn][base + j] = make_int2(v, j);
-  } else {
-    append(p.fr[fn], &p.ctl->fcount[fn], v);
   }
-  atomicAdd((unsigned long long*)&acc.fdeg, (unsigned long long)d);
+  unsigned long long sd = (unsigned long long)d;
+  for (int o = 16; o > 0; o >>= 1) sd += __shfl_down_sync(0xffffffffu, sd, o);
+  if ((threadIdx.x & 31) == 0 && sd) atomicAdd((unsigned long long*)&acc.fdeg, sd);
 }
 
-// Top-down on a batch of up to 4 arcs per lane: heads, then labels, then the
-// twin residual of the still-unvisited heads, then the claims.
+// Top-down step over arcs [base, base + 128) of virtual row r (4 arcs per
+// lane in flight); all 32 lanes call it.
 template <class Topo, int DIR>
-__device__ __forceinline__ void td_batch(const Params<Topo>& p, const VRow& r, int v0, int vend, int stride,
-                                         int level, int fn, BlockAcc& acc, unsigned long long& arcs) {
+__device__ __forceinline__ void td_batch(const Params<Topo>& p, const VRow& r, int base, int vend, int level,
+                                         int fn, BlockAcc& acc, unsigned long long& arcs) {
+  const int lane = threadIdx.x & 31;
   int kk[4], aa[4], dst[4];
   bool ok[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    const int vi = v0 + q * stride;
+    const int vi = base + q * 32 + lane;
     ok[q] = vi < vend;
     dst[q] = -1;
     if (ok[q]) {
@@ -895,8 +957,10 @@ __device__ __forceinline__ void td_batch(const Params<Topo>& p, const VRow& r, i
       if (ok[q]) ok[q] = p.g.twin_cf(kk[q], aa[q]) > 0;
   }
 #pragma unroll
-  for (int q = 0; q < 4; ++q)
-    if (ok[q] && atomicCAS(p.lab + dst[q], p.n, level + 1) == p.n) bfs_discover(p, dst[q], fn, acc);
+  for (int q = 0; q < 4; ++q) {
+    const bool won = ok[q] && atomicCAS(p.lab + dst[q], p.n, level + 1) == p.n;
+    warp_frontier(p, &p.ctl->fcount[fn], &p.ctl->fhcount[fn], fn, dst[q], won, acc);
+  }
 }
 
 // does the arc a of row x make x adjacent to a vertex labelled `level`?
@@ -914,37 +978,51 @@ __device__ __forceinline__ bool bu_arc(const Params<Topo>& p, int k, int a, int 
 }
 
 template <class Topo, int DIR>
-__device__ void bfs_top_down(const Params<Topo>& p, int level, int fc, int fn, BlockAcc& acc) {
-  Ctl* c = p.ctl;
-  const int nf = ldv(&c->fcount[fc]);
-  const int nfh = ldv(&c->fhcount[fc]);
-  const int lane = threadIdx.x & 31;
+__device__ void bfs_top_down(const Params<Topo>& p, int level, int nf, int nfh, int fc, int fn,
+                             BlockAcc& acc) {
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   unsigned long long arcs = 0;
-  // chunk items of long rows: a warp per 1024-arc chunk, 128 arcs in flight
+  // chunk items of long rows: a warp per 1024-arc chunk
   for (int i = gw; i < nfh; i += nwarps) {
     const int2 it = __ldcg(p.frh[fc] + i);
     const VRow r = vrow(p.g, it.x);
     const int lo = it.y * kTdChunk, hi = min(r.deg, lo + kTdChunk);
-    for (int v0 = lo + lane; v0 < hi; v0 += 128) td_batch<Topo, DIR>(p, r, v0, hi, 32, level, fn, acc, arcs);
+    for (int b = lo; b < hi; b += 128) td_batch<Topo, DIR>(p, r, b, hi, level, fn, acc, arcs);
   }
   // short rows (<= kTdHeavy arcs): a warp per row
   for (int i = gw; i < nf; i += nwarps) {
     const int x = __ldcg(p.fr[fc] + i);
     const VRow r = vrow(p.g, x);
-    for (int v0 = lane; v0 < r.deg; v0 += 128) td_batch<Topo, DIR>(p, r, v0, r.deg, 32, level, fn, acc, arcs);
+    for (int b = 0; b < r.deg; b += 128) td_batch<Topo, DIR>(p, r, b, r.deg, level, fn, acc, arcs);
   }
   if (arcs) atomicAdd(&acc.bfs_arcs, arcs);
 }
 
+// Materialise the frontier (vertices labelled `level`) after a bottom-up
+// level, into fr[fc] / frh[fc] with the counters mcount / mhcount.
+template <class Topo>
+__device__ void bfs_materialise(const Params<Topo>& p, int level, int fc, BlockAcc& acc) {
+  Ctl* c = p.ctl;
+  const int lane = threadIdx.x & 31;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+  const int nall = p.n_light + p.n_medium + p.n_heavy;
+  for (int base = gt - lane; base < nall; base += gs) {
+    const int i = base + lane;
+    int v = -1;
+    if (i < nall) v = __ldg(p.cls + i);
+    const bool in = v >= 0 && __ldcg(p.lab + v) == level;
+    warp_frontier(p, &c->mcount, &c->mhcount, fc, v, in, acc);
+  }
+}
+
 template <class Topo, int DIR>
-__device__ void bfs_bottom_up(const Params<Topo>& p, int level, int fn, BlockAcc& acc) {
+__device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
   Ctl* c = p.ctl;
   const int lane = threadIdx.x & 31;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   const int gw = gt >> 5, nwarps = gs >> 5;
-  unsigned long long arcs = 0, verts = 0;
+  unsigned long long arcs = 0, verts = 0, found = 0, fdeg = 0;
   // short rows (<= kLightDeg): a thread each, 4 rows and 4 arcs in flight
   for (int i0 = gt; i0 < p.n_light; i0 += 4 * gs) {
     int xs[4];
@@ -988,7 +1066,8 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, int fn, BlockAcc
       }
       if (hit) {
         p.lab[x] = level + 1;
-        bfs_discover(p, x, fn, acc);
+        ++found;
+        fdeg += (unsigned long long)r.deg;
       }
     }
   }
@@ -998,9 +1077,11 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, int fn, BlockAcc
     if (lane == 0) ++verts;
     if (x == p.bfs_excl || __ldcg(p.lab + x) != p.n) continue;
     bool hit = false;
+    int deg = 0;
     for (int k = 0; k < Topo::kSeg && !hit; ++k) {
       int b, e;
       p.g.seg(x, k, b, e);
+      deg += e - b;
       for (int base = b; base < e; base += 128) {
         bool h = false;
 #pragma unroll
@@ -1019,11 +1100,10 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, int fn, BlockAcc
     }
     if (hit && lane == 0) {
       p.lab[x] = level + 1;
-      bfs_discover(p, x, fn, acc);
+      ++found;
+      fdeg += (unsigned long long)p.g.deg(x);
     }
   }
-  if (arcs) atomicAdd(&acc.bfs_arcs, arcs);
-  if (verts) atomicAdd(&acc.bfs_vertices, verts);
   // long rows: blocks over static 2048-arc chunks; first chunk to hit wins
   __shared__ int s_item;
   __shared__ int s_skip;
@@ -1057,10 +1137,35 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, int fn, BlockAcc
         break;
       }
     }
-    if (hit && threadIdx.x == 0 && atomicCAS(p.lab + ch.x, p.n, level + 1) == p.n)
-      bfs_discover(p, ch.x, fn, acc);
+    if (hit && threadIdx.x == 0 && atomicCAS(p.lab + ch.x, p.n, level + 1) == p.n) {
+      ++found;
+      fdeg += (unsigned long long)p.g.deg(ch.x);
+    }
   }
-  if (ha) atomicAdd(&acc.bfs_arcs, ha);
+  arcs += ha;
+  // one atomic per block for the level's count and arcs
+  for (int o = 16; o > 0; o >>= 1) {
+    found += __shfl_down_sync(0xffffffffu, found, o);
+    fdeg += __shfl_down_sync(0xffffffffu, fdeg, o);
+    arcs += __shfl_down_sync(0xffffffffu, arcs, o);
+    verts += __shfl_down_sync(0xffffffffu, verts, o);
+  }
+  __shared__ unsigned long long s_f, s_d, s_a, s_v;
+  if (threadIdx.x == 0) s_f = s_d = s_a = s_v = 0;
+  __syncthreads();
+  if (lane == 0) {
+    if (found) atomicAdd(&s_f, found);
+    if (fdeg) atomicAdd(&s_d, fdeg);
+    if (arcs) atomicAdd(&s_a, arcs);
+    if (verts) atomicAdd(&s_v, verts);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_f) atomicAdd(&c->bu_found[level % 3], (int)s_f);
+    if (s_d) atomicAdd((unsigned long long*)&acc.fdeg, s_d);
+    if (s_a) atomicAdd(&acc.bfs_arcs, s_a);
+    if (s_v) atomicAdd(&acc.bfs_vertices, s_v);
+  }
 }
 
 // Full BFS; on return every block has passed the closing barrier.  When
@@ -1069,6 +1174,7 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, int fn, BlockAcc
 template <class Topo, int DIR>
 __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, BlockAcc& acc) {
   Ctl* c = p.ctl;
+  const int lane = threadIdx.x & 31;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   for (int v = gt; v < p.n; v += gs) p.lab[v] = (v == root) ? 0 : p.n;
   if (gt == 0) {
@@ -1087,6 +1193,8 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
     c->fhcount[1] = c->fhcount[2] = 0;
     c->fdeg[0] = d;
     c->fdeg[1] = c->fdeg[2] = 0;
+    c->bu_found[0] = c->bu_found[1] = c->bu_found[2] = 0;
+    c->mcount = c->mhcount = 0;
     c->bfs_heavy_next[0] = c->bfs_heavy_next[1] = c->bfs_heavy_next[2] = 0;
     if (queues) {
       c->lcount[cur] = 0;
@@ -1100,43 +1208,71 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
   }
   if (!grid_sync(c, p.bar_timeout_ns)) return false;
   // Every block derives the direction from values that are final at the
-  // barrier (frontier size and degree of this level), so all blocks agree.
-  bool bu = false;
+  // barrier (frontier size and arcs of this level), so all blocks agree.
+  bool bu = false, prev_bu = false;
   long long visited = 0;
   for (int level = 0;; ++level) {
     const int fc = level % 3, fn = (level + 1) % 3, fr = (level + 2) % 3;
-    const int nf = ldv(&c->fcount[fc]) + ldv(&c->fhcount[fc]);
+    // frontier size: list counters after top-down, found count after bottom-up
+    const int nf = prev_bu ? ldv(&c->bu_found[(level + 2) % 3])
+                           : ldv(&c->fcount[fc]) + ldv(&c->fhcount[fc]);
     if (nf == 0) break;
     const long long fdeg = ldv64(&c->fdeg[fc]);
     visited += fdeg;
     const long long rem = p.total_deg - visited;
     if (!bu && fdeg * kBfsAlpha > rem) bu = true;
     else if (bu && (long long)nf * kBfsBeta < (long long)p.n) bu = false;
+    const bool mat = !bu && prev_bu;
+    int nl = 0, nlh = 0;
+    if (mat) {
+      // the list of the bottom-up level's finds is built by a label scan
+      bfs_materialise(p, level, fc, acc);
+      if (!grid_sync(c, p.bar_timeout_ns)) return false;
+      nl = ldv(&c->mcount);
+      nlh = ldv(&c->mhcount);
+    } else if (!bu) {
+      nl = ldv(&c->fcount[fc]);
+      nlh = ldv(&c->fhcount[fc]);
+    }
     if (gt == 0) {
+      // Each counter reset here was last read before the previous barrier
+      // and is next written after the coming one.
       c->fcount[fr] = 0;
       c->fhcount[fr] = 0;
       c->fdeg[fr] = 0;
       c->bfs_heavy_next[fn] = 0;
+      c->bu_found[fn] = 0;
+      if (!mat) c->mcount = c->mhcount = 0;
       atomicAdd(&p.st->bfs_levels, 1);
       if (bu) atomicAdd(&p.st->bu_levels, 1);
       TRACE(p, kTrLevel, bu ? 1 : 0, nf, fdeg);
     }
     if (threadIdx.x == 0) acc.fdeg = 0;
     __syncthreads();
-    if (bu) bfs_bottom_up<Topo, DIR>(p, level, fn, acc);
-    else bfs_top_down<Topo, DIR>(p, level, fc, fn, acc);
+    const unsigned long long tb = gtime();
+    if (bu) bfs_bottom_up<Topo, DIR>(p, level, acc);
+    else bfs_top_down<Topo, DIR>(p, level, nl, nlh, fc, fn, acc);
+    TRACE_BLOCK(p, tb);
     __syncthreads();
     if (threadIdx.x == 0 && acc.fdeg)
       atomicAdd((unsigned long long*)&c->fdeg[fn], (unsigned long long)acc.fdeg);
     if (!grid_sync(c, p.bar_timeout_ns)) return false;
+    prev_bu = bu;
   }
   if (queues) {
     const int nall = p.n_light + p.n_medium + p.n_heavy;
-    for (int i = gt; i < nall; i += gs) {
-      const int v = __ldg(p.cls + i);
-      if (v == p.s || v == p.t) continue;
-      const int ev = ldv(p.e + v);
-      if (ev > 0 && __ldcg(p.lab + v) < p.n) file_active(p, cur, v, ev);
+    for (int base = gt - lane; base < nall; base += gs) {
+      const int i = base + lane;
+      int v = -1, ev = 0;
+      bool pred = false;
+      if (i < nall) {
+        v = __ldg(p.cls + i);
+        if (v != p.s && v != p.t) {
+          ev = ldv(p.e + v);
+          pred = ev > 0 && __ldcg(p.lab + v) < p.n;
+        }
+      }
+      warp_file(p, cur, v, ev, pred);
     }
     if (!grid_sync(c, p.bar_timeout_ns)) return false;
   }
@@ -1145,7 +1281,7 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
 
 // ---------------------------------------------------------------------------
 template <class Topo, int W>
-__global__ void __launch_bounds__(256, 3) pr_persistent(Params<Topo> p) {
+__global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ Params<Topo> p) {
   __shared__ BlockAcc acc;
   Ctl* c = p.ctl;
   if (threadIdx.x == 0) {
@@ -1222,18 +1358,35 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(Params<Topo> p) {
     }
     const unsigned long long t0 = gtime();
     if (gt == 0) TRACE(p, kTrRound, rounds, nL, nH);
+    unsigned long long tb = gtime();
+    if (p.trace && threadIdx.x == 0) p.bt2[gridDim.x + blockIdx.x] = tb;
     push_first<Topo, W>(p, cur, raw, acc);
     if (nH > 0) {
+      TRACE_BLOCK(p, tb);
       if (!grid_sync(c, p.bar_timeout_ns)) break;
       const unsigned long long dp = *(volatile unsigned long long*)&c->dpack;
       const int nD = (int)(dp & 0xffffffffu);
-      if (gt == 0) TRACE(p, kTrPassA, rounds, (long long)(dp >> 32), nD);
+      if (gt == 0) {
+        TRACE(p, kTrPassA, rounds, (long long)(dp >> 32), nD);
+        if (p.trace) {  // longest heavy part and longest light part of any block
+          unsigned long long mh = 0, ml = 0;
+          for (int b = 0; b < (int)gridDim.x; ++b) {
+            const unsigned long long t0b = p.bt2[gridDim.x + b], th = p.bt2[b];
+            const unsigned long long tot = p.bt[b];
+            mh = max(mh, th - t0b);
+            ml = max(ml, tot > th - t0b ? tot - (th - t0b) : 0ull);
+          }
+          TRACE(p, kTrSplit, rounds, (long long)mh, (long long)ml);
+        }
+      }
+      tb = gtime();
       if (nD > 0) {
         push_deep<Topo>(p, 0, nD, raw, acc);
         if (!grid_sync(c, p.bar_timeout_ns)) break;
         push_deep<Topo>(p, 1, nD, raw, acc);
       }
     }
+    TRACE_BLOCK(p, tb);
     flush_sink(p.e + p.t, acc);
     flush_acc(acc, p.st, &c->work[raw]);
     if (!grid_sync(c, p.bar_timeout_ns)) break;
@@ -1241,7 +1394,9 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(Params<Topo> p) {
       push_ns += gtime() - t0;
       TRACE(p, kTrPassB, rounds, 0, 0);
     }
+    tb = gtime();
     relabel_phase<Topo>(p, cur, cur ^ 1, raw, acc);
+    TRACE_BLOCK(p, tb);
     flush_acc(acc, p.st, &c->work[raw]);
     if (gt == 0) {
       round_ns += gtime() - t0;
