@@ -255,14 +255,16 @@ def run_ours(args) -> None:
     achieved = alg / (launch_ms * 1e-3) / 1e9
     prof = profile_traffic()
     traffic = prof.get("dram_bytes_per_launch") if prof else None
-    h2d = 32 * g.m + 8 * (g.n + 1)
+    # the input CSR crosses once (offsets, heads, capacities); BCSR is built in HBM
+    h2d = 8 * g.m + 4 * (g.n + 1) if args.layout == "bcsr" else 32 * g.m + 8 * (g.n + 1)
     dg.close()
     # e2e through the C ABI from host buffers
     e2e_steps = min(args.steps, args.e2e_steps)
-    e2e_s = 0.0
+    e2e_s = create_s = 0.0
     for _ in range(e2e_steps):
         t1 = time.perf_counter()
         with W.DeviceGraph(g, args.layout) as dd:
+            create_s += time.perf_counter() - t1
             r = dd.solve(args.algo, g.s, g.t, **tuning)
         e2e_s += time.perf_counter() - t1
         if r.flow != flow:
@@ -272,7 +274,10 @@ def run_ours(args) -> None:
     if e2e_steps > 0:
         e2e = {"value": world * e2e_steps * g.m / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": 8 + 128, "steps": e2e_steps,
-               "path": "wbpr_graph_create (host BCSR build + H2D) + wbpr_solve + result read-back"}
+               "create_ms": create_s * 1e3 / e2e_steps, "ms_per_step": e2e_s * 1e3 / e2e_steps,
+               "path": ("wbpr_graph_create (H2D of the input CSR, BCSR built on the device) + wbpr_solve"
+                        " + result read-back" if args.layout == "bcsr" else
+                        "wbpr_graph_create (host RCSR build + H2D) + wbpr_solve + result read-back")}
     if rank == 0:
         cpu = cpu_baseline_once() if world == 1 and not args.no_cpu_baseline else None
         workload = "rmat22_ef16_cap1-100" if args.scale == 22 else f"rmat{args.scale}_ef16_cap1-100 (profiling size)"
@@ -302,6 +307,183 @@ def run_ours(args) -> None:
     d.close()
 
 
+# ---------------------------------------------------------------------------
+# The other workloads (one JSON line each; `--config N`).  The default run is
+# the R-MAT line above; these are measured on request.
+def _line(metric, value, unit, hib, workload, **extra):
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "higher_is_better": hib,
+         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generators)",
+         "config": {"workload": workload}}
+    d.update(extra)
+    print(json.dumps(d), flush=True)
+
+
+def _serial_ms(g) -> float:
+    import oracle
+
+    t0 = time.perf_counter()
+    v, st = oracle.serial_maxflow(g.n, g.off, g.dst, g.cap, g.s, g.t)
+    if st != 0:
+        raise RuntimeError(f"serial status {st}")
+    return (time.perf_counter() - t0) * 1e3, v
+
+
+def config0(args):
+    """GENRMF a=8, b=16 (1,024 vertices, 4,544 arcs), seeds 0..K-1: TC over
+    RCSR (and VC beside it); each solve's certificate checked on the device."""
+    import wbpr_gb300 as W
+
+    seeds = range(args.instances or 20)
+    tc, vc, flows = [], [], []
+    for sd in seeds:
+        g = W.gen_genrmf(8, 16, 1, 10000, sd)
+        with W.DeviceGraph(g, "rcsr") as d:
+            for _ in range(args.warmup):
+                d.solve("tc", g.s, g.t)
+            r = [d.solve("tc", g.s, g.t) for _ in range(args.steps)]
+            if not d.verify()["ok"] or len({x.flow for x in r}) != 1:
+                raise AssertionError("certificate failed")
+            tc += [x.solve_ms for x in r]
+            flows.append(r[0].flow)
+            r = [d.solve("vc", g.s, g.t) for _ in range(args.steps)]
+            if {x.flow for x in r} != {flows[-1]}:
+                raise AssertionError("tc/vc differ")
+            vc += [x.solve_ms for x in r]
+    cpu = None
+    if not args.no_cpu_baseline:
+        ms, v = _serial_ms(W.gen_genrmf(8, 16, 1, 10000, 0))
+        if v != flows[0]:
+            raise AssertionError("serial flow differs")
+        cpu = {"value": ms, "unit": "ms", "cores": 1, "kind": "port",
+               "sample": "seed 0 instance: oracle restatement of maxflow-serial"}
+    _line("max-flow solve ms (GENRMF 8x16, TC over RCSR)", statistics.median(tc), "ms", False,
+          f"genrmf_a8_b16_cap1-10000 seeds 0..{len(seeds) - 1}", steps=args.steps, warmup=args.warmup,
+          vc_ms_median=statistics.median(vc), tc_ms_p90=sorted(tc)[int(0.9 * (len(tc) - 1))],
+          flows_first=flows[:5], verified=True, cpu_baseline=cpu)
+
+
+def config2(args):
+    """Unit-capacity bipartite matching, 2M x 2M, Zipf(2.0) left degrees."""
+    import wbpr_gb300 as W
+
+    g = W.gen_bipartite(2000000, 2000000, 2.0, 4096, 1)
+    with W.DeviceGraph(g, "bcsr") as d:
+        for _ in range(args.warmup):
+            d.solve("vc", g.s, g.t)
+        r = [d.solve("vc", g.s, g.t) for _ in range(args.steps)]
+        rep = d.verify()
+    if not rep["ok"] or len({x.flow for x in r}) != 1:
+        raise AssertionError(f"certificate failed: {rep}")
+    ms = statistics.median(x.solve_ms for x in r)
+    _line("max-flow MTEPS (bipartite matching, unit capacity)", g.m / ms / 1e3, "MTEPS", True,
+          f"bipartite_L2M_R2M_zipf2.0 (n={g.n}, m={g.m})", steps=args.steps, warmup=args.warmup,
+          solve_ms=ms, gr_ms=r[-1].gr_ms, rounds=r[-1].rounds, matching=r[0].flow, verified=True)
+
+
+def _config3_instances(count: int, seed: int = 7):
+    import numpy as np
+    import wbpr_gb300 as W
+
+    rng = np.random.default_rng(seed)
+    aw = np.arange(4, 33)
+    aw_p = (1.0 / aw) / (1.0 / aw).sum()  # log-uniform over the integers
+    bw = np.arange(4, 65)
+    bw_p = (1.0 / bw) / (1.0 / bw).sum()
+    out = []
+    for i in range(count):
+        if i % 2 == 0:
+            out.append(W.gen_genrmf(int(rng.choice(aw, p=aw_p)), int(rng.choice(bw, p=bw_p)), 1, 10000, i))
+        else:
+            out.append(W.gen_layered(int(rng.integers(8, 65)), int(rng.integers(16, 513)), 3, 6, 1, 1000, i))
+    return out
+
+
+def config3(args):
+    """4,096 uneven instances in one persistent launch (CUDA graph replay,
+    autotuned) against a loop of the plain solver over a sample."""
+    import numpy as np
+    import wbpr_gb300 as W
+
+    count = args.instances or 4096
+    gs = _config3_instances(count)
+    with W.Batch(gs) as b:
+        best, _ = b.autotune()
+        for _ in range(args.warmup):
+            b.solve(best)
+        runs = [b.solve(best) for _ in range(args.steps)]
+        flows = runs[0][0]
+        if any(not np.array_equal(f, flows) for f, _ in runs):
+            raise AssertionError("batch flows differ between steps")
+        ims, rounds = b.instance_stats()
+    ms = statistics.median(x[1] for x in runs)
+    idx = np.random.default_rng(1).choice(count, min(count, 96), replace=False)
+    lat = []
+    for i in idx:
+        with W.DeviceGraph(gs[i], "bcsr") as d:
+            d.solve("vc", gs[i].s, gs[i].t)
+            r = d.solve("vc", gs[i].s, gs[i].t)
+            if r.flow != flows[i] or not d.verify()["ok"]:
+                raise AssertionError(f"instance {i}: batch {flows[i]} plain {r.flow}")
+            lat.append(r.solve_ms)
+    loop = len(lat) / sum(lat) * 1e3
+    _line("batched max-flow instances/s (exact flows)", count / ms * 1e3, "instances/s", True,
+          f"{count} instances: half GENRMF a,b log-uniform [4,32]x[4,64], half layered 8-64 x 16-512",
+          steps=args.steps, warmup=args.warmup, batch_ms=ms,
+          tuning={"tile": best.tile, "block": best.block, "gr_alpha": best.gr_alpha},
+          inst_p50_ms=float(np.percentile(ims, 50)), inst_p99_ms=float(np.percentile(ims, 99)),
+          looped_plain={"instances_per_s": loop, "sample": len(lat), "p50_ms": float(np.percentile(lat, 50)),
+                        "p99_ms": float(np.percentile(lat, 99))},
+          speedup_vs_loop=count / ms * 1e3 / loop, n_total=int(sum(g.n for g in gs)),
+          m_total=int(sum(g.m for g in gs)))
+
+
+def config4(args):
+    """512x512 graph-cut grids: forward solve, then both adjoint sides; the
+    cut of each indicator must equal the flow, and a few arcs of the first
+    grid are checked against +-1 re-solves."""
+    import numpy as np
+    import wbpr_gb300 as W
+
+    grids = args.instances or 32
+    fwd, adj, flows = [], [], []
+    fd_checked = 0
+    for sd in range(grids):
+        g = W.gen_grid(512, 512, sd)
+        with W.DeviceGraph(g, "bcsr") as d:
+            for _ in range(args.warmup if sd == 0 else 0):
+                d.solve("vc", g.s, g.t)
+            r = d.solve("vc", g.s, g.t)
+            i0, ms0 = d.mincut_adjoint(0)
+            i1, ms1 = d.mincut_adjoint(1)
+        cap = g.cap.astype(np.int64)
+        if int((i0 * cap).sum()) != r.flow or int((i1 * cap).sum()) != r.flow:
+            raise AssertionError("cut != flow")
+        fwd.append(r.solve_ms)
+        adj.append(ms0 + ms1)
+        flows.append(r.flow)
+        if sd == 0:
+            rng = np.random.default_rng(0)
+            for e in rng.choice(g.m, 6, replace=False):
+                up = g.cap.copy()
+                up[e] += 1
+                dp = W.maxflow(W.Graph(g.n, g.off, g.dst, up, g.s, g.t)) - r.flow
+                dm = 0
+                if g.cap[e] > 0:
+                    dn = g.cap.copy()
+                    dn[e] -= 1
+                    dm = r.flow - W.maxflow(W.Graph(g.n, g.off, g.dst, dn, g.s, g.t))
+                for ind in (i0, i1):
+                    if not (dp <= ind[e] and (g.cap[e] == 0 or ind[e] <= dm)):
+                        raise AssertionError(f"finite difference at arc {e}")
+                fd_checked += 1
+    pct = 100.0 * sum(adj) / sum(fwd)
+    _line("adjoint ms as % of forward solve (512x512 grids)", pct, "%", False,
+          f"{grids} grids 512x512, 4-connected, seeds 0..{grids - 1}", steps=grids, warmup=args.warmup,
+          forward_ms_median=statistics.median(fwd), adjoint_ms_median=statistics.median(adj),
+          grids_per_s=grids / (sum(fwd) + sum(adj)) * 1e3, fd_arcs_checked=fd_checked,
+          flows_first=flows[:3], verified=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -318,11 +500,17 @@ def main() -> None:
     ap.add_argument("--scale", type=int, default=22, help="R-MAT scale (22 is the benchmark; smaller "
                     "sizes are for profiling captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU sample (profiling)")
+    ap.add_argument("--config", type=int, choices=[0, 1, 2, 3, 4], default=1,
+                    help="1: the R-MAT benchmark (default); 0: GENRMF 8x16; 2: bipartite matching; "
+                    "3: batched instances; 4: grids with the adjoint")
+    ap.add_argument("--instances", type=int, default=0, help="instances/seeds/grids for --config 0/3/4")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.config != 1:
+        {0: config0, 2: config2, 3: config3, 4: config4}[args.config](args)
     else:
         run_ours(args)
 

@@ -208,6 +208,13 @@ wbpr_status wbpr_graph_create(const wbpr_csr* g, wbpr_layout layout,
 wbpr_status wbpr_graph_destroy(wbpr_graph* g);
 /* Bytes of device memory held by the handle. */
 int64_t wbpr_graph_device_bytes(const wbpr_graph* g);
+/* Copy a BCSR handle's residual graph, as built on the device, back to host
+ * buffers in the format of wbpr_build_bcsr (offsets[n+1], destinations[2m],
+ * capacities[2m], backward_idx[2m]; any may be NULL).  The device build is
+ * the same arrays as the host build, entry for entry.  INVALID_ARG for an
+ * RCSR handle. */
+wbpr_status wbpr_graph_read_bcsr(const wbpr_graph* g, int32_t* offsets, int32_t* destinations,
+                                 int32_t* capacities, int32_t* backward_idx);
 /* Fresh solve: reset residuals to capacities, preflow from s, push/relabel to
  * a maximum preflow.  Result flow = excess(t). s/t = -1 use the graph's. */
 wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo,

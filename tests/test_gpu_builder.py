@@ -1,0 +1,78 @@
+"""On-device BCSR build (wbpr_graph_create, BCSR layout): the residual graph
+it leaves in HBM must be the host builder's (wbpr_build_bcsr, the layout of
+maxflow-bcsr/src/graph.cpp:317-360) entry for entry -- offsets, heads,
+capacities and twin indices -- for every shape the sort and the length
+classes see: empty rows, isolated vertices, parallel arcs, rows longer than
+the push chunk, heads that need one to four radix passes."""
+import numpy as np
+import pytest
+
+import wbpr_gb300 as W
+from conftest import graph_of
+
+pytestmark = pytest.mark.gpu
+
+
+def same_as_host(g):
+    with W.DeviceGraph(g, "bcsr") as d:
+        dev = d.read_bcsr()
+    host = W.build_bcsr(g)
+    for a, b, name in zip(dev, host, ("offsets", "destinations", "capacities", "backward_idx")):
+        assert np.array_equal(a, b), name
+
+
+def random_graph(n, m, seed, max_cap=100, hot=None):
+    rng = np.random.default_rng(seed)
+    src = rng.integers(0, n, m)
+    dst = rng.integers(0, n, m)
+    if hot is not None:  # a vertex with many arcs in and out
+        k = m // 3
+        src[:k] = hot
+        dst[k:2 * k] = hot
+    cap = rng.integers(0, max_cap, m)
+    return W.Graph.from_arcs(n, src, dst, cap, 0, n - 1)
+
+
+def test_golden_cases(golden):
+    for case in golden:
+        same_as_host(graph_of(case))
+
+
+@pytest.mark.parametrize("n,m", [(2, 1), (3, 0), (7, 40), (257, 3000), (300, 20000), (65537, 200000)])
+def test_random_shapes(n, m):
+    same_as_host(random_graph(n, m, n + m))
+
+
+def test_long_rows_and_hot_vertex():
+    # rows far longer than the 2048-arc push chunk, in and out of one vertex
+    same_as_host(random_graph(5000, 120000, 3, hot=17))
+
+
+def test_four_radix_passes():
+    # heads need 25 bits: four 8-bit passes
+    same_as_host(random_graph((1 << 24) + 5, 100000, 4))
+
+
+def test_generators():
+    same_as_host(W.gen_rmat(14, 16, seed=2))
+    same_as_host(W.gen_genrmf(6, 8, 1, 100, 3))
+    same_as_host(W.gen_bipartite(3000, 3000, 4.0, 8192, 5))
+    same_as_host(W.gen_grid(40, 30, 1))
+
+
+def test_device_overflow_check():
+    g = W.Graph.from_arcs(3, [0, 0, 1, 1], [1, 2, 2, 2], [2**31 - 1, 2**31 - 1, 2**31 - 1, 5], 0, 2)
+    with pytest.raises(W.WbprError) as ei:
+        W.DeviceGraph(g, "bcsr")
+    assert ei.value.status == 4
+    # at the limit exactly it builds
+    g = W.Graph.from_arcs(3, [0, 1], [2, 2], [2**31 - 2, 1], 0, 2)
+    same_as_host(g)
+
+
+def test_rcsr_handle_has_no_bcsr():
+    g = random_graph(50, 200, 1)
+    with W.DeviceGraph(g, "rcsr") as d:
+        with pytest.raises(W.WbprError) as ei:
+            d.read_bcsr()
+        assert ei.value.status == 1

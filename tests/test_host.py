@@ -175,10 +175,11 @@ def test_rmat_independent_of_thread_count():
 
 
 def test_overflowing_capacities_are_rejected(has_gpu):
-    # sum of capacities into t exceeds int32: refused before any device work
+    # sum of capacities into t exceeds int32: the RCSR layout refuses it on the
+    # host before any device work (BCSR checks while it builds on the device)
     g = W.Graph.from_arcs(3, [0, 0, 1, 1], [1, 2, 2, 2], [2**31 - 1, 2**31 - 1, 2**31 - 1, 5], 0, 2)
     with pytest.raises(W.WbprError) as ei:
-        W.DeviceGraph(g, "bcsr")
+        W.DeviceGraph(g, "rcsr")
     assert ei.value.status == 4
 
 

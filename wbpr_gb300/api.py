@@ -84,7 +84,7 @@ EXPORTED = [
     "wbpr_write_snap_bin", "wbpr_write_dimacs", "wbpr_host_csr_copy", "wbpr_host_csr_free",
     "wbpr_gen_genrmf", "wbpr_gen_rmat", "wbpr_gen_bipartite", "wbpr_gen_layered", "wbpr_gen_grid",
     "wbpr_build_rcsr", "wbpr_build_bcsr", "wbpr_build_bcsr2", "wbpr_graph_create",
-    "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_solve", "wbpr_read_state",
+    "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_graph_read_bcsr", "wbpr_solve", "wbpr_read_state",
     "wbpr_verify", "wbpr_mincut_adjoint", "wbpr_rcsr_preflow", "wbpr_rcsr_push_relabel",
     "wbpr_read_trace", "wbpr_solve_bcsr_noalloc", "wbpr_batch_create", "wbpr_batch_destroy",
     "wbpr_batch_device_bytes", "wbpr_batch_solve", "wbpr_batch_instance_stats", "wbpr_batch_autotune",
@@ -130,6 +130,7 @@ def lib() -> C.CDLL:
         "wbpr_graph_create": (C.c_int, [C.POINTER(CsrView), C.c_int, C.POINTER(vp)]),
         "wbpr_graph_destroy": (C.c_int, [vp]),
         "wbpr_graph_device_bytes": (C.c_int64, [vp]),
+        "wbpr_graph_read_bcsr": (C.c_int, [vp, _i32p, _i32p, _i32p, _i32p]),
         "wbpr_solve": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int, C.POINTER(Tuning), C.POINTER(Result)]),
         "wbpr_read_state": (C.c_int, [vp, _i32p, _i32p, _i32p]),
         "wbpr_read_trace": (C.c_int32, [vp, C.POINTER(C.c_int64), C.c_int32]),
@@ -378,6 +379,14 @@ class DeviceGraph:
         rep = VerifyReport()
         _check(lib().wbpr_verify(self._h, C.byref(rep)), "wbpr_verify")
         return rep.as_dict()
+
+    def read_bcsr(self):
+        """The device-built BCSR arrays, as build_bcsr returns them."""
+        off = np.zeros(self.n + 1, np.int32)
+        k = max(2 * self.m, 1)
+        dst, cap, bidx = (np.zeros(k, np.int32) for _ in range(3))
+        _check(lib().wbpr_graph_read_bcsr(self._h, _p(off), _p(dst), _p(cap), _p(bidx)), "wbpr_graph_read_bcsr")
+        return off, dst[:2 * self.m], cap[:2 * self.m], bidx[:2 * self.m]
 
     def read_state(self):
         h = np.zeros(self.n, np.int32)

@@ -254,6 +254,404 @@ __global__ void flow_kernel(const int* ioff, const int* row, const int2* arc, co
 }
 
 // ---------------------------------------------------------------------------
+// On-device BCSR16 builder.  Produces exactly the layout of the host builder:
+// row u holds its forward arcs in input order, then one twin per arc entering
+// u in increasing input-arc order.  With inoff = exclusive scan of in-degrees,
+// row[u] = off[u] + inoff[u], the forward slot of input arc i (tail u) is
+// i + inoff[u], and the twin of the arc at position p of the arcs stably
+// sorted by head v is off[v + 1] + p.  The stable sort is an LSD radix sort
+// by head over warp tiles; its last pass writes only that position p.
+__global__ void db_count(const int* dst, const int* cap, long long m, int* indeg, unsigned long long* incap) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+    const int v = dst[i];
+    atomicAdd(indeg + v, 1);
+    atomicAdd(incap + v, (unsigned long long)(cap ? cap[i] : 1));
+  }
+}
+__global__ void db_max(const unsigned long long* incap, int n, unsigned long long* out) {
+  unsigned long long mx = 0;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) mx = max(mx, incap[u]);
+  for (int d = 16; d; d >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(out, mx);
+}
+__global__ void db_row(const int* off, const int* inoff, int n, int* row) {
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u <= n; u += gridDim.x * blockDim.x) row[u] = off[u] + inoff[u];
+}
+
+constexpr int kScanTile = 4096;  // 1024 threads x 4 items
+__global__ void __launch_bounds__(1024) db_scan_tiles(int* data, long long count, int* sums) {
+  __shared__ int s_w[32];
+  const long long base = (long long)blockIdx.x * kScanTile + 4LL * threadIdx.x;
+  int v[4], t = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k] = base + k < count ? data[base + k] : 0;
+    t += v[k];
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int inc = t;
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, d);
+    if (lane >= d) inc += y;
+  }
+  if (lane == 31) s_w[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    int w = s_w[lane];
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, d);
+      if (lane >= d) w += y;
+    }
+    s_w[lane] = w;  // inclusive warp totals
+  }
+  __syncthreads();
+  int run = (wid ? s_w[wid - 1] : 0) + inc - t;  // exclusive prefix of this thread
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (base + k < count) data[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == blockDim.x - 1 && sums) sums[blockIdx.x] = run;
+}
+__global__ void db_scan_add(int* data, long long count, const int* sums) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+    data[i] += sums[i / kScanTile];
+}
+
+// radix sort by head: one warp tile = kSortRounds x 32 arcs, striped so that
+// (round, lane) order is input order and match_any ranks are stable
+constexpr int kSortRounds = 64;
+constexpr int kSortTile = kSortRounds * 32;
+__global__ void __launch_bounds__(256) db_sort_hist(const int* key, long long m, int shift, int ntiles, int* hist) {
+  __shared__ int cnt[8][256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int tile = blockIdx.x * 8 + w;
+  for (int b = lane; b < 256; b += 32) cnt[w][b] = 0;
+  __syncwarp();
+  if (tile >= ntiles) return;
+  const long long base = (long long)tile * kSortTile;
+  for (int r = 0; r < kSortRounds; ++r) {
+    const long long i = base + r * 32 + lane;
+    const int d = i < m ? (key[i] >> shift) & 255 : 256;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    if (d < 256 && lane == __ffs(peers) - 1) cnt[w][d] += __popc(peers);
+    __syncwarp();
+  }
+  for (int b = lane; b < 256; b += 32) hist[(long long)b * ntiles + tile] = cnt[w][b];
+}
+__global__ void __launch_bounds__(256) db_sort_scatter(const int* kin, const int* vin, long long m, int shift,
+                                                       int ntiles, const int* hist, int* kout, int* vout,
+                                                       int* pos_of) {
+  __shared__ int off[8][256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int tile = blockIdx.x * 8 + w;
+  if (tile >= ntiles) return;
+  for (int b = lane; b < 256; b += 32) off[w][b] = hist[(long long)b * ntiles + tile];
+  __syncwarp();
+  const unsigned lt = (1u << lane) - 1;
+  const long long base = (long long)tile * kSortTile;
+  for (int r = 0; r < kSortRounds; ++r) {
+    const long long i = base + r * 32 + lane;
+    const bool ok = i < m;
+    const int k = ok ? kin[i] : 0;
+    const int d = ok ? (k >> shift) & 255 : 256;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    if (ok) {
+      const int pos = off[w][d] + __popc(peers & lt);
+      const int val = vin ? vin[i] : (int)i;
+      if (pos_of) {
+        pos_of[val] = pos;
+      } else {
+        kout[pos] = k;
+        vout[pos] = val;
+      }
+    }
+    __syncwarp();
+    if (ok && lane == __ffs(peers) - 1) off[w][d] += __popc(peers);
+    __syncwarp();
+  }
+}
+
+// one warp per 256 input arcs: tails by a binary search narrowed to the
+// warp's row range, then both slots of every pair
+__global__ void db_fill(const int* off, const int* inoff, const int* dst, const int* cap, const int* pos_of,
+                        int n, long long m, int2* arc, int2* arx) {
+  const int lane = threadIdx.x & 31;
+  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long base = (blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5)) * 256; base < m;
+       base += nw * 256) {
+    int u_edge = 0;
+    if (lane < 2) {
+      const long long x = lane ? min(base + 255, m - 1) : base;
+      int lo = 0, hi = n;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= x) lo = mid;
+        else hi = mid;
+      }
+      u_edge = lo;
+    }
+    const int u_lo = __shfl_sync(0xffffffffu, u_edge, 0);
+    const int u_hi = __shfl_sync(0xffffffffu, u_edge, 1) + 1;
+#pragma unroll 4
+    for (int k = 0; k < 8; ++k) {
+      const long long i = base + k * 32 + lane;
+      if (i >= m) break;
+      int lo = u_lo, hi = u_hi;  // off[lo] <= i < off[hi]
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= i) lo = mid;
+        else hi = mid;
+      }
+      const int u = lo, v = dst[i], c = cap ? cap[i] : 1;
+      const int f = (int)i + __ldg(inoff + u);
+      const int r = __ldg(off + v + 1) + pos_of[i];
+      arc[f] = make_int2(v, c);
+      arx[f] = make_int2(r, c);
+      arc[r] = make_int2(u, 0);
+      arx[r] = make_int2(f, 0);
+    }
+  }
+}
+
+// length classes (flags for three stable compactions) and the chunk counts
+// cnt: [0] rows > kTdHeavy [1] their top-down chunk items [2] push-phase chunk bound
+__global__ void db_classify(const int* row, int n, int* f0, int* f1, int* f2, unsigned long long* cnt) {
+  unsigned long long a = 0, b = 0, c = 0;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u <= n; u += gridDim.x * blockDim.x) {
+    const int d = u < n ? row[u + 1] - row[u] : 0;
+    f0[u] = d > 0 && d <= kLightDeg;
+    f1[u] = d > kLightDeg && d <= kHeavyDeg;
+    f2[u] = d > kHeavyDeg;
+    c += (d + kChunk - 1) / kChunk;
+    if (d > kTdHeavy) {
+      a += 1;
+      b += (d + kTdChunk - 1) / kTdChunk;
+    }
+  }
+  for (int s = 16; s; s >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, s);
+    b += __shfl_xor_sync(0xffffffffu, b, s);
+    c += __shfl_xor_sync(0xffffffffu, c, s);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (a) atomicAdd(cnt + 0, a);
+    if (b) atomicAdd(cnt + 1, b);
+    if (c) atomicAdd(cnt + 2, c);
+  }
+}
+__global__ void db_cls_scatter(const int* row, int n, const int* s0, const int* s1, const int* s2, int* cls) {
+  const int n0 = s0[n], n01 = n0 + s1[n];
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    const int d = row[u + 1] - row[u];
+    if (d == 0) continue;
+    if (d <= kLightDeg) cls[s0[u]] = u;
+    else if (d <= kHeavyDeg) cls[n0 + s1[u]] = u;
+    else cls[n01 + s2[u]] = u;
+  }
+}
+__global__ void db_heavy_chunks(const int* row, const int* hcls, int nh, int* nch) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j <= nh; j += gridDim.x * blockDim.x) {
+    if (j == nh) {
+      nch[j] = 0;
+    } else {
+      const int u = hcls[j];
+      nch[j] = (row[u + 1] - row[u] + kChunk - 1) / kChunk;
+    }
+  }
+}
+__global__ void db_bch_fill(const int* row, const int* hcls, int nh, const int* cbase, int4* bch) {
+  for (int j = blockIdx.x; j < nh; j += gridDim.x) {
+    const int u = hcls[j], b = row[u], e = row[u + 1];
+    const int nc = cbase[j + 1] - cbase[j];
+    for (int k = threadIdx.x; k < nc; k += blockDim.x)
+      bch[cbase[j] + k] = make_int4(u, 0, b + k * kChunk, min(e, b + (k + 1) * kChunk));
+  }
+}
+
+// exclusive scan of data[0, count) in place (int32 totals)
+wbpr_status device_scan(int* data, long long count, cudaStream_t st) {
+  const long long tiles = (count + kScanTile - 1) / kScanTile;
+  if (tiles <= 1) {
+    db_scan_tiles<<<1, 1024, 0, st>>>(data, count, nullptr);
+    CK(cudaGetLastError());
+    return WBPR_OK;
+  }
+  int* sums = nullptr;
+  CK(cudaMallocAsync(&sums, sizeof(int) * tiles, st));
+  db_scan_tiles<<<(unsigned)tiles, 1024, 0, st>>>(data, count, sums);
+  cudaError_t e = cudaGetLastError();
+  wbpr_status r = e == cudaSuccess ? device_scan(sums, tiles, st) : WBPR_ERR_CUDA;
+  if (r == WBPR_OK) {
+    db_scan_add<<<1024, 256, 0, st>>>(data, count, sums);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) r = WBPR_ERR_CUDA;
+  }
+  cudaFreeAsync(sums, st);
+  if (e != cudaSuccess) g_last_error = std::string("device scan: ") + cudaGetErrorString(e);
+  return r;
+}
+
+// Fills g->row/arc/arx/ioff/cls/bch/hown/hsum/hmin and the class counts.
+wbpr_status build_bcsr_device(wbpr_graph* g, const wbpr_csr* in) {
+  const int n = g->n;
+  const long long m = g->m;
+  cudaStream_t st = g->stream;
+  const int blocks = g->sms * 8;
+  wbpr_status rs;
+  if ((rs = dalloc(g, &g->row, (size_t)n + 1))) return rs;
+  if ((rs = dalloc(g, &g->arc, (size_t)(2 * m)))) return rs;
+  if ((rs = dalloc(g, &g->arx, (size_t)(2 * m)))) return rs;
+  if ((rs = dalloc(g, &g->ioff, (size_t)n + 1))) return rs;
+  std::vector<void*> tmp;
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(st);
+    for (void* p : tmp) cudaFree(p);
+    tmp.clear();
+  };
+  auto talloc = [&](size_t bytes) -> void* {
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
+    tmp.push_back(p);
+    return p;
+  };
+#define DB(x)                                                         \
+  do {                                                                \
+    cudaError_t e_ = (x);                                             \
+    if (e_ != cudaSuccess) {                                          \
+      g_last_error = std::string(#x) + ": " + cudaGetErrorString(e_); \
+      cleanup();                                                      \
+      return WBPR_ERR_CUDA;                                           \
+    }                                                                 \
+  } while (0)
+#define DBS(x)          \
+  do {                  \
+    rs = (x);           \
+    if (rs) {           \
+      cleanup();        \
+      return rs;        \
+    }                   \
+  } while (0)
+  const int ntiles = (int)((m + kSortTile - 1) / kSortTile);
+  int* d_dst = (int*)talloc(4 * (size_t)m);
+  int* d_cap = in->capacities ? (int*)talloc(4 * (size_t)m) : nullptr;
+  int* inoff = (int*)talloc(4 * ((size_t)n + 1));
+  auto* incap = (unsigned long long*)talloc(8 * ((size_t)n + 1));
+  auto* cnt = (unsigned long long*)talloc(8 * 8);
+  int* kb[2] = {(int*)talloc(4 * (size_t)m), (int*)talloc(4 * (size_t)m)};
+  int* vb[2] = {(int*)talloc(4 * (size_t)m), (int*)talloc(4 * (size_t)m)};
+  int* hist = (int*)talloc(4 * ((size_t)ntiles * 256 + 1));
+  if (!d_dst || (in->capacities && !d_cap) || !inoff || !incap || !cnt || !kb[0] || !kb[1] || !vb[0] || !vb[1] ||
+      !hist) {
+    cudaGetLastError();
+    g_last_error = "device build: out of device memory";
+    cleanup();
+    return WBPR_ERR_CUDA;
+  }
+  DB(cudaMemcpyAsync(g->ioff, in->offsets, 4 * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
+  if (m) {
+    DB(cudaMemcpyAsync(d_dst, in->destinations, 4 * (size_t)m, cudaMemcpyHostToDevice, st));
+    if (d_cap) DB(cudaMemcpyAsync(d_cap, in->capacities, 4 * (size_t)m, cudaMemcpyHostToDevice, st));
+  }
+  DB(cudaMemsetAsync(inoff, 0, 4 * ((size_t)n + 1), st));
+  DB(cudaMemsetAsync(incap, 0, 8 * ((size_t)n + 1), st));
+  DB(cudaMemsetAsync(cnt, 0, 8 * 8, st));
+  if (m) db_count<<<blocks, 256, 0, st>>>(d_dst, d_cap, m, inoff, incap);
+  db_max<<<blocks, 256, 0, st>>>(incap, n, cnt + 7);
+  DB(cudaGetLastError());
+  unsigned long long maxcap = 0;
+  DB(cudaMemcpyAsync(&maxcap, cnt + 7, 8, cudaMemcpyDeviceToHost, st));
+  DB(cudaStreamSynchronize(st));
+  if (maxcap > 0x7fffffffull) {
+    cleanup();
+    return WBPR_ERR_OVERFLOW;
+  }
+  DBS(device_scan(inoff, (long long)n + 1, st));
+  db_row<<<blocks, 256, 0, st>>>(g->ioff, inoff, n, g->row);
+  DB(cudaGetLastError());
+  if (m) {
+    const int bits = n > 1 ? 32 - __builtin_clz((unsigned)(n - 1)) : 1;
+    const int passes = (bits + 7) / 8;
+    const unsigned sblocks = (unsigned)((ntiles + 7) / 8);
+    for (int p = 0; p < passes; ++p) {
+      const int* kin = p ? kb[(p - 1) & 1] : d_dst;
+      const int* vin = p ? vb[(p - 1) & 1] : nullptr;
+      const bool last = p == passes - 1;
+      db_sort_hist<<<sblocks, 256, 0, st>>>(kin, m, 8 * p, ntiles, hist);
+      DB(cudaGetLastError());
+      DBS(device_scan(hist, (long long)ntiles * 256, st));
+      db_sort_scatter<<<sblocks, 256, 0, st>>>(kin, vin, m, 8 * p, ntiles, hist, kb[p & 1], vb[p & 1],
+                                               last ? kb[p & 1] : nullptr);
+      DB(cudaGetLastError());
+    }
+    const int* pos_of = kb[(passes - 1) & 1];
+    db_fill<<<blocks, 256, 0, st>>>(g->ioff, inoff, d_dst, d_cap, pos_of, n, m, g->arc, g->arx);
+    DB(cudaGetLastError());
+  }
+  // length classes in vertex order, by three stable compactions
+  int* fl[3] = {vb[0], vb[1], kb[0]};
+  if ((size_t)m < (size_t)n + 1) {
+    for (int k = 0; k < 3; ++k) fl[k] = (int*)talloc(4 * ((size_t)n + 1));
+    if (!fl[0] || !fl[1] || !fl[2]) {
+      cudaGetLastError();
+      g_last_error = "device build: out of device memory";
+      cleanup();
+      return WBPR_ERR_CUDA;
+    }
+  }
+  db_classify<<<blocks, 256, 0, st>>>(g->row, n, fl[0], fl[1], fl[2], cnt);
+  DB(cudaGetLastError());
+  for (int k = 0; k < 3; ++k) DBS(device_scan(fl[k], (long long)n + 1, st));
+  int tot[3];
+  unsigned long long hc[3];
+  for (int k = 0; k < 3; ++k) DB(cudaMemcpyAsync(tot + k, fl[k] + n, 4, cudaMemcpyDeviceToHost, st));
+  DB(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+  DB(cudaStreamSynchronize(st));
+  g->n_light = tot[0];
+  g->n_medium = tot[1];
+  g->n_heavy = tot[2];
+  g->n_td_heavy = (int)hc[0];
+  g->n_td_items = (int64_t)hc[1];
+  g->total_deg = 2 * m;
+  g->avg_deg = (double)g->total_deg / std::max<int64_t>(1, g->n_light + g->n_medium + g->n_heavy);
+  DBS(dalloc(g, &g->cls, (size_t)(tot[0] + tot[1] + tot[2])));
+  db_cls_scatter<<<blocks, 256, 0, st>>>(g->row, n, fl[0], fl[1], fl[2], g->cls);
+  DB(cudaGetLastError());
+  // static kChunk pieces of the heavy rows, in vertex order
+  const int nh = tot[2];
+  int* cbase = hist;  // reused when it is large enough
+  if ((size_t)nh + 1 > (size_t)ntiles * 256 + 1) {
+    cbase = (int*)talloc(4 * ((size_t)nh + 1));
+    if (!cbase) {
+      cudaGetLastError();
+      g_last_error = "device build: out of device memory";
+      cleanup();
+      return WBPR_ERR_CUDA;
+    }
+  }
+  const int* hcls = g->cls + tot[0] + tot[1];
+  db_heavy_chunks<<<blocks, 256, 0, st>>>(g->row, hcls, nh, cbase);
+  DB(cudaGetLastError());
+  DBS(device_scan(cbase, (long long)nh + 1, st));
+  int nbch = 0;
+  DB(cudaMemcpyAsync(&nbch, cbase + nh, 4, cudaMemcpyDeviceToHost, st));
+  DB(cudaStreamSynchronize(st));
+  g->n_bch = nbch;
+  DBS(dalloc(g, &g->bch, (size_t)nbch));
+  if (nh) db_bch_fill<<<std::min(nh, blocks), 128, 0, st>>>(g->row, hcls, nh, cbase, g->bch);
+  DB(cudaGetLastError());
+  const size_t max_chunks = (size_t)hc[2] + 1;
+  DBS(dalloc(g, &g->hown, max_chunks));
+  DBS(dalloc(g, &g->hsum, max_chunks));
+  DBS(dalloc(g, &g->hmin, max_chunks));
+  DB(cudaStreamSynchronize(st));
+#undef DB
+#undef DBS
+  cleanup();
+  return WBPR_OK;
+}
+
+// ---------------------------------------------------------------------------
 wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out) {
   if (!out) return WBPR_ERR_INVALID_ARG;
   *out = nullptr;
@@ -262,8 +660,10 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   if (in->num_nodes < 2) return WBPR_ERR_INVALID_ARG;
   if (layout != WBPR_LAYOUT_RCSR && layout != WBPR_LAYOUT_BCSR && layout != WBPR_LAYOUT_BCSR2)
     return WBPR_ERR_INVALID_ARG;
-  if (wbpr::max_in_capacity(in) > std::numeric_limits<int32_t>::max()) return WBPR_ERR_OVERFLOW;
   if (2 * in->num_edges > std::numeric_limits<int32_t>::max()) return WBPR_ERR_OVERFLOW;
+  // BCSR checks incoming-capacity overflow on the device while it builds
+  if (layout == WBPR_LAYOUT_RCSR && wbpr::max_in_capacity(in) > std::numeric_limits<int32_t>::max())
+    return WBPR_ERR_OVERFLOW;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();
@@ -304,18 +704,7 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   std::vector<int32_t> deg((size_t)n);
   std::vector<int32_t> row_host, rrow_host;
   if (g->layout == WBPR_LAYOUT_BCSR) {
-    wbpr::Bcsr16 b;
-    TRY(wbpr::build_bcsr16(in, &b));
-    TRY(dalloc(g, &g->row, (size_t)n + 1));
-    TRY(dalloc(g, &g->arc, (size_t)(2 * m)));
-    TRY(dalloc(g, &g->arx, (size_t)(2 * m)));
-    TRYC(cudaMemcpy(g->row, b.row.data(), 4 * ((size_t)n + 1), cudaMemcpyHostToDevice));
-    if (m) {
-      TRYC(cudaMemcpy(g->arc, b.arc.data(), 16 * (size_t)m, cudaMemcpyHostToDevice));
-      TRYC(cudaMemcpy(g->arx, b.arx.data(), 16 * (size_t)m, cudaMemcpyHostToDevice));
-    }
-    for (int u = 0; u < n; ++u) deg[u] = b.row[u + 1] - b.row[u];
-    row_host.swap(b.row);
+    TRY(build_bcsr_device(g, in));
   } else {
     wbpr::Rcsr r;
     TRY(wbpr::build_rcsr_dev(in, &r));
@@ -336,6 +725,7 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
     for (int u = 0; u < n; ++u) deg[u] = (r.frow[u + 1] - r.frow[u]) + (r.rrow[u + 1] - r.rrow[u]);
     rrow_host.swap(r.rrow);
   }
+  if (g->layout == WBPR_LAYOUT_RCSR) {
   TRY(dalloc(g, &g->ioff, (size_t)n + 1));
   TRYC(cudaMemcpy(g->ioff, in->offsets, 4 * ((size_t)n + 1), cudaMemcpyHostToDevice));
   // length classes for the BFS (isolated vertices are left out)
@@ -395,6 +785,7 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
     TRY(dalloc(g, &g->hsum, (size_t)max_chunks));
     TRY(dalloc(g, &g->hmin, (size_t)max_chunks));
   }
+  }  // RCSR host classification
   int** vec[] = {&g->h, &g->e, &g->rl_min, &g->rl_left, &g->lq[0], &g->lq[1], &g->hq[0], &g->hq[1],
                  &g->esnap, &g->dq, &g->dbase, &g->dE, &g->derem, &g->dmin0,
                  &g->qraw, &g->fr[0], &g->fr[1], &g->fr[2], &g->vlab};
@@ -622,6 +1013,26 @@ wbpr_status wbpr_graph_destroy(wbpr_graph* g) {
 }
 
 int64_t wbpr_graph_device_bytes(const wbpr_graph* g) { return g ? g->bytes : 0; }
+
+wbpr_status wbpr_graph_read_bcsr(const wbpr_graph* g, int32_t* offsets, int32_t* destinations,
+                                 int32_t* capacities, int32_t* backward_idx) {
+  if (!g || g->layout != WBPR_LAYOUT_BCSR) return WBPR_ERR_INVALID_ARG;
+  CK(cudaSetDevice(g->device));
+  CK(cudaStreamSynchronize(g->stream));
+  if (offsets) CK(cudaMemcpy(offsets, g->row, 4 * ((size_t)g->n + 1), cudaMemcpyDeviceToHost));
+  const size_t na = (size_t)(2 * g->m);
+  if (na && (destinations || capacities || backward_idx)) {
+    std::vector<int2> a(na), x(na);
+    CK(cudaMemcpy(a.data(), g->arc, 8 * na, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(x.data(), g->arx, 8 * na, cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < na; ++k) {
+      if (destinations) destinations[k] = a[k].x;
+      if (capacities) capacities[k] = x[k].y;
+      if (backward_idx) backward_idx[k] = x[k].x;
+    }
+  }
+  return WBPR_OK;
+}
 
 wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, const wbpr_tuning* tu,
                        wbpr_result* out) {
