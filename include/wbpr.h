@@ -85,7 +85,7 @@ typedef struct wbpr_host_csr {
 
 typedef struct wbpr_tuning {
   int32_t tile;          /* VC tile width: 8, 16 or 32 (0 = auto)                 */
-  int32_t block;         /* threads per block: 128..1024, multiple of 32 (0=auto) */
+  int32_t block;         /* threads per block: 64..256, multiple of 32 (0 = 256)  */
   int32_t heavy_degree;  /* rows longer than this are discharged by a whole warp  */
                          /* (128 arcs in flight) instead of a tile (0 = 32)       */
   int32_t blocks_per_sm; /* resident blocks per SM for the persistent grid (0=max) */
@@ -96,7 +96,9 @@ typedef struct wbpr_tuning {
   int32_t verify;        /* 1: run the device certificate check after the solve  */
   int32_t trace;         /* 1: record a per-level / per-phase event trace         */
   int32_t gr_rounds;     /* also relabel globally after this many rounds (0 = 48) */
-  int32_t reserved;
+  int32_t grid_blocks;   /* blocks of the persistent grid (0 = auto: one block,   */
+                         /* with block-local barriers, when n + arcs <= 16384;    */
+                         /* otherwise every SM x blocks_per_sm)                   */
 } wbpr_tuning;
 
 typedef struct wbpr_result {

@@ -37,12 +37,15 @@ def solve_all(g, combos=COMBOS, **kw):
     return out
 
 
-def test_golden_cases(golden):
+@pytest.mark.parametrize("grid", [0, 4096])
+def test_golden_cases(golden, grid):
+    # grid 0: small graphs run on one block (block barriers); 4096: every
+    # resident block of the device (grid barriers)
     for c in golden:
         g = graph_of(c)
         if g.n < 2 or g.s == g.t:
             continue
-        for key, v in solve_all(g).items():
+        for key, v in solve_all(g, grid_blocks=grid).items():
             assert v == c["expected"], (c["name"], key)
             if not c["reference_defect"]:
                 assert v == c["reference"], (c["name"], key)
@@ -53,8 +56,9 @@ def test_parallel_source_arcs_are_not_lost():
     assert set(solve_all(g).values()) == {10}
 
 
+@pytest.mark.parametrize("grid", [0, 4096])
 @pytest.mark.parametrize("seed", range(30))
-def test_random_graphs(seed):
+def test_random_graphs(seed, grid):
     rng = np.random.default_rng(1000 + seed)
     n = int(rng.integers(2, 300))
     m = int(rng.integers(0, 8 * n))
@@ -64,7 +68,7 @@ def test_random_graphs(seed):
     s, t = 0, n - 1
     g = W.Graph.from_arcs(n, tail, head, cap, s, t)
     expected = oracle.dinic(g.n, g.off, g.dst, g.cap, s, t)
-    for key, v in solve_all(g).items():
+    for key, v in solve_all(g, grid_blocks=grid).items():
         assert v == expected, key
 
 
@@ -178,7 +182,7 @@ def test_budget_exhaustion_is_reported():
 @pytest.mark.parametrize("tune", [
     dict(heavy_degree=64), dict(heavy_degree=256, gr_alpha=2.0), dict(heavy_degree=256, gr_alpha=8.0),
     dict(gr_alpha=0.05), dict(tile=8, heavy_degree=2048, gr_alpha=4.0), dict(blocks_per_sm=1, tile=16),
-    dict(block=128, heavy_degree=128, gr_alpha=3.0)])
+    dict(block=128, heavy_degree=128, gr_alpha=3.0), dict(grid_blocks=1), dict(grid_blocks=7, tile=8)])
 def test_tuning_space_exact_and_valid(tune):
     """Every tuning gives the exact value, a valid final labelling and the
     certificate, within a bounded time (a livelock would hit max_ms)."""

@@ -48,7 +48,7 @@ class Tuning(C.Structure):
     _fields_ = [("tile", C.c_int32), ("block", C.c_int32), ("heavy_degree", C.c_int32),
                 ("blocks_per_sm", C.c_int32), ("gr_alpha", C.c_double), ("max_rounds", C.c_int64),
                 ("max_ms", C.c_double), ("verify", C.c_int32), ("trace", C.c_int32),
-                ("gr_rounds", C.c_int32), ("reserved", C.c_int32)]
+                ("gr_rounds", C.c_int32), ("grid_blocks", C.c_int32)]
 
 
 class Result(C.Structure):

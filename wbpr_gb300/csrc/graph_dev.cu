@@ -260,7 +260,7 @@ __global__ void flow_kernel(const int* ioff, const int* row, const int2* arc, co
 // row[u] = off[u] + inoff[u], the forward slot of input arc i (tail u) is
 // i + inoff[u], and the twin of the arc at position p of the arcs stably
 // sorted by head v is off[v + 1] + p.  The stable sort is an LSD radix sort
-// by head over warp tiles; its last pass writes only that position p.
+// by head over warp tiles; its last pass also records each arc's position p.
 __global__ void db_count(const int* dst, const int* cap, long long m, int* indeg, unsigned long long* incap) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
     const int v = dst[i];
@@ -319,9 +319,20 @@ __global__ void db_scan_add(int* data, long long count, const int* sums) {
 }
 
 // radix sort by head: one warp tile = kSortRounds x 32 arcs, striped so that
-// (round, lane) order is input order and match_any ranks are stable
+// (round, lane) order is input order; lanes holding the same digit are found
+// with eight ballots (one per digit bit), which keeps the ranks stable
 constexpr int kSortRounds = 64;
 constexpr int kSortTile = kSortRounds * 32;
+__device__ __forceinline__ unsigned digit_peers(int d, bool ok) {
+  unsigned peers = __ballot_sync(0xffffffffu, ok);
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const bool bit = (d >> b) & 1;
+    const unsigned x = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? x : ~x;
+  }
+  return peers;
+}
 __global__ void __launch_bounds__(256) db_sort_hist(const int* key, long long m, int shift, int ntiles, int* hist) {
   __shared__ int cnt[8][256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -332,13 +343,15 @@ __global__ void __launch_bounds__(256) db_sort_hist(const int* key, long long m,
   const long long base = (long long)tile * kSortTile;
   for (int r = 0; r < kSortRounds; ++r) {
     const long long i = base + r * 32 + lane;
-    const int d = i < m ? (key[i] >> shift) & 255 : 256;
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
-    if (d < 256 && lane == __ffs(peers) - 1) cnt[w][d] += __popc(peers);
+    const bool ok = i < m;
+    const int d = ok ? (key[i] >> shift) & 255 : 0;
+    const unsigned peers = digit_peers(d, ok);
+    if (ok && lane == __ffs(peers) - 1) cnt[w][d] += __popc(peers);
     __syncwarp();
   }
   for (int b = lane; b < 256; b += 32) hist[(long long)b * ntiles + tile] = cnt[w][b];
 }
+// pos_of != nullptr on the last pass: also record each arc's sorted position
 __global__ void __launch_bounds__(256) db_sort_scatter(const int* kin, const int* vin, long long m, int shift,
                                                        int ntiles, const int* hist, int* kout, int* vout,
                                                        int* pos_of) {
@@ -354,17 +367,14 @@ __global__ void __launch_bounds__(256) db_sort_scatter(const int* kin, const int
     const long long i = base + r * 32 + lane;
     const bool ok = i < m;
     const int k = ok ? kin[i] : 0;
-    const int d = ok ? (k >> shift) & 255 : 256;
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int d = (k >> shift) & 255;
+    const unsigned peers = digit_peers(d, ok);
     if (ok) {
       const int pos = off[w][d] + __popc(peers & lt);
       const int val = vin ? vin[i] : (int)i;
-      if (pos_of) {
-        pos_of[val] = pos;
-      } else {
-        kout[pos] = k;
-        vout[pos] = val;
-      }
+      kout[pos] = k;
+      vout[pos] = val;
+      if (pos_of) pos_of[val] = pos;
     }
     __syncwarp();
     if (ok && lane == __ffs(peers) - 1) off[w][d] += __popc(peers);
@@ -372,10 +382,11 @@ __global__ void __launch_bounds__(256) db_sort_scatter(const int* kin, const int
   }
 }
 
-// one warp per 256 input arcs: tails by a binary search narrowed to the
-// warp's row range, then both slots of every pair
-__global__ void db_fill(const int* off, const int* inoff, const int* dst, const int* cap, const int* pos_of,
-                        int n, long long m, int2* arc, int2* arx) {
+// forward slots, one warp per 256 input arcs: tails by a binary search
+// narrowed to the warp's row range; records (tail, forward slot) per arc for
+// the twin pass
+__global__ void db_fill_fwd(const int* off, const int* inoff, const int* dst, const int* cap, const int* pos_of,
+                            int n, long long m, int2* arc, int2* arx, int2* uf) {
   const int lane = threadIdx.x & 31;
   const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
   for (long long base = (blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5)) * 256; base < m;
@@ -403,14 +414,25 @@ __global__ void db_fill(const int* off, const int* inoff, const int* dst, const 
         if (__ldg(off + mid) <= i) lo = mid;
         else hi = mid;
       }
-      const int u = lo, v = dst[i], c = cap ? cap[i] : 1;
-      const int f = (int)i + __ldg(inoff + u);
+      const int v = dst[i], c = cap ? cap[i] : 1;
+      const int f = (int)i + __ldg(inoff + lo);
       const int r = __ldg(off + v + 1) + pos_of[i];
       arc[f] = make_int2(v, c);
       arx[f] = make_int2(r, c);
-      arc[r] = make_int2(u, 0);
-      arx[r] = make_int2(f, 0);
+      uf[i] = make_int2(lo, f);
     }
+  }
+}
+// twin slots in sorted order: the twin of sorted position p is off[v + 1] + p,
+// so consecutive p write consecutive slots
+__global__ void db_fill_twin(const int* off, const int* skey, const int* sval, const int2* uf, long long m,
+                             int2* arc, int2* arx) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < m; p += (long long)gridDim.x * blockDim.x) {
+    const int v = skey[p];
+    const int2 t = uf[sval[p]];
+    const int r = __ldg(off + v + 1) + (int)p;
+    arc[r] = make_int2(t.x, 0);
+    arx[r] = make_int2(t.y, 0);
   }
 }
 
@@ -573,23 +595,31 @@ wbpr_status build_bcsr_device(wbpr_graph* g, const wbpr_csr* in) {
     const int bits = n > 1 ? 32 - __builtin_clz((unsigned)(n - 1)) : 1;
     const int passes = (bits + 7) / 8;
     const unsigned sblocks = (unsigned)((ntiles + 7) / 8);
+    int* pos_of = (int*)talloc(4 * (size_t)m);
+    int2* uf = (int2*)talloc(8 * (size_t)m);
+    if (!pos_of || !uf) {
+      cudaGetLastError();
+      g_last_error = "device build: out of device memory";
+      cleanup();
+      return WBPR_ERR_CUDA;
+    }
     for (int p = 0; p < passes; ++p) {
       const int* kin = p ? kb[(p - 1) & 1] : d_dst;
       const int* vin = p ? vb[(p - 1) & 1] : nullptr;
-      const bool last = p == passes - 1;
       db_sort_hist<<<sblocks, 256, 0, st>>>(kin, m, 8 * p, ntiles, hist);
       DB(cudaGetLastError());
       DBS(device_scan(hist, (long long)ntiles * 256, st));
       db_sort_scatter<<<sblocks, 256, 0, st>>>(kin, vin, m, 8 * p, ntiles, hist, kb[p & 1], vb[p & 1],
-                                               last ? kb[p & 1] : nullptr);
+                                               p == passes - 1 ? pos_of : nullptr);
       DB(cudaGetLastError());
     }
-    const int* pos_of = kb[(passes - 1) & 1];
-    db_fill<<<blocks, 256, 0, st>>>(g->ioff, inoff, d_dst, d_cap, pos_of, n, m, g->arc, g->arx);
+    db_fill_fwd<<<blocks, 256, 0, st>>>(g->ioff, inoff, d_dst, d_cap, pos_of, n, m, g->arc, g->arx, uf);
+    db_fill_twin<<<blocks, 256, 0, st>>>(g->ioff, kb[(passes - 1) & 1], vb[(passes - 1) & 1], uf, m, g->arc,
+                                         g->arx);
     DB(cudaGetLastError());
   }
   // length classes in vertex order, by three stable compactions
-  int* fl[3] = {vb[0], vb[1], kb[0]};
+  int* fl[3] = {vb[0], vb[1], kb[0]};  // free once the fill kernels have run (stream order)
   if ((size_t)m < (size_t)n + 1) {
     for (int k = 0; k < 3; ++k) fl[k] = (int*)talloc(4 * ((size_t)n + 1));
     if (!fl[0] || !fl[1] || !fl[2]) {
@@ -854,12 +884,17 @@ void topo_of(wbpr_graph* g, TopoR& r) {
   r.rarc = g->rarc;
 }
 
+// graphs with n + residual arcs up to this run on one block: its phases are
+// then separated by block barriers instead of grid barriers
+constexpr int64_t kOneBlockUnits = 16384;
+
 struct RunCfg {
   int mode;
   int s, t;
   int tile;
   int threads;
   int blocks_per_sm;
+  int grid_blocks;
   int heavy_deg;
   unsigned long long gr_threshold;
   int gr_rounds;
@@ -911,10 +946,13 @@ wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch
     return WBPR_ERR_CUDA;
   }
   const int bps = rc.blocks_per_sm > 0 ? std::min(occ, rc.blocks_per_sm) : occ;
+  int blocks = g->sms * bps;
+  if (rc.grid_blocks > 0) blocks = std::min(blocks, rc.grid_blocks);
+  else if ((int64_t)g->n + g->total_deg <= kOneBlockUnits) blocks = 1;
   CK(cudaMemsetAsync(g->ctl, 0, sizeof(Ctl), g->stream));
   CK(cudaMemsetAsync(g->st, 0, sizeof(Stats), g->stream));
   CK(cudaEventRecord(g->ev2, g->stream));
-  CK(launch_pr(p, rc.tile, g->sms * bps, rc.threads, g->stream));
+  CK(launch_pr(p, rc.tile, blocks, rc.threads, g->stream));
   CK(cudaEventRecord(g->ev3, g->stream));
   if (rc.mode != kModeBfsOnly) CK(launch_stranded(p, g->sms * 4, 256, g->stream));
   Ctl hc;
@@ -955,6 +993,8 @@ wbpr_status make_cfg(wbpr_graph* g, int s, int t, wbpr_algo algo, const wbpr_tun
   if (threads < 64 || threads > 256 || threads % 32) return WBPR_ERR_INVALID_ARG;
   rc->threads = threads;
   rc->blocks_per_sm = tu->blocks_per_sm > 0 ? tu->blocks_per_sm : 0;
+  if (tu->grid_blocks < 0) return WBPR_ERR_INVALID_ARG;
+  rc->grid_blocks = tu->grid_blocks;
   rc->heavy_deg = tu->heavy_degree > 0 ? tu->heavy_degree : 32;
   const double alpha = tu->gr_alpha > 0 ? tu->gr_alpha : 0.75;
   rc->gr_threshold = (unsigned long long)(alpha * ((double)g->n + (double)g->total_deg)) + 1;

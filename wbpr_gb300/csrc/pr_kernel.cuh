@@ -53,28 +53,31 @@ enum Mode : int {
   kModeBfsOnly = 2  // only the BFS into `lab` (verification / adjoint)
 };
 
-// Device control block (scratch owned by the graph handle).
+// Device control block (scratch owned by the graph handle).  Words that every
+// block hits in the same phase sit on their own 128-byte lines, so the barrier
+// word, the work-claim counters and the list counters do not share an L2 line.
+constexpr int kWorkSlots = 32;  // the per-round work sum is spread over 32 lines
 struct Ctl {
-  unsigned bar_count;
-  unsigned bar_gen;
-  int err;
+  alignas(128) unsigned bar;  // grid barrier word (zero at launch)
+  alignas(128) int err;
   int stop;
-  int lcount[2];
+  alignas(128) int lcount[2];
   int hcount[2];
-  int qraw_count[2];
-  int light_next;
-  int heavy_next;
-  int deep_next_a;
+  alignas(128) int qraw_count[2];
+  alignas(128) int light_next;
+  alignas(128) int heavy_next;
+  alignas(128) int deep_next_a;
   int deep_next_b;
-  int fcount[3];
+  alignas(128) int fcount[3];
   int fhcount[3];
   long long fdeg[3];
-  unsigned long long work[2];  // work done in rounds of even / odd parity
-  unsigned long long dpack;    // deep list of the round: (entries << 32) | chunk items
-  int bfs_heavy_next[3];
+  alignas(128) unsigned long long dpack;  // deep list of the round: (entries << 32) | chunk items
+  alignas(128) int bfs_heavy_next[3];
   int bu_found[3];  // vertices labelled by a bottom-up level, by level % 3
   int mcount;       // materialised frontier: short rows
   int mhcount;      //   long-row chunk items
+  // work done in rounds of even / odd parity; block b adds to slot b % 32
+  alignas(128) unsigned long long work[2][kWorkSlots * 16];
 };
 
 struct Stats {
@@ -285,31 +288,36 @@ struct BlockAcc {
   unsigned long long bfs_arcs;
   unsigned long long bfs_vertices;
   long long fdeg;
+  unsigned long long wmark;  // scanned + visits + relabels at the last work flush
   int sink;
   int pad;
 };
 
 // ---------------------------------------------------------------------------
-// Bounded grid barrier.  Thread 0 of each block arrives on a counter; the last
-// arrival resets it and bumps the generation.  Waiting gives up after
-// timeout_ns of globaltimer time and records WBPR_ERR_TIMEOUT.
+// Bounded grid barrier on one word.  Block 0 adds 2^31 - (blocks - 1), every other
+// block adds 1: the arrivals of one episode sum to exactly 2^31, so bit 31
+// flips when -- and only when -- the last block arrives, and the low 31 bits
+// stay zero between episodes (the word is zero at launch).  A block waits for
+// bit 31 to differ from the value its own arrival returned; a block that
+// races ahead into the next episode cannot flip it back before the slowest
+// block has left this one.  The wait gives up after timeout_ns.
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
 __device__ __forceinline__ bool grid_sync(Ctl* c, unsigned long long timeout_ns) {
   __syncthreads();
+  if (gridDim.x == 1) return ldv(&c->err) == 0;  // a one-block grid: the block barrier is enough
   if (threadIdx.x == 0) {
-    volatile unsigned* genp = &c->bar_gen;
-    unsigned g = *genp;
+    const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
     __threadfence();
-    unsigned arrived = atomicAdd(&c->bar_count, 1u) + 1u;
-    if (arrived == gridDim.x) {
-      atomicExch(&c->bar_count, 0u);
-      __threadfence();
-      atomicAdd(&c->bar_gen, 1u);
+    const unsigned old = atomicAdd(&c->bar, add);
+    if (((old + add) ^ old) & 0x80000000u) {
+      // last arrival: nothing to wait for
     } else {
-      unsigned long long t0 = gtime();
-      unsigned ns = 32;
-      while (*genp == g) {
-        __nanosleep(ns);
-        if (ns < 256) ns <<= 1;
+      const unsigned long long t0 = gtime();
+      while (!((ld_acquire(&c->bar) ^ old) & 0x80000000u)) {
         if (gtime() - t0 > timeout_ns) {
           atomicCAS(&c->err, 0, (int)WBPR_ERR_TIMEOUT);
           break;
@@ -331,19 +339,36 @@ __device__ __forceinline__ void append(int* q, int* cnt, int v) {
   q[base + g.thread_rank()] = v;
 }
 
-__device__ __forceinline__ void flush_acc(BlockAcc& a, Stats* st,
-                                          unsigned long long* work = nullptr) {
+// Per-round work (arcs scanned + vertex visits + relabels) of this block since
+// its last flush, added to one of the 32 slots of the round's parity.
+__device__ __forceinline__ void flush_work(BlockAcc& a, Ctl* c, int parity) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned long long w = a.scanned + a.visits + a.relabels;
-    if (work && w) atomicAdd(work, w);
+    const unsigned long long tot = a.scanned + a.visits + a.relabels;
+    const unsigned long long w = tot - a.wmark;
+    a.wmark = tot;
+    if (w) atomicAdd(&c->work[parity][(blockIdx.x % kWorkSlots) * 16], w);
+  }
+  __syncthreads();
+}
+// Sum of the 32 work slots of one parity (every warp computes it).
+__device__ __forceinline__ unsigned long long work_total(Ctl* c, int parity) {
+  unsigned long long w = *(volatile unsigned long long*)&c->work[parity][(threadIdx.x & 31) * 16];
+  for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+  return w;
+}
+
+// Counters into Stats, once per launch.
+__device__ __forceinline__ void flush_acc(BlockAcc& a, Stats* st) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
     if (a.scanned) atomicAdd(&st->arcs_scanned, a.scanned);
     if (a.pushes) atomicAdd(&st->pushes, a.pushes);
     if (a.relabels) atomicAdd(&st->relabels, a.relabels);
     if (a.visits) atomicAdd(&st->vertex_visits, a.visits);
     if (a.bfs_arcs) atomicAdd(&st->bfs_arcs, a.bfs_arcs);
     if (a.bfs_vertices) atomicAdd(&st->bfs_vertices, a.bfs_vertices);
-    a.scanned = a.pushes = a.relabels = a.visits = a.bfs_arcs = a.bfs_vertices = 0;
+    a.scanned = a.pushes = a.relabels = a.visits = a.bfs_arcs = a.bfs_vertices = a.wmark = 0;
   }
   __syncthreads();
 }
@@ -771,27 +796,29 @@ __device__ void push_first(const Params<Topo>& p, int cur, int raw, BlockAcc& ac
   const int nH = ldv(&c->hcount[cur]);
   int* rawcnt = &c->qraw_count[raw];
   const int lane = threadIdx.x & 31;
-  for (;;) {
-    int idx = 0;
-    if (lane == 0) idx = atomicAdd(&c->heavy_next, 1);
-    idx = __shfl_sync(0xffffffffu, idx, 0);
-    if (idx >= nH) break;
+  // first item of every warp by its index, the rest claimed (an idle round
+  // touches no counter)
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int idx = gw; idx < nH;) {
     tile_discharge<Topo, 32, 4>(p, __ldcg(p.hq[cur] + idx), kChunk, rawcnt, acc);
+    int nx = 0;
+    if (lane == 0) nx = nwarps + atomicAdd(&c->heavy_next, 1);
+    idx = __shfl_sync(0xffffffffu, nx, 0);
   }
   if (p.trace && threadIdx.x == 0) p.bt2[blockIdx.x] = gtime();
   constexpr int kTpw = 32 / W;
   constexpr int kGrab = 2 * kTpw;
-  for (;;) {
-    int base = 0;
-    if (lane == 0) base = atomicAdd(&c->light_next, kGrab);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= nL) break;
+  for (int base = gw * kGrab; base < nL;) {
 #pragma unroll 1
     for (int r = 0; r < 2; ++r) {
       const int idx = base + r * kTpw + lane / W;
       if (idx < nL) tile_discharge<Topo, W, 4>(p, __ldcg(p.lq[cur] + idx), kChunk, rawcnt, acc);
     }
     __syncwarp();
+    int nx = 0;
+    if (lane == 0) nx = nwarps * kGrab + atomicAdd(&c->light_next, kGrab);
+    base = __shfl_sync(0xffffffffu, nx, 0);
   }
 }
 
@@ -801,14 +828,13 @@ __device__ void push_deep(const Params<Topo>& p, int pass, int nD, int raw, Bloc
   int* rawcnt = &c->qraw_count[raw];
   int* ctr = pass == 0 ? &c->deep_next_a : &c->deep_next_b;
   __shared__ int s_item;
-  for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(ctr, 1);
-    __syncthreads();
-    const int it = s_item;
-    __syncthreads();
-    if (it >= nD) break;
+  for (int it = blockIdx.x; it < nD;) {
     if (pass == 0) deep_pass_a<Topo>(p, it, acc);
     else deep_pass_b<Topo>(p, it, rawcnt, acc);
+    if (threadIdx.x == 0) s_item = (int)gridDim.x + atomicAdd(ctr, 1);
+    __syncthreads();
+    it = s_item;
+    __syncthreads();
   }
 }
 
@@ -882,12 +908,12 @@ __device__ void relabel_phase(const Params<Topo>& p, int cur, int nxt, int raw, 
     c->hcount[cur] = 0;
     c->dpack = 0;
     c->qraw_count[raw ^ 1] = 0;
-    c->work[raw ^ 1] = 0;
     c->light_next = 0;
     c->heavy_next = 0;
     c->deep_next_a = 0;
     c->deep_next_b = 0;
   }
+  if (blockIdx.x == 0 && threadIdx.x < kWorkSlots) c->work[raw ^ 1][threadIdx.x * 16] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1109,18 +1135,17 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
   __shared__ int s_skip;
   const int cur3 = level % 3;
   unsigned long long ha = 0;
-  for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(&c->bfs_heavy_next[cur3], 1);
-    __syncthreads();
-    const int it = s_item;
-    if (it >= p.n_bch) {
-      __syncthreads();
-      break;
-    }
+  for (int it = blockIdx.x; it < p.n_bch;) {
     const int4 ch = __ldg(p.bch + it);  // {vertex, segment, begin, end}
-    if (threadIdx.x == 0) s_skip = (ch.x == p.bfs_excl || __ldcg(p.lab + ch.x) != p.n);
+    if (threadIdx.x == 0) {
+      s_skip = (ch.x == p.bfs_excl || __ldcg(p.lab + ch.x) != p.n);
+      s_item = (int)gridDim.x + atomicAdd(&c->bfs_heavy_next[cur3], 1);
+    }
     __syncthreads();
-    if (s_skip) continue;
+    const bool skip = s_skip;
+    it = s_item;
+    __syncthreads();
+    if (skip) continue;
     bool hit = false;
     for (int base = ch.z; base < ch.w; base += blockDim.x * 4) {
       bool h = false;
@@ -1285,7 +1310,7 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
   __shared__ BlockAcc acc;
   Ctl* c = p.ctl;
   if (threadIdx.x == 0) {
-    acc.scanned = acc.pushes = acc.relabels = acc.visits = acc.bfs_arcs = acc.bfs_vertices = 0;
+    acc.scanned = acc.pushes = acc.relabels = acc.visits = acc.bfs_arcs = acc.bfs_vertices = acc.wmark = 0;
     acc.fdeg = 0;
     acc.sink = 0;
   }
@@ -1388,7 +1413,7 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
     }
     TRACE_BLOCK(p, tb);
     flush_sink(p.e + p.t, acc);
-    flush_acc(acc, p.st, &c->work[raw]);
+    flush_work(acc, c, raw);
     if (!grid_sync(c, p.bar_timeout_ns)) break;
     if (gt == 0) {
       push_ns += gtime() - t0;
@@ -1397,7 +1422,7 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
     tb = gtime();
     relabel_phase<Topo>(p, cur, cur ^ 1, raw, acc);
     TRACE_BLOCK(p, tb);
-    flush_acc(acc, p.st, &c->work[raw]);
+    flush_work(acc, c, raw);
     if (gt == 0) {
       round_ns += gtime() - t0;
       if ((p.max_rounds > 0 && rounds + 1 >= p.max_rounds) || gtime() - t_start > p.budget_ns)
@@ -1405,7 +1430,7 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
     }
     if (!grid_sync(c, p.bar_timeout_ns)) break;
     if (gt == 0) TRACE(p, kTrRelabel, rounds, ldv(&c->qraw_count[raw]), 0);
-    work += *(volatile unsigned long long*)&c->work[raw];
+    work += work_total(c, raw);
     ++rounds;
     ++since_gr;
     cur ^= 1;
