@@ -145,110 +145,196 @@ struct VerifyAcc {
   long long cut;
 };
 
-// warp per vertex: capacity pair invariant, conservation, cut of the sink side
-__global__ void verify_bcsr(const int* row, const int2* arc, const int2* arx, const int* e,
-                            const int* lab, const int* h, int n, int s, int t, VerifyAcc* out) {
+// Arc-parallel walks over a CSR: every warp takes tiles of kTile consecutive
+// entries (kTile / 32 per lane, striped so a load instruction is coalesced).
+// Lanes 0 and 1 find the rows of the tile's first and last entries by binary
+// search over the offsets; each entry then searches between those two rows.
+// Rows of any length cost the same per entry (a 262,144-arc row is spread
+// over 1,024 warps instead of walked by one).
+constexpr int kTile = 256;
+struct TileRows {
+  int lo, hi;  // off[lo] <= first entry, last entry < off[hi]
+};
+__device__ __forceinline__ int row_search(const int* off, long long i, int lo, int hi) {
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= i) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+__device__ __forceinline__ TileRows tile_rows(const int* off, int n, long long base, long long count) {
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  for (int v = gw; v < n; v += nw) {
-    long long net = 0, cut = 0;
-    int bad = 0, lv = 0;
-    const bool vin = lab[v] < n;
-    const int hv = h[v];
-    for (int a = row[v] + lane; a < row[v + 1]; a += 32) {
-      const int2 r = arc[a], x = arx[a];
-      const int2 rr = arc[x.x], xr = arx[x.x];
-      if (r.y < 0 || (long long)r.y + rr.y != (long long)x.y + xr.y) ++bad;
-      net += (long long)r.y - x.y;
-      if (!vin && x.y > 0 && lab[r.x] < n) cut += x.y;
-      if (r.y > 0 && v != s && hv < n && hv > h[r.x] + 1) ++lv;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      net += __shfl_down_sync(0xffffffffu, net, o);
-      cut += __shfl_down_sync(0xffffffffu, cut, o);
-      bad += __shfl_down_sync(0xffffffffu, bad, o);
-      lv += __shfl_down_sync(0xffffffffu, lv, o);
-    }
-    if (lane == 0) {
-      if (bad) atomicAdd(&out->cap_viol, bad);
-      if (lv) atomicAdd(&out->label_viol, lv);
-      if (v != s && net != (long long)e[v]) atomicAdd(&out->cons_viol, 1);
-      if (cut) atomicAdd((unsigned long long*)&out->cut, (unsigned long long)cut);
-      if (v != s && v != t && e[v] > 0 && vin) atomicAdd(&out->excess_reach, 1);
-    }
+  int r = 0;
+  if (lane < 2) r = row_search(off, lane ? min(base + kTile - 1, count - 1) : base, 0, n);
+  TileRows t;
+  t.lo = __shfl_sync(0xffffffffu, r, 0);
+  t.hi = __shfl_sync(0xffffffffu, r, 1) + 1;
+  return t;
+}
+#define FOR_TILES(count)                                                                        \
+  for (long long base = (blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5)) * kTile; \
+       base < (count); base += (long long)gridDim.x * (blockDim.x >> 5) * kTile)
+
+// Sum of v over the run of equal keys ending at this lane (keys are
+// non-decreasing across the warp); true on the run's last lane.
+__device__ __forceinline__ bool run_sum(int key, bool valid, long long& v) {
+  const int lane = threadIdx.x & 31;
+  for (int d = 1; d < 32; d <<= 1) {
+    const long long y = __shfl_up_sync(0xffffffffu, v, d);
+    const int k = __shfl_up_sync(0xffffffffu, key, d);
+    if (lane >= d && k == key) v += y;
+  }
+  const int kn = __shfl_down_sync(0xffffffffu, key, 1);
+  const bool vn = __shfl_down_sync(0xffffffffu, valid, 1);
+  return valid && (lane == 31 || !vn || kn != key);
+}
+
+__device__ __forceinline__ void verify_flush(VerifyAcc* out, int bad, int lv, long long cut) {
+  for (int o = 16; o > 0; o >>= 1) {
+    bad += __shfl_down_sync(0xffffffffu, bad, o);
+    lv += __shfl_down_sync(0xffffffffu, lv, o);
+    cut += __shfl_down_sync(0xffffffffu, cut, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (bad) atomicAdd(&out->cap_viol, bad);
+    if (lv) atomicAdd(&out->label_viol, lv);
+    if (cut) atomicAdd((unsigned long long*)&out->cut, (unsigned long long)cut);
   }
 }
 
-__global__ void verify_rcsr(const int* frow, const int2* farc, const int* fcb, const int* fcap,
-                            const int* rrow, const int2* rarc, const int* e, const int* lab, const int* h,
-                            int n, int s, int t, VerifyAcc* out) {
+// Certificate, arc part (BCSR): capacity pair invariant, label validity, cut
+// of the sink side, and each vertex's net residual change into net[].
+__global__ void verify_arcs_bcsr(const int* row, const int2* arc, const int2* arx, const int* lab,
+                                 const int* h, int n, int s, long long na, long long* net, VerifyAcc* out) {
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  for (int v = gw; v < n; v += nw) {
-    long long net = 0, cut = 0;
-    int bad = 0, lv = 0;
-    const bool vin = lab[v] < n;
-    const int hv = h[v];
-    for (int i = frow[v] + lane; i < frow[v + 1]; i += 32) {
-      const int2 r = farc[i];
-      const int b = fcb[i], c = fcap[i];
-      if (r.y < 0 || b < 0 || (long long)r.y + b != c) ++bad;
-      net -= b;
-      if (!vin && c > 0 && lab[r.x] < n) cut += c;
-      if (r.y > 0 && v != s && hv < n && hv > h[r.x] + 1) ++lv;
+  int bad = 0, lv = 0;
+  long long cut = 0;
+  FOR_TILES(na) {
+    const TileRows tr = tile_rows(row, n, base, na);
+#pragma unroll 1
+    for (int k = 0; k < kTile / 32; ++k) {
+      const long long a = base + k * 32 + lane;
+      const bool ok = a < na;
+      int u = -1;
+      long long d = 0;
+      if (ok) {
+        u = row_search(row, a, tr.lo, tr.hi);
+        const int2 r = arc[a], x = arx[a];
+        const int2 rr = arc[x.x], xr = arx[x.x];
+        if (r.y < 0 || (long long)r.y + rr.y != (long long)x.y + xr.y) ++bad;
+        d = (long long)r.y - x.y;
+        if (x.y > 0 && lab[u] >= n && lab[r.x] < n) cut += x.y;
+        const int hu = h[u];
+        if (r.y > 0 && u != s && hu < n && hu > h[r.x] + 1) ++lv;
+      }
+      if (run_sum(u, ok, d) && d) atomicAdd((unsigned long long*)(net + u), (unsigned long long)d);
     }
-    for (int j = rrow[v] + lane; j < rrow[v + 1]; j += 32) {
-      const int2 q = rarc[j];
-      const int f = fcb[q.y];
-      net += f;
-      if (f > 0 && v != s && hv < n && hv > h[q.x] + 1) ++lv;
+  }
+  verify_flush(out, bad, lv, cut);
+}
+// RCSR: forward arcs (tails by frow) and reverse entries (tails by rrow)
+__global__ void verify_arcs_rcsr(const int* frow, const int2* farc, const int* fcb, const int* fcap,
+                                 const int* rrow, const int2* rarc, const int* lab, const int* h, int n, int s,
+                                 long long m, long long* net, VerifyAcc* out) {
+  const int lane = threadIdx.x & 31;
+  int bad = 0, lv = 0;
+  long long cut = 0;
+  // forward arcs in tiles [0, M), reverse entries in tiles [M, 2M), M = m
+  // rounded up to whole tiles, so no tile mixes the two
+  const long long M = (m + kTile - 1) / kTile * kTile;
+  FOR_TILES(2 * M) {
+    const bool rev = base >= M;
+    const long long b0 = rev ? base - M : base;
+    const int* off = rev ? rrow : frow;
+    const TileRows tr = tile_rows(off, n, b0, m);
+#pragma unroll 1
+    for (int k = 0; k < kTile / 32; ++k) {
+      const long long i = b0 + k * 32 + lane;
+      const bool ok = i < m;
+      int u = -1;
+      long long d = 0;
+      if (ok) {
+        u = row_search(off, i, tr.lo, tr.hi);
+        const int hu = h[u];
+        if (!rev) {
+          const int2 r = farc[i];
+          const int fb = fcb[i], c = fcap[i];
+          if (r.y < 0 || fb < 0 || (long long)r.y + fb != c) ++bad;
+          d = -(long long)fb;
+          if (c > 0 && lab[u] >= n && lab[r.x] < n) cut += c;
+          if (r.y > 0 && u != s && hu < n && hu > h[r.x] + 1) ++lv;
+        } else {
+          const int2 q = rarc[i];
+          const int f = fcb[q.y];
+          d = f;
+          if (f > 0 && u != s && hu < n && hu > h[q.x] + 1) ++lv;
+        }
+      }
+      if (run_sum(u, ok, d) && d) atomicAdd((unsigned long long*)(net + u), (unsigned long long)d);
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      net += __shfl_down_sync(0xffffffffu, net, o);
-      cut += __shfl_down_sync(0xffffffffu, cut, o);
-      bad += __shfl_down_sync(0xffffffffu, bad, o);
-      lv += __shfl_down_sync(0xffffffffu, lv, o);
-    }
-    if (lane == 0) {
-      if (bad) atomicAdd(&out->cap_viol, bad);
-      if (lv) atomicAdd(&out->label_viol, lv);
-      if (v != s && net != (long long)e[v]) atomicAdd(&out->cons_viol, 1);
-      if (cut) atomicAdd((unsigned long long*)&out->cut, (unsigned long long)cut);
-      if (v != s && v != t && e[v] > 0 && vin) atomicAdd(&out->excess_reach, 1);
-    }
+  }
+  verify_flush(out, bad, lv, cut);
+}
+// Certificate, vertex part: conservation and excess that still reaches t.
+__global__ void verify_vertices(const int* e, const int* lab, const long long* net, int n, int s, int t,
+                                VerifyAcc* out) {
+  int cv = 0, er = 0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    if (v == s) continue;
+    const int ev = e[v];
+    if (net[v] != (long long)ev) ++cv;
+    if (v != t && ev > 0 && lab[v] < n) ++er;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    cv += __shfl_down_sync(0xffffffffu, cv, o);
+    er += __shfl_down_sync(0xffffffffu, er, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (cv) atomicAdd(&out->cons_viol, cv);
+    if (er) atomicAdd(&out->excess_reach, er);
   }
 }
 
 // per input arc (tail u, head v): side 0 -> [u cannot reach t, v can];
-// side 1 -> [u reached from s, v not]
+// side 1 -> [u reachable from s, v not]  (labels < n mark the BFS's set)
 __global__ void indicator_kernel(const int* ioff, const int* row, const int2* arc, const int2* farc,
-                                 const int* lab, int n, int side, int8_t* ind) {
+                                 const int* lab, int n, long long m, int side, int8_t* ind) {
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  for (int u = gw; u < n; u += nw) {
-    const int b = ioff[u], e = ioff[u + 1];
-    const bool uin = lab[u] < n;
-    for (int i = b + lane; i < e; i += 32) {
-      const int v = row ? arc[row[u] + (i - b)].x : farc[i].x;
-      const bool vin = lab[v] < n;
+  FOR_TILES(m) {
+    const TileRows tr = tile_rows(ioff, n, base, m);
+#pragma unroll 2
+    for (int k = 0; k < kTile / 32; ++k) {
+      const long long i = base + k * 32 + lane;
+      if (i >= m) break;
+      const int u = row_search(ioff, i, tr.lo, tr.hi);
+      const int v = row ? arc[row[u] + (int)(i - ioff[u])].x : farc[i].x;
+      const bool uin = lab[u] < n, vin = lab[v] < n;
       ind[i] = side == 0 ? (int8_t)(!uin && vin) : (int8_t)(uin && !vin);
     }
   }
 }
 
+// per input arc: flow = capacity - residual
 __global__ void flow_kernel(const int* ioff, const int* row, const int2* arc, const int2* arx,
-                            const int* fcb, int n, int* flow) {
+                            const int* fcb, int n, long long m, int* flow) {
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  for (int u = gw; u < n; u += nw) {
-    const int b = ioff[u], e = ioff[u + 1];
-    for (int i = b + lane; i < e; i += 32) {
-      if (row) {
-        const int a = row[u] + (i - b);
-        flow[i] = arx[a].y - arc[a].y;
-      } else {
-        flow[i] = fcb[i];
+  FOR_TILES(m) {
+    if (!row) {
+      for (int k = 0; k < kTile / 32; ++k) {
+        const long long i = base + k * 32 + lane;
+        if (i < m) flow[i] = fcb[i];
       }
+      continue;
+    }
+    const TileRows tr = tile_rows(ioff, n, base, m);
+#pragma unroll 2
+    for (int k = 0; k < kTile / 32; ++k) {
+      const long long i = base + k * 32 + lane;
+      if (i >= m) break;
+      const int u = row_search(ioff, i, tr.lo, tr.hi);
+      const int a = row[u] + (int)(i - ioff[u]);
+      flow[i] = arx[a].y - arc[a].y;
     }
   }
 }
@@ -382,44 +468,24 @@ __global__ void __launch_bounds__(256) db_sort_scatter(const int* kin, const int
   }
 }
 
-// forward slots, one warp per 256 input arcs: tails by a binary search
-// narrowed to the warp's row range; records (tail, forward slot) per arc for
-// the twin pass
+// forward slots, arc-parallel (tails as in the tile walk above); records
+// (tail, forward slot) per arc for the twin pass
 __global__ void db_fill_fwd(const int* off, const int* inoff, const int* dst, const int* cap, const int* pos_of,
                             int n, long long m, int2* arc, int2* arx, int2* uf) {
   const int lane = threadIdx.x & 31;
-  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long base = (blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5)) * 256; base < m;
-       base += nw * 256) {
-    int u_edge = 0;
-    if (lane < 2) {
-      const long long x = lane ? min(base + 255, m - 1) : base;
-      int lo = 0, hi = n;
-      while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (__ldg(off + mid) <= x) lo = mid;
-        else hi = mid;
-      }
-      u_edge = lo;
-    }
-    const int u_lo = __shfl_sync(0xffffffffu, u_edge, 0);
-    const int u_hi = __shfl_sync(0xffffffffu, u_edge, 1) + 1;
+  FOR_TILES(m) {
+    const TileRows tr = tile_rows(off, n, base, m);
 #pragma unroll 4
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < kTile / 32; ++k) {
       const long long i = base + k * 32 + lane;
       if (i >= m) break;
-      int lo = u_lo, hi = u_hi;  // off[lo] <= i < off[hi]
-      while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (__ldg(off + mid) <= i) lo = mid;
-        else hi = mid;
-      }
+      const int u = row_search(off, i, tr.lo, tr.hi);
       const int v = dst[i], c = cap ? cap[i] : 1;
-      const int f = (int)i + __ldg(inoff + lo);
+      const int f = (int)i + __ldg(inoff + u);
       const int r = __ldg(off + v + 1) + pos_of[i];
       arc[f] = make_int2(v, c);
       arx[f] = make_int2(r, c);
-      uf[i] = make_int2(lo, f);
+      uf[i] = make_int2(u, f);
     }
   }
 }
@@ -1160,7 +1226,7 @@ wbpr_status wbpr_read_state(wbpr_graph* g, int32_t* height, int32_t* excess, int
       wbpr_status st = dalloc(g, &g->flow_tmp, (size_t)g->m);
       if (st) return st;
     }
-    flow_kernel<<<g->sms * 4, 256, 0, g->stream>>>(g->ioff, g->row, g->arc, g->arx, g->fcb, g->n,
+    flow_kernel<<<g->sms * 8, 256, 0, g->stream>>>(g->ioff, g->row, g->arc, g->arx, g->fcb, g->n, g->m,
                                                    g->flow_tmp);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(arc_flow, g->flow_tmp, 4 * (size_t)g->m, cudaMemcpyDeviceToHost, g->stream));
@@ -1192,12 +1258,17 @@ wbpr_status wbpr_verify(wbpr_graph* g, wbpr_verify_report* rep) {
   VerifyAcc* dacc = nullptr;
   CK(cudaMalloc(&dacc, sizeof(VerifyAcc)));
   cudaMemsetAsync(dacc, 0, sizeof(VerifyAcc), g->stream);
+  long long* net = nullptr;
+  CK(cudaMallocAsync(&net, 8 * (size_t)g->n, g->stream));
+  cudaMemsetAsync(net, 0, 8 * (size_t)g->n, g->stream);
   if (g->layout == WBPR_LAYOUT_RCSR)
-    verify_rcsr<<<g->sms * 4, 256, 0, g->stream>>>(g->frow, g->farc, g->fcb, g->fcap, g->rrow, g->rarc,
-                                                   g->e, g->vlab, g->h, g->n, g->s, g->t, dacc);
+    verify_arcs_rcsr<<<g->sms * 8, 256, 0, g->stream>>>(g->frow, g->farc, g->fcb, g->fcap, g->rrow, g->rarc,
+                                                        g->vlab, g->h, g->n, g->s, g->m, net, dacc);
   else
-    verify_bcsr<<<g->sms * 4, 256, 0, g->stream>>>(g->row, g->arc, g->arx, g->e, g->vlab, g->h, g->n, g->s,
-                                                   g->t, dacc);
+    verify_arcs_bcsr<<<g->sms * 8, 256, 0, g->stream>>>(g->row, g->arc, g->arx, g->vlab, g->h, g->n, g->s,
+                                                        2 * g->m, net, dacc);
+  verify_vertices<<<g->sms * 4, 256, 0, g->stream>>>(g->e, g->vlab, net, g->n, g->s, g->t, dacc);
+  cudaFreeAsync(net, g->stream);
   VerifyAcc h;
   int ls = 0, et = 0;
   cudaError_t ce = cudaGetLastError();
@@ -1250,7 +1321,7 @@ wbpr_status wbpr_mincut_adjoint(wbpr_graph* g, int32_t side, int8_t* indicator, 
     st = bfs_labels(g, g->s, 1, -1);
   }
   if (st) return st;
-  indicator_kernel<<<g->sms * 4, 256, 0, g->stream>>>(g->ioff, g->row, g->arc, g->farc, g->vlab, g->n,
+  indicator_kernel<<<g->sms * 8, 256, 0, g->stream>>>(g->ioff, g->row, g->arc, g->farc, g->vlab, g->n, g->m,
                                                       side, g->ind);
   CK(cudaGetLastError());
   CK(cudaEventRecord(g->ev1, g->stream));

@@ -177,6 +177,8 @@ struct TopoB {  // BCSR16: row[n+1], arc {dst, cf}, arx {rev, cap}
     int r = __ldg(&arx[a].x);
     return __ldcg(&arc[r].y);
   }
+  // address of the twin's residual (one load here, none for RCSR forward)
+  __device__ __forceinline__ const int* twin_ptr(int, int a) const { return &arc[__ldg(&arx[a].x)].y; }
 };
 
 struct TopoR {  // RCSR: forward {dst, cf_f} + cf_b, reverse {tail, forward id}
@@ -222,6 +224,9 @@ struct TopoR {  // RCSR: forward {dst, cf_f} + cf_b, reverse {tail, forward id}
     if (k == 0) return __ldcg(fcb + a);
     int fi = __ldg(&rarc[a].y);
     return __ldcg(&farc[fi].y);
+  }
+  __device__ __forceinline__ const int* twin_ptr(int k, int a) const {
+    return k == 0 ? fcb + a : &farc[__ldg(&rarc[a].y)].y;
   }
 };
 
@@ -934,9 +939,9 @@ constexpr int kTdChunk = 1024;
 // into fr, long rows as chunk items into frh.  All lanes call it.
 template <class Topo>
 __device__ __forceinline__ void warp_frontier(const Params<Topo>& p, int* fcnt, int* fhcnt, int fn, int v,
-                                              bool pred, BlockAcc& acc) {
+                                              bool pred, BlockAcc& acc, int dpre = -1) {
   int d = 0;
-  if (pred) d = p.g.deg(v);
+  if (pred) d = dpre >= 0 ? dpre : p.g.deg(v);
   const bool lng = pred && d > kTdHeavy;
   warp_append(p.fr[fn], fcnt, v, pred && !lng);
   if (lng) {
@@ -955,37 +960,49 @@ template <class Topo, int DIR>
 __device__ __forceinline__ void td_batch(const Params<Topo>& p, const VRow& r, int base, int vend, int level,
                                          int fn, BlockAcc& acc, unsigned long long& arcs) {
   const int lane = threadIdx.x & 31;
-  int kk[4], aa[4], dst[4];
+  int dst[4], cf[4], dg[4];
+  const int* tp[4];
   bool ok[4];
+  // step 1: heads (and residuals or twin addresses) of 4 arcs per lane
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int vi = base + q * 32 + lane;
     ok[q] = vi < vend;
-    dst[q] = -1;
+    dst[q] = 0;
+    cf[q] = 1;
+    tp[q] = nullptr;
     if (ok[q]) {
-      vidx(r, vi, kk[q], aa[q]);
+      int kk, aa;
+      vidx(r, vi, kk, aa);
       if (DIR == 0) {
-        dst[q] = p.g.head(kk[q], aa[q]);
+        dst[q] = p.g.head(kk, aa);
+        tp[q] = p.g.twin_ptr(kk, aa);
       } else {
-        int cf;
-        p.g.load(kk[q], aa[q], dst[q], cf);
-        ok[q] = cf > 0;
+        p.g.load(kk, aa, dst[q], cf[q]);
       }
       ++arcs;
     }
   }
+  // step 2: label of the head, the residual towards this row, the head's
+  // degree (for the next frontier), all independent of each other
+  int lv[4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q)
-    if (ok[q]) ok[q] = dst[q] != p.bfs_excl && __ldcg(p.lab + dst[q]) == p.n;
-  if (DIR == 0) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-      if (ok[q]) ok[q] = p.g.twin_cf(kk[q], aa[q]) > 0;
+  for (int q = 0; q < 4; ++q) {
+    lv[q] = 0;
+    dg[q] = 0;
+    if (ok[q]) {
+      lv[q] = __ldcg(p.lab + dst[q]);
+      if (DIR == 0) cf[q] = __ldcg(tp[q]);
+      dg[q] = p.g.deg(dst[q]);
+    }
   }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) ok[q] = ok[q] && cf[q] > 0 && lv[q] == p.n && dst[q] != p.bfs_excl;
+  // step 3: claim
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const bool won = ok[q] && atomicCAS(p.lab + dst[q], p.n, level + 1) == p.n;
-    warp_frontier(p, &p.ctl->fcount[fn], &p.ctl->fhcount[fn], fn, dst[q], won, acc);
+    warp_frontier(p, &p.ctl->fcount[fn], &p.ctl->fhcount[fn], fn, dst[q], won, acc, dg[q]);
   }
 }
 
@@ -1049,85 +1066,116 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   const int gw = gt >> 5, nwarps = gs >> 5;
   unsigned long long arcs = 0, verts = 0, found = 0, fdeg = 0;
-  // short rows (<= kLightDeg): a thread each, 4 rows and 4 arcs in flight
+  // short rows (<= kLightDeg): a thread each; 4 rows advance together, 4 arcs
+  // of each in flight per step
   for (int i0 = gt; i0 < p.n_light; i0 += 4 * gs) {
     int xs[4];
     bool todo[4];
+    VRow rr[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int i = i0 + q * gs;
       xs[q] = i < p.n_light ? __ldg(p.cls + i) : -1;
     }
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-      todo[q] = xs[q] >= 0 && xs[q] != p.bfs_excl && __ldcg(p.lab + xs[q]) == p.n;
-#pragma unroll 1
     for (int q = 0; q < 4; ++q) {
+      todo[q] = xs[q] >= 0 && xs[q] != p.bfs_excl && __ldcg(p.lab + xs[q]) == p.n;
       if (xs[q] >= 0) ++verts;
-      if (!todo[q]) continue;
-      const int x = xs[q];
-      const VRow r = vrow(p.g, x);
-      bool hit = false;
-      for (int v0 = 0; v0 < r.deg && !hit; v0 += 4) {
-        int kk[4], aa[4], dst[4], cf[4];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      rr[q].b0 = rr[q].d0 = rr[q].b1 = rr[q].deg = 0;
+      if (todo[q]) rr[q] = vrow(p.g, xs[q]);
+    }
+#pragma unroll 1
+    for (int v0 = 0; todo[0] || todo[1] || todo[2] || todo[3]; v0 += 4) {
+      int dst[4][4], cf[4][4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
 #pragma unroll
         for (int w = 0; w < 4; ++w) {
-          cf[w] = 0;
-          dst[w] = 0;
-          if (v0 + w < r.deg) {
-            vidx(r, v0 + w, kk[w], aa[w]);
-            p.g.load(kk[w], aa[w], dst[w], cf[w]);
+          cf[q][w] = 0;
+          dst[q][w] = 0;
+          if (todo[q] && v0 + w < rr[q].deg) {
+            int kk, aa;
+            vidx(rr[q], v0 + w, kk, aa);
+            p.g.load(kk, aa, dst[q][w], cf[q][w]);
+            if (DIR == 1) cf[q][w] = p.g.twin_cf(kk, aa);
             ++arcs;
           }
         }
 #pragma unroll
-        for (int w = 0; w < 4; ++w) {
-          if (v0 + w >= r.deg) continue;
-          if (DIR == 0) {
-            if (cf[w] > 0 && __ldcg(p.lab + dst[w]) == level) hit = true;
-          } else {
-            if (__ldcg(p.lab + dst[w]) == level && p.g.twin_cf(kk[w], aa[w]) > 0) hit = true;
-          }
+      for (int q = 0; q < 4; ++q) {
+        bool hit = false;
+#pragma unroll
+        for (int w = 0; w < 4; ++w)
+          if (cf[q][w] > 0 && __ldcg(p.lab + dst[q][w]) == level) hit = true;
+        if (todo[q] && hit) {
+          p.lab[xs[q]] = level + 1;
+          ++found;
+          fdeg += (unsigned long long)rr[q].deg;
         }
-      }
-      if (hit) {
-        p.lab[x] = level + 1;
-        ++found;
-        fdeg += (unsigned long long)r.deg;
+        if (hit || v0 + 4 >= rr[q].deg) todo[q] = false;
       }
     }
   }
-  // medium rows: a warp each, 4 arcs per lane in flight
-  for (int i = gw; i < p.n_medium; i += nwarps) {
-    const int x = __ldg(p.cls + p.n_light + i);
-    if (lane == 0) ++verts;
-    if (x == p.bfs_excl || __ldcg(p.lab + x) != p.n) continue;
-    bool hit = false;
-    int deg = 0;
-    for (int k = 0; k < Topo::kSeg && !hit; ++k) {
-      int b, e;
-      p.g.seg(x, k, b, e);
-      deg += e - b;
-      for (int base = b; base < e; base += 128) {
-        bool h = false;
+  // medium rows: 8-lane tiles, four rows per warp at a time; the warp first
+  // checks 32 rows' labels at once and keeps only the unvisited ones
+  {
+    const int sub = lane >> 3, sl = lane & 7;
+    const unsigned smask = 0xffu << (sub * 8);
+    for (int base = gw * 32; base < p.n_medium; base += nwarps * 32) {
+      const int i = base + lane;
+      int x = -1;
+      if (i < p.n_medium) {
+        x = __ldg(p.cls + p.n_light + i);
+        ++verts;
+      }
+      const bool open = x >= 0 && x != p.bfs_excl && __ldcg(p.lab + x) == p.n;
+      VRow r;
+      r.b0 = r.d0 = r.b1 = r.deg = 0;
+      if (open) r = vrow(p.g, x);
+      unsigned todo = __ballot_sync(0xffffffffu, open);
+      while (todo) {
+        // this tile's row: the (sub+1)-th open one; `rest` drops the first four
+        unsigned rest = todo, pick = 32;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int a = base + q * 32 + lane;
-          if (a < e) {
-            ++arcs;
-            h |= bu_arc<Topo, DIR>(p, k, a, level);
+        for (int j = 0; j < 4; ++j) {
+          if (j == sub && rest) pick = __ffs(rest) - 1;
+          rest &= rest - 1u;
+        }
+        const int src = pick < 32 ? (int)pick : lane;
+        const int xr = __shfl_sync(0xffffffffu, x, src);
+        VRow q;
+        q.b0 = __shfl_sync(0xffffffffu, r.b0, src);
+        q.d0 = __shfl_sync(0xffffffffu, r.d0, src);
+        q.b1 = __shfl_sync(0xffffffffu, r.b1, src);
+        q.deg = __shfl_sync(0xffffffffu, r.deg, src);
+        todo = rest;
+        if (pick < 32) {
+          bool hit = false;
+          for (int v0 = 0; v0 < q.deg && !hit; v0 += 32) {
+            bool h = false;
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+              const int vi = v0 + w * 8 + sl;
+              if (vi < q.deg) {
+                int kk, aa;
+                vidx(q, vi, kk, aa);
+                ++arcs;
+                h |= bu_arc<Topo, DIR>(p, kk, aa, level);
+              }
+            }
+            hit = __any_sync(smask, h);
+          }
+          if (hit && sl == 0) {
+            p.lab[xr] = level + 1;
+            ++found;
+            fdeg += (unsigned long long)q.deg;
           }
         }
-        if (__any_sync(0xffffffffu, h)) {
-          hit = true;
-          break;
-        }
+        __syncwarp();
       }
-    }
-    if (hit && lane == 0) {
-      p.lab[x] = level + 1;
-      ++found;
-      fdeg += (unsigned long long)p.g.deg(x);
     }
   }
   // long rows: blocks over static 2048-arc chunks; first chunk to hit wins
