@@ -1119,15 +1119,20 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
       }
     }
   }
-  // medium rows: 8-lane tiles, four rows per warp at a time; the warp first
-  // checks 32 rows' labels at once and keeps only the unvisited ones
+  // medium rows: the warp checks a batch of rows' labels at once (32 rows, or
+  // 8 when there are too few rows to give every warp several batches); 8-lane
+  // tiles scan the open rows four at a time over their first kBuTile arcs
+  // (where most hits are), and the whole warp finishes the rows that are
+  // longer and have not hit yet
   {
+    constexpr int kBuTile = 128;
     const int sub = lane >> 3, sl = lane & 7;
     const unsigned smask = 0xffu << (sub * 8);
-    for (int base = gw * 32; base < p.n_medium; base += nwarps * 32) {
+    const int B = p.n_medium >= 64 * nwarps ? 32 : 8;
+    for (int base = gw * B; base < p.n_medium; base += nwarps * B) {
       const int i = base + lane;
       int x = -1;
-      if (i < p.n_medium) {
+      if (lane < B && i < p.n_medium) {
         x = __ldg(p.cls + p.n_light + i);
         ++verts;
       }
@@ -1136,6 +1141,7 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
       r.b0 = r.d0 = r.b1 = r.deg = 0;
       if (open) r = vrow(p.g, x);
       unsigned todo = __ballot_sync(0xffffffffu, open);
+      unsigned big = 0;
       while (todo) {
         // this tile's row: the (sub+1)-th open one; `rest` drops the first four
         unsigned rest = todo, pick = 32;
@@ -1152,14 +1158,16 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
         q.b1 = __shfl_sync(0xffffffffu, r.b1, src);
         q.deg = __shfl_sync(0xffffffffu, r.deg, src);
         todo = rest;
+        bool defer = false;
         if (pick < 32) {
+          const int lim = min(q.deg, kBuTile);
           bool hit = false;
-          for (int v0 = 0; v0 < q.deg && !hit; v0 += 32) {
+          for (int v0 = 0; v0 < lim && !hit; v0 += 32) {
             bool h = false;
 #pragma unroll
             for (int w = 0; w < 4; ++w) {
               const int vi = v0 + w * 8 + sl;
-              if (vi < q.deg) {
+              if (vi < lim) {
                 int kk, aa;
                 vidx(q, vi, kk, aa);
                 ++arcs;
@@ -1173,8 +1181,39 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
             ++found;
             fdeg += (unsigned long long)q.deg;
           }
+          defer = !hit && q.deg > kBuTile && sl == 0;
         }
-        __syncwarp();
+        big |= __reduce_or_sync(0xffffffffu, defer ? (1u << pick) : 0u);
+      }
+      while (big) {
+        const int src = __ffs(big) - 1;
+        big &= big - 1u;
+        const int xr = __shfl_sync(0xffffffffu, x, src);
+        VRow q;
+        q.b0 = __shfl_sync(0xffffffffu, r.b0, src);
+        q.d0 = __shfl_sync(0xffffffffu, r.d0, src);
+        q.b1 = __shfl_sync(0xffffffffu, r.b1, src);
+        q.deg = __shfl_sync(0xffffffffu, r.deg, src);
+        bool hit = false;
+        for (int v0 = kBuTile; v0 < q.deg && !hit; v0 += 128) {
+          bool h = false;
+#pragma unroll
+          for (int w = 0; w < 4; ++w) {
+            const int vi = v0 + w * 32 + lane;
+            if (vi < q.deg) {
+              int kk, aa;
+              vidx(q, vi, kk, aa);
+              ++arcs;
+              h |= bu_arc<Topo, DIR>(p, kk, aa, level);
+            }
+          }
+          hit = __any_sync(0xffffffffu, h);
+        }
+        if (hit && lane == 0) {
+          p.lab[xr] = level + 1;
+          ++found;
+          fdeg += (unsigned long long)q.deg;
+        }
       }
     }
   }
