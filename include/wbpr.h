@@ -156,6 +156,25 @@ wbpr_status wbpr_read_dimacs(const char* path, wbpr_host_csr** out);
 /* Writers: SNAP binary (graph.cpp:219-233) and DIMACS text. */
 wbpr_status wbpr_write_snap_bin(const char* path, const wbpr_csr* g);
 wbpr_status wbpr_write_dimacs(const char* path, const wbpr_csr* g);
+/* -v 3: graph cache, new (the SNAP .bin above has no capacities and no
+ * terminals): "WBPRCSR1", int32 version 1, int32 flags (bit 0: capacities
+ * present), int64 n, m, m_declared, int32 s, t, then int32 offsets[n+1],
+ * destinations[m], capacities[m]; little endian.  Reading is one copy. */
+wbpr_status wbpr_write_graph_cache(const char* path, const wbpr_csr* g);
+wbpr_status wbpr_read_graph_cache(const char* path, wbpr_host_csr** out);
+/* Maximum-flow solution in DIMACS form: "s <flow>" and one "f u v x" line
+ * (1-based) per input arc with x = arc_flow[i] > 0, in input order.  Give it
+ * the flows of a completed flow (wbpr_complete_flow, then wbpr_read_state). */
+wbpr_status wbpr_write_dimacs_flow(const char* path, const wbpr_csr* g, int64_t flow,
+                                   const int32_t* arc_flow);
+/* Bipartite matching as maximum flow (WBPR paper, section IV-A): left
+ * vertices 0..L-1, right L..L+R-1, s = L+R, t = L+R+1; arcs s->l, l->r for
+ * every listed pair (left[k], right[k]) (ids 0-based within their side;
+ * duplicates kept once) and r->t, all of capacity 1.  The matching is the set
+ * of l->r arcs that carry flow in a completed flow. */
+wbpr_status wbpr_bipartite_network(int32_t L, int32_t R, int64_t num_pairs,
+                                   const int32_t* left, const int32_t* right,
+                                   wbpr_host_csr** out);
 /* Copy a caller CSR into a library-owned one. */
 wbpr_status wbpr_host_csr_copy(const wbpr_csr* in, wbpr_host_csr** out);
 void wbpr_host_csr_free(wbpr_host_csr* g);
@@ -189,6 +208,8 @@ wbpr_status wbpr_gen_grid(int32_t w, int32_t h, uint64_t seed,
                           wbpr_host_csr** out);
 
 /* ---- residual-graph builders (exact reverse pairing, O(n + m)) ----------- */
+/* (wbpr_graph_create builds the same arrays on the device; these host
+ * builders are for callers that want them in host memory.) */
 /* RCSR (maxflow-cuda/src/graph.cpp:317-402): roffsets[n+1], rdestinations[m],
  * flow_index[m] (reverse entry -> forward arc id).  Caller-allocated. */
 wbpr_status wbpr_build_rcsr(const wbpr_csr* g, int32_t* roffsets,
@@ -217,6 +238,11 @@ int64_t wbpr_graph_device_bytes(const wbpr_graph* g);
  * RCSR handle. */
 wbpr_status wbpr_graph_read_bcsr(const wbpr_graph* g, int32_t* offsets, int32_t* destinations,
                                  int32_t* capacities, int32_t* backward_idx);
+/* The same for an RCSR handle, in the format of wbpr_build_rcsr (roffsets[n+1],
+ * rdestinations[m], flow_index[m]; the forward arrays are the input CSR).
+ * INVALID_ARG for a BCSR handle. */
+wbpr_status wbpr_graph_read_rcsr(const wbpr_graph* g, int32_t* roffsets, int32_t* rdestinations,
+                                 int32_t* flow_index);
 /* Fresh solve: reset residuals to capacities, preflow from s, push/relabel to
  * a maximum preflow.  Result flow = excess(t). s/t = -1 use the graph's. */
 wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo,
@@ -244,6 +270,17 @@ wbpr_status wbpr_verify(wbpr_graph* g, wbpr_verify_report* rep);
  * g = [u in S and v not in S]).  `indicator` is a host buffer of m bytes. */
 wbpr_status wbpr_mincut_adjoint(wbpr_graph* g, int32_t side, int8_t* indicator,
                                 float* adjoint_ms);
+/* Turn the maximum preflow of the last solve into a maximum flow: the excess
+ * left at vertices that cannot reach t is pushed back to s (a second solve
+ * with s as the sink), so every vertex other than s and t conserves flow.
+ * Per-arc flows read afterwards (wbpr_read_state) form a valid maximum flow;
+ * the flow value is unchanged.  `ms` (may be NULL) receives the device time. */
+wbpr_status wbpr_complete_flow(wbpr_graph* g, float* ms);
+/* Vertex sides of the two extreme minimum cuts: side 0 -> in_set[v] = 1 iff v
+ * can reach t in the residual graph (the sink side T); side 1 -> in_set[v] = 1
+ * iff v is reachable from s after wbpr_complete_flow (the source side S).
+ * `in_set` is a host buffer of n bytes. */
+wbpr_status wbpr_cut_sides(wbpr_graph* g, int32_t side, int8_t* in_set);
 
 /* ---- batched solver ---------------------------------------------------------- */
 /* No counterpart in the reference (its CLI solves one graph per process).

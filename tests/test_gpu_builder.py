@@ -1,9 +1,11 @@
-"""On-device BCSR build (wbpr_graph_create, BCSR layout): the residual graph
-it leaves in HBM must be the host builder's (wbpr_build_bcsr, the layout of
-maxflow-bcsr/src/graph.cpp:317-360) entry for entry -- offsets, heads,
-capacities and twin indices -- for every shape the sort and the length
-classes see: empty rows, isolated vertices, parallel arcs, rows longer than
-the push chunk, heads that need one to four radix passes."""
+"""On-device residual-graph build (wbpr_graph_create): the graph it leaves in
+HBM must be the host builder's entry for entry -- BCSR offsets, heads,
+capacities and twin indices (wbpr_build_bcsr, the layout of
+maxflow-bcsr/src/graph.cpp:317-360), RCSR reverse offsets, reverse heads and
+flow_index (wbpr_build_rcsr, maxflow-cuda/src/graph.cpp:317-402) -- for every
+shape the sort and the length classes see: empty rows, isolated vertices,
+parallel arcs, rows longer than the push chunk, heads that need one to four
+radix passes."""
 import numpy as np
 import pytest
 
@@ -18,6 +20,11 @@ def same_as_host(g):
         dev = d.read_bcsr()
     host = W.build_bcsr(g)
     for a, b, name in zip(dev, host, ("offsets", "destinations", "capacities", "backward_idx")):
+        assert np.array_equal(a, b), name
+    with W.DeviceGraph(g, "rcsr") as d:
+        dev = d.read_rcsr()
+    host = W.build_rcsr(g)
+    for a, b, name in zip(dev, host, ("roffsets", "rdestinations", "flow_index")):
         assert np.array_equal(a, b), name
 
 
@@ -60,19 +67,24 @@ def test_generators():
     same_as_host(W.gen_grid(40, 30, 1))
 
 
-def test_device_overflow_check():
+@pytest.mark.parametrize("layout", ["bcsr", "rcsr"])
+def test_device_overflow_check(layout):
     g = W.Graph.from_arcs(3, [0, 0, 1, 1], [1, 2, 2, 2], [2**31 - 1, 2**31 - 1, 2**31 - 1, 5], 0, 2)
     with pytest.raises(W.WbprError) as ei:
-        W.DeviceGraph(g, "bcsr")
+        W.DeviceGraph(g, layout)
     assert ei.value.status == 4
     # at the limit exactly it builds
     g = W.Graph.from_arcs(3, [0, 1], [2, 2], [2**31 - 2, 1], 0, 2)
     same_as_host(g)
 
 
-def test_rcsr_handle_has_no_bcsr():
+def test_read_back_matches_the_layout():
     g = random_graph(50, 200, 1)
     with W.DeviceGraph(g, "rcsr") as d:
         with pytest.raises(W.WbprError) as ei:
             d.read_bcsr()
+        assert ei.value.status == 1
+    with W.DeviceGraph(g, "bcsr") as d:
+        with pytest.raises(W.WbprError) as ei:
+            d.read_rcsr()
         assert ei.value.status == 1

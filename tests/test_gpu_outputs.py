@@ -1,0 +1,119 @@
+"""What comes after the solve: the maximum flow itself (wbpr_complete_flow
+then per-arc flows), the vertex sides of the two extreme minimum cuts
+(wbpr_cut_sides), the DIMACS solution written by the CLI (-o), the graph
+cache (-c / -v 3) and the bipartite-matching front end.  Checked against the
+oracle's exact values and by exact conservation on the host."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+import wbpr_gb300 as W
+from wbpr_gb300 import build as wb
+
+pytestmark = pytest.mark.gpu
+
+
+def graphs():
+    yield W.gen_genrmf(5, 6, 1, 100, 1)
+    yield W.gen_rmat(12, 8, seed=3)
+    yield W.gen_grid(32, 32, 2)
+    yield W.gen_bipartite(500, 400, 2.0, 64, 3)
+    rng = np.random.default_rng(5)
+    n, m = 80, 600  # parallel and antiparallel arcs, zero capacities
+    yield W.Graph.from_arcs(n, rng.integers(0, n, m), rng.integers(0, n, m), rng.integers(0, 6, m), 0, n - 1)
+
+
+def check_flow(g, f, value):
+    assert np.all(f >= 0) and np.all(f <= g.cap)
+    tails = np.repeat(np.arange(g.n), np.diff(g.off))
+    net = np.zeros(g.n, np.int64)
+    np.add.at(net, tails, -f.astype(np.int64))
+    np.add.at(net, g.dst, f.astype(np.int64))
+    inner = np.ones(g.n, bool)
+    inner[[g.s, g.t]] = False
+    assert np.all(net[inner] == 0)
+    assert net[g.t] == value and net[g.s] == -value
+
+
+@pytest.mark.parametrize("layout", ["bcsr", "rcsr"])
+def test_completed_flow_is_a_maximum_flow(layout):
+    for g in graphs():
+        v = oracle.dinic(g.n, g.off, g.dst, g.cap, g.s, g.t)
+        with W.DeviceGraph(g, layout) as d:
+            r = d.solve("vc", g.s, g.t)
+            assert r.flow == v
+            d.complete_flow()
+            h, e, f = d.read_state()
+            check_flow(g, f, v)
+            inner = np.ones(g.n, bool)
+            inner[[g.s, g.t]] = False
+            assert np.all(e[inner] == 0)
+            rep = d.verify()
+            assert rep["ok"] and rep["flow_value"] == v
+            # a second call finds nothing left to return
+            d.complete_flow()
+            assert np.array_equal(d.read_state()[2], f)
+
+
+@pytest.mark.parametrize("layout", ["bcsr", "rcsr"])
+def test_cut_sides_give_the_extreme_cuts(layout):
+    for g in graphs():
+        v, sink_side, src_side = oracle.mincut(g.n, g.off, g.dst, g.cap, g.s, g.t)
+        tails = np.repeat(np.arange(g.n), np.diff(g.off))
+        with W.DeviceGraph(g, layout) as d:
+            d.solve("vc", g.s, g.t)
+            T = d.cut_sides(0).astype(bool)
+            S = d.cut_sides(1).astype(bool)
+        assert T[g.t] and not T[g.s] and S[g.s] and not S[g.t]
+        assert np.array_equal((~T[tails] & T[g.dst]).astype(np.int8), sink_side)
+        assert np.array_equal((S[tails] & ~S[g.dst]).astype(np.int8), src_side)
+        assert int(g.cap[~T[tails] & T[g.dst]].astype(np.int64).sum()) == v
+        assert not np.any(S & T)
+
+
+def test_bipartite_matching():
+    scipy_graph = pytest.importorskip("scipy.sparse.csgraph")
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(8)
+    for L, R, k in ((1, 1, 1), (50, 40, 200), (3000, 2000, 12000)):
+        left = rng.integers(0, L, k)
+        right = rng.integers(0, R, k)
+        size, pairs = W.bipartite_matching(L, R, left, right)
+        a = sp.csr_matrix((np.ones(k), (left, right)), shape=(L, R))
+        match = scipy_graph.maximum_bipartite_matching(a, perm_type="column")
+        assert size == int((match >= 0).sum())
+        assert len(np.unique(pairs[:, 0])) == size and len(np.unique(pairs[:, 1])) == size
+        edges = set(zip(left.tolist(), right.tolist()))
+        assert all((int(x), int(y)) in edges for x, y in pairs)
+        g = W.bipartite_network(L, R, left, right)
+        assert size == oracle.dinic(g.n, g.off, g.dst, g.cap, g.s, g.t)
+
+
+def test_cli_solution_and_cache(tmp_path):
+    g = W.gen_genrmf(4, 5, 1, 300, 4)
+    src = tmp_path / "g.dimacs"
+    W.write_dimacs(str(src), g)
+    sol, cache = tmp_path / "sol.txt", tmp_path / "g.wgc"
+    r = subprocess.run([wb.CLI, "-v", "2", "-f", str(src), "-a", "1", "-l", "bcsr", "-o", str(sol), "-c", str(cache)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    v = oracle.dinic(g.n, g.off, g.dst, g.cap, g.s, g.t)
+    assert f"is {v}, {v}" in r.stdout
+    lines = sol.read_text().splitlines()
+    assert f"s {v}" in lines
+    f = np.zeros(g.m, np.int64)
+    pos = {}
+    tails = np.repeat(np.arange(g.n), np.diff(g.off))
+    for i in range(g.m):
+        pos.setdefault((int(tails[i]) + 1, int(g.dst[i]) + 1), []).append(i)
+    for line in lines:
+        if line.startswith("f "):
+            _, a, b, x = line.split()
+            f[pos[(int(a), int(b))].pop(0)] = int(x)
+    check_flow(g, f, v)
+    r2 = subprocess.run([wb.CLI, "-v", "3", "-f", str(cache), "-a", "0"], capture_output=True, text=True)
+    assert r2.returncode == 0 and f"is {v}, {v}" in r2.stdout

@@ -174,13 +174,18 @@ def test_rmat_independent_of_thread_count():
     assert one == many
 
 
-def test_overflowing_capacities_are_rejected(has_gpu):
-    # sum of capacities into t exceeds int32: the RCSR layout refuses it on the
-    # host before any device work (BCSR checks while it builds on the device)
-    g = W.Graph.from_arcs(3, [0, 0, 1, 1], [1, 2, 2, 2], [2**31 - 1, 2**31 - 1, 2**31 - 1, 5], 0, 2)
-    with pytest.raises(W.WbprError) as ei:
-        W.DeviceGraph(g, "rcsr")
-    assert ei.value.status == 4
+def test_overflowing_arc_count_is_rejected_on_the_host():
+    # more than 2^31 - 1 input arcs: refused by the host checks before any
+    # array is read or any device call is made (incoming-capacity sums that
+    # overflow int32 are refused by the device build, see the GPU tests)
+    dummy = np.zeros(4, np.int32)
+    v = W.api.CsrView()
+    v.num_nodes = 3
+    v.num_edges = 2**31
+    v.offsets = v.destinations = v.capacities = dummy.ctypes.data_as(W.api._i32p)
+    for layout in (0, 1):
+        h = W.api.C.c_void_p()
+        assert W.lib().wbpr_graph_create(W.api.C.byref(v), layout, W.api.C.byref(h)) == 4
 
 
 def test_cli_usage_and_errors(tmp_path):
@@ -191,3 +196,99 @@ def test_cli_usage_and_errors(tmp_path):
     assert r.returncode == 1
     r = subprocess.run([cli, "-v", "9", "-f", "x"], capture_output=True, text=True)
     assert r.returncode == 1 and "Invalid file type" in r.stdout
+
+
+# ---- graph cache, DIMACS solution writer, bipartite network ---------------
+def test_graph_cache_round_trip(tmp_path):
+    g = W.gen_genrmf(4, 6, 1, 500, 2)
+    p = str(tmp_path / "g.wgc")
+    W.write_graph_cache(p, g)
+    h = W.read_graph_cache(p)
+    assert (h.n, h.m, h.s, h.t) == (g.n, g.m, g.s, g.t)
+    assert np.array_equal(h.off, g.off) and np.array_equal(h.dst, g.dst) and np.array_equal(h.cap, g.cap)
+    # without capacities the cache stores none and reads back capacity 1
+    v = g.view()
+    v.capacities = None
+    q = str(tmp_path / "u.wgc")
+    assert W.lib().wbpr_write_graph_cache(os.fsencode(q), W.api.C.byref(v)) == 0
+    u = W.read_graph_cache(q)
+    assert np.array_equal(u.dst, g.dst) and np.all(u.cap == 1)
+    assert os.path.getsize(q) == 48 + 4 * (g.n + 1 + g.m)
+
+
+def test_graph_cache_rejects_damage(tmp_path):
+    g = W.gen_genrmf(3, 3, 1, 50, 1)
+    p = tmp_path / "g.wgc"
+    W.write_graph_cache(str(p), g)
+    raw = p.read_bytes()
+    for bad in (raw[:-4], raw + b"\0\0\0\0", b"WBPRCSR2" + raw[8:], raw[:8] + b"\2\0\0\0" + raw[12:]):
+        p.write_bytes(bad)
+        with pytest.raises(W.WbprError) as ei:
+            W.read_graph_cache(str(p))
+        assert ei.value.status == 6
+    # an arc head out of range
+    arr = bytearray(raw)
+    at = 48 + 4 * (g.n + 1)
+    arr[at:at + 4] = (g.n + 5).to_bytes(4, "little")
+    p.write_bytes(bytes(arr))
+    with pytest.raises(W.WbprError):
+        W.read_graph_cache(str(p))
+
+
+def test_dimacs_reader_is_thread_count_independent(tmp_path):
+    g = W.gen_rmat(12, 8, seed=4)
+    p = str(tmp_path / "r.dimacs")
+    W.write_dimacs(p, g)
+    # comments and a terminal line among the arcs; the last "n s" counts
+    lines = open(p).read().splitlines()
+    lines.insert(len(lines) // 2, "c a comment in the middle")
+    lines.insert(len(lines) // 3, f"n {g.t + 1} t")
+    lines.append(f"n {g.s + 1} s")
+    open(p, "w").write("\n".join(lines) + "\n")
+    code = ("import sys, hashlib; sys.path.insert(0, %r); import wbpr_gb300 as W; g = W.read_dimacs(%r);"
+            "print(g.n, g.m, g.s, g.t, hashlib.sha256(g.off.tobytes() + g.dst.tobytes() + g.cap.tobytes())"
+            ".hexdigest())" % (ROOT, p))
+    one = subprocess.run(["python3", "-c", code], env=dict(os.environ, WBPR_HOST_THREADS="1"),
+                         capture_output=True, text=True, check=True).stdout
+    many = subprocess.run(["python3", "-c", code], env=dict(os.environ, WBPR_HOST_THREADS="7"),
+                          capture_output=True, text=True, check=True).stdout
+    assert one == many
+    h = W.read_dimacs(p)
+    assert np.array_equal(h.dst, g.dst) and np.array_equal(h.cap, g.cap) and (h.s, h.t) == (g.s, g.t)
+
+
+def test_dimacs_problem_line_after_arcs_is_rejected(tmp_path):
+    p = tmp_path / "bad.dimacs"
+    p.write_text("p max 3 2\nn 1 s\nn 3 t\na 1 2 5\np max 3 2\na 2 3 5\n")
+    with pytest.raises(W.WbprError) as ei:
+        W.read_dimacs(str(p))
+    assert ei.value.status == 6
+
+
+def test_dimacs_flow_writer(tmp_path):
+    g = W.Graph.from_arcs(4, [0, 0, 1, 2, 1], [1, 2, 3, 3, 2], [3, 2, 2, 3, 1], 0, 3)
+    flow = np.array([2, 2, 0, 2, 0], np.int32)  # in CSR order: 0->1, 0->2, 1->3, 1->2, 2->3
+    p = str(tmp_path / "sol.txt")
+    W.write_dimacs_flow(p, g, 4, flow)
+    text = open(p).read().splitlines()
+    assert text[1] == "s 4"
+    f_lines = [t for t in text if t.startswith("f ")]
+    heads = {(int(a), int(b)): int(c) for _, a, b, c in (t.split() for t in f_lines)}
+    tails = np.repeat(np.arange(g.n), np.diff(g.off))
+    expect = {(int(tails[i]) + 1, int(g.dst[i]) + 1): int(flow[i]) for i in range(g.m) if flow[i] > 0}
+    assert heads == expect
+    with pytest.raises(ValueError):
+        W.write_dimacs_flow(p, g, 4, flow[:3])
+
+
+def test_bipartite_network_shape():
+    g = W.bipartite_network(3, 2, [0, 1, 1, 2, 0], [0, 0, 1, 1, 0])
+    assert (g.n, g.s, g.t) == (7, 5, 6)
+    tails = np.repeat(np.arange(g.n), np.diff(g.off))
+    arcs = sorted(zip(tails.tolist(), g.dst.tolist()))
+    assert arcs == sorted([(0, 3), (1, 3), (1, 4), (2, 4), (3, 6), (4, 6), (5, 0), (5, 1), (5, 2)])
+    assert np.all(g.cap == 1)
+    for left, right in (([3], [0]), ([0], [2]), ([-1], [0])):
+        with pytest.raises(W.WbprError) as ei:
+            W.bipartite_network(3, 2, left, right)
+        assert ei.value.status == 1

@@ -81,10 +81,12 @@ ALGOS = {"tc": 0, "vc": 1, 0: 0, 1: 1}
 EXPORTED = [
     "wbpr_status_str", "wbpr_abi_version", "wbpr_default_tuning", "wbpr_device_count",
     "wbpr_last_error", "wbpr_read_snap_txt", "wbpr_read_snap_bin", "wbpr_read_dimacs",
-    "wbpr_write_snap_bin", "wbpr_write_dimacs", "wbpr_host_csr_copy", "wbpr_host_csr_free",
+    "wbpr_write_snap_bin", "wbpr_write_dimacs", "wbpr_write_graph_cache", "wbpr_read_graph_cache",
+    "wbpr_write_dimacs_flow", "wbpr_bipartite_network", "wbpr_complete_flow", "wbpr_cut_sides",
+    "wbpr_host_csr_copy", "wbpr_host_csr_free",
     "wbpr_gen_genrmf", "wbpr_gen_rmat", "wbpr_gen_bipartite", "wbpr_gen_layered", "wbpr_gen_grid",
     "wbpr_build_rcsr", "wbpr_build_bcsr", "wbpr_build_bcsr2", "wbpr_graph_create",
-    "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_graph_read_bcsr", "wbpr_solve", "wbpr_read_state",
+    "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_graph_read_bcsr", "wbpr_graph_read_rcsr", "wbpr_solve", "wbpr_read_state",
     "wbpr_verify", "wbpr_mincut_adjoint", "wbpr_rcsr_preflow", "wbpr_rcsr_push_relabel",
     "wbpr_read_trace", "wbpr_solve_bcsr_noalloc", "wbpr_batch_create", "wbpr_batch_destroy",
     "wbpr_batch_device_bytes", "wbpr_batch_solve", "wbpr_batch_instance_stats", "wbpr_batch_autotune",
@@ -115,6 +117,12 @@ def lib() -> C.CDLL:
         "wbpr_read_dimacs": (C.c_int, [C.c_char_p, hp]),
         "wbpr_write_snap_bin": (C.c_int, [C.c_char_p, C.POINTER(CsrView)]),
         "wbpr_write_dimacs": (C.c_int, [C.c_char_p, C.POINTER(CsrView)]),
+        "wbpr_write_graph_cache": (C.c_int, [C.c_char_p, C.POINTER(CsrView)]),
+        "wbpr_read_graph_cache": (C.c_int, [C.c_char_p, hp]),
+        "wbpr_write_dimacs_flow": (C.c_int, [C.c_char_p, C.POINTER(CsrView), C.c_int64, _i32p]),
+        "wbpr_bipartite_network": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, _i32p, _i32p, hp]),
+        "wbpr_complete_flow": (C.c_int, [vp, C.POINTER(C.c_float)]),
+        "wbpr_cut_sides": (C.c_int, [vp, C.c_int32, _i8p]),
         "wbpr_host_csr_copy": (C.c_int, [C.POINTER(CsrView), hp]),
         "wbpr_host_csr_free": (None, [C.POINTER(HostCsr)]),
         "wbpr_gen_genrmf": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, hp]),
@@ -131,6 +139,7 @@ def lib() -> C.CDLL:
         "wbpr_graph_destroy": (C.c_int, [vp]),
         "wbpr_graph_device_bytes": (C.c_int64, [vp]),
         "wbpr_graph_read_bcsr": (C.c_int, [vp, _i32p, _i32p, _i32p, _i32p]),
+        "wbpr_graph_read_rcsr": (C.c_int, [vp, _i32p, _i32p, _i32p]),
         "wbpr_solve": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int, C.POINTER(Tuning), C.POINTER(Result)]),
         "wbpr_read_state": (C.c_int, [vp, _i32p, _i32p, _i32p]),
         "wbpr_read_trace": (C.c_int32, [vp, C.POINTER(C.c_int64), C.c_int32]),
@@ -246,8 +255,57 @@ def read_dimacs(path: str) -> Graph:
     return _reader("wbpr_read_dimacs", path)
 
 
+def read_graph_cache(path: str) -> Graph:
+    """The library's own cache format (capacities and terminals included)."""
+    return _reader("wbpr_read_graph_cache", path)
+
+
 def read_graph(path: str, file_type: int) -> Graph:
-    return [read_snap_txt, read_snap_bin, read_dimacs][file_type](path)
+    """file_type as the CLI's -v: 0 SNAP text, 1 SNAP binary, 2 DIMACS, 3 cache."""
+    return [read_snap_txt, read_snap_bin, read_dimacs, read_graph_cache][file_type](path)
+
+
+def write_graph_cache(path: str, g: Graph) -> None:
+    v = g.view()
+    _check(lib().wbpr_write_graph_cache(os.fsencode(path), C.byref(v)), "wbpr_write_graph_cache")
+
+
+def write_dimacs_flow(path: str, g: Graph, flow: int, arc_flow) -> None:
+    """DIMACS solution: "s <flow>" and "f u v x" for every arc carrying flow."""
+    v = g.view()
+    f = np.ascontiguousarray(arc_flow, np.int32)
+    if f.shape != (g.m,):
+        raise ValueError("arc_flow must hold one value per input arc")
+    _check(lib().wbpr_write_dimacs_flow(os.fsencode(path), C.byref(v), int(flow), _p(f)),
+           "wbpr_write_dimacs_flow")
+
+
+def bipartite_network(L: int, R: int, left, right) -> Graph:
+    """Unit-capacity matching network: left 0..L-1, right L..L+R-1,
+    s = L+R, t = L+R+1 (pairs are 0-based within their side)."""
+    lt = np.ascontiguousarray(left, np.int32)
+    rt = np.ascontiguousarray(right, np.int32)
+    if lt.shape != rt.shape:
+        raise ValueError("left and right must have the same length")
+    out = C.POINTER(HostCsr)()
+    _check(lib().wbpr_bipartite_network(L, R, lt.size, _p(lt), _p(rt), C.byref(out)), "wbpr_bipartite_network")
+    return _take(out)
+
+
+def bipartite_matching(L: int, R: int, left, right, **tuning):
+    """Maximum matching of a bipartite graph: (size, pairs) with pairs an
+    (size, 2) array of (left id, right id)."""
+    g = bipartite_network(L, R, left, right)
+    with DeviceGraph(g, "bcsr") as d:
+        r = d.solve("vc", g.s, g.t, **tuning)
+        d.complete_flow()
+        _, _, f = d.read_state()
+    tails = np.repeat(np.arange(g.n, dtype=np.int64), np.diff(g.off))
+    sel = (tails < L) & (f > 0)
+    pairs = np.stack([tails[sel], g.dst[sel].astype(np.int64) - L], axis=1)
+    if len(pairs) != r.flow:
+        raise WbprError(5, "matching size differs from the flow value")
+    return int(r.flow), pairs
 
 
 def write_dimacs(path: str, g: Graph) -> None:
@@ -388,12 +446,32 @@ class DeviceGraph:
         _check(lib().wbpr_graph_read_bcsr(self._h, _p(off), _p(dst), _p(cap), _p(bidx)), "wbpr_graph_read_bcsr")
         return off, dst[:2 * self.m], cap[:2 * self.m], bidx[:2 * self.m]
 
+    def read_rcsr(self):
+        """The device-built RCSR reverse arrays, as build_rcsr returns them."""
+        roff = np.zeros(self.n + 1, np.int32)
+        k = max(self.m, 1)
+        rdst, fidx = np.zeros(k, np.int32), np.zeros(k, np.int32)
+        _check(lib().wbpr_graph_read_rcsr(self._h, _p(roff), _p(rdst), _p(fidx)), "wbpr_graph_read_rcsr")
+        return roff, rdst[:self.m], fidx[:self.m]
+
     def read_state(self):
         h = np.zeros(self.n, np.int32)
         e = np.zeros(self.n, np.int32)
         f = np.zeros(max(self.m, 1), np.int32)
         _check(lib().wbpr_read_state(self._h, _p(h), _p(e), _p(f)), "wbpr_read_state")
         return h, e, f[:self.m]
+
+    def complete_flow(self) -> float:
+        """Return stranded excess to s so the arc flows form a maximum flow."""
+        ms = C.c_float(0)
+        _check(lib().wbpr_complete_flow(self._h, C.byref(ms)), "wbpr_complete_flow")
+        return float(ms.value)
+
+    def cut_sides(self, side: int = 0) -> np.ndarray:
+        """Per-vertex membership (int8) of T (side 0) or S (side 1)."""
+        out = np.zeros(self.n, np.int8)
+        _check(lib().wbpr_cut_sides(self._h, side, out.ctypes.data_as(_i8p)), "wbpr_cut_sides")
+        return out
 
     def mincut_adjoint(self, side: int = 0):
         ind = np.zeros(max(self.m, 1), np.int8)

@@ -502,12 +502,17 @@ __global__ void db_fill_twin(const int* off, const int* skey, const int* sval, c
   }
 }
 
+// A row is one or two segments of offset arrays: BCSR [o1[u], o1[u+1]);
+// RCSR forward arcs [o1[u], o1[u+1]) then reverse entries [o2[u], o2[u+1]).
+__device__ __forceinline__ int seg_len(const int* o, int u) { return o ? __ldg(o + u + 1) - __ldg(o + u) : 0; }
+
 // length classes (flags for three stable compactions) and the chunk counts
 // cnt: [0] rows > kTdHeavy [1] their top-down chunk items [2] push-phase chunk bound
-__global__ void db_classify(const int* row, int n, int* f0, int* f1, int* f2, unsigned long long* cnt) {
+__global__ void db_classify(const int* o1, const int* o2, int n, int* f0, int* f1, int* f2,
+                            unsigned long long* cnt) {
   unsigned long long a = 0, b = 0, c = 0;
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u <= n; u += gridDim.x * blockDim.x) {
-    const int d = u < n ? row[u + 1] - row[u] : 0;
+    const int d = u < n ? seg_len(o1, u) + seg_len(o2, u) : 0;
     f0[u] = d > 0 && d <= kLightDeg;
     f1[u] = d > kLightDeg && d <= kHeavyDeg;
     f2[u] = d > kHeavyDeg;
@@ -528,32 +533,69 @@ __global__ void db_classify(const int* row, int n, int* f0, int* f1, int* f2, un
     if (c) atomicAdd(cnt + 2, c);
   }
 }
-__global__ void db_cls_scatter(const int* row, int n, const int* s0, const int* s1, const int* s2, int* cls) {
+__global__ void db_cls_scatter(const int* o1, const int* o2, int n, const int* s0, const int* s1, const int* s2,
+                               int* cls) {
   const int n0 = s0[n], n01 = n0 + s1[n];
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
-    const int d = row[u + 1] - row[u];
+    const int d = seg_len(o1, u) + seg_len(o2, u);
     if (d == 0) continue;
     if (d <= kLightDeg) cls[s0[u]] = u;
     else if (d <= kHeavyDeg) cls[n0 + s1[u]] = u;
     else cls[n01 + s2[u]] = u;
   }
 }
-__global__ void db_heavy_chunks(const int* row, const int* hcls, int nh, int* nch) {
+// chunk items of heavy row j: kChunk pieces of each segment
+__global__ void db_heavy_chunks(const int* o1, const int* o2, const int* hcls, int nh, int* nch) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j <= nh; j += gridDim.x * blockDim.x) {
     if (j == nh) {
       nch[j] = 0;
     } else {
       const int u = hcls[j];
-      nch[j] = (row[u + 1] - row[u] + kChunk - 1) / kChunk;
+      nch[j] = (seg_len(o1, u) + kChunk - 1) / kChunk + (seg_len(o2, u) + kChunk - 1) / kChunk;
     }
   }
 }
-__global__ void db_bch_fill(const int* row, const int* hcls, int nh, const int* cbase, int4* bch) {
+__global__ void db_bch_fill(const int* o1, const int* o2, const int* hcls, int nh, const int* cbase,
+                            int4* bch) {
   for (int j = blockIdx.x; j < nh; j += gridDim.x) {
-    const int u = hcls[j], b = row[u], e = row[u + 1];
-    const int nc = cbase[j + 1] - cbase[j];
-    for (int k = threadIdx.x; k < nc; k += blockDim.x)
-      bch[cbase[j] + k] = make_int4(u, 0, b + k * kChunk, min(e, b + (k + 1) * kChunk));
+    const int u = hcls[j];
+    int at = cbase[j];
+    for (int k = 0; k < 2; ++k) {
+      const int* o = k ? o2 : o1;
+      if (!o) break;
+      const int b = o[u], e = o[u + 1];
+      const int nc = (e - b + kChunk - 1) / kChunk;
+      for (int q = threadIdx.x; q < nc; q += blockDim.x)
+        bch[at + q] = make_int4(u, k, b + q * kChunk, min(e, b + (q + 1) * kChunk));
+      at += nc;
+    }
+  }
+}
+
+// RCSR forward arcs in input order, and the tail of every input arc
+__global__ void db_rcsr_fwd(const int* off, const int* dst, const int* cap, int n, long long m, int2* farc,
+                            int* fcap, int* fcb, int* tail) {
+  const int lane = threadIdx.x & 31;
+  FOR_TILES(m) {
+    const TileRows tr = tile_rows(off, n, base, m);
+#pragma unroll 4
+    for (int k = 0; k < kTile / 32; ++k) {
+      const long long i = base + k * 32 + lane;
+      if (i >= m) break;
+      const int c = cap ? cap[i] : 1;
+      farc[i] = make_int2(dst[i], c);
+      fcap[i] = c;
+      fcb[i] = 0;
+      tail[i] = row_search(off, i, tr.lo, tr.hi);
+    }
+  }
+}
+// RCSR reverse entries: position p of the arcs stably sorted by head holds
+// {tail, forward arc id} (the reference's rdestinations / flow_index)
+__global__ void db_rcsr_rev(const int* sval, const int* tail, long long m, int2* rarc) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < m; p += (long long)gridDim.x * blockDim.x) {
+    const int i = sval[p];
+    rarc[p] = make_int2(__ldg(tail + i), i);
   }
 }
 
@@ -580,16 +622,28 @@ wbpr_status device_scan(int* data, long long count, cudaStream_t st) {
   return r;
 }
 
-// Fills g->row/arc/arx/ioff/cls/bch/hown/hsum/hmin and the class counts.
-wbpr_status build_bcsr_device(wbpr_graph* g, const wbpr_csr* in) {
+// Builds the residual graph of g->layout in HBM from the input CSR:
+// BCSR row/arc/arx or RCSR frow/farc/fcb/fcap/rrow/rarc, plus ioff, the
+// length classes cls, the heavy-row chunks bch, hown/hsum/hmin and counts.
+wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   const int n = g->n;
   const long long m = g->m;
   cudaStream_t st = g->stream;
   const int blocks = g->sms * 8;
+  const bool bcsr = g->layout == WBPR_LAYOUT_BCSR;
   wbpr_status rs;
-  if ((rs = dalloc(g, &g->row, (size_t)n + 1))) return rs;
-  if ((rs = dalloc(g, &g->arc, (size_t)(2 * m)))) return rs;
-  if ((rs = dalloc(g, &g->arx, (size_t)(2 * m)))) return rs;
+  if (bcsr) {
+    if ((rs = dalloc(g, &g->row, (size_t)n + 1))) return rs;
+    if ((rs = dalloc(g, &g->arc, (size_t)(2 * m)))) return rs;
+    if ((rs = dalloc(g, &g->arx, (size_t)(2 * m)))) return rs;
+  } else {
+    if ((rs = dalloc(g, &g->frow, (size_t)n + 1))) return rs;
+    if ((rs = dalloc(g, &g->farc, (size_t)m))) return rs;
+    if ((rs = dalloc(g, &g->fcb, (size_t)m))) return rs;
+    if ((rs = dalloc(g, &g->fcap, (size_t)m))) return rs;
+    if ((rs = dalloc(g, &g->rrow, (size_t)n + 1))) return rs;
+    if ((rs = dalloc(g, &g->rarc, (size_t)m))) return rs;
+  }
   if ((rs = dalloc(g, &g->ioff, (size_t)n + 1))) return rs;
   std::vector<void*> tmp;
   auto cleanup = [&]() {
@@ -655,8 +709,13 @@ wbpr_status build_bcsr_device(wbpr_graph* g, const wbpr_csr* in) {
     return WBPR_ERR_OVERFLOW;
   }
   DBS(device_scan(inoff, (long long)n + 1, st));
-  db_row<<<blocks, 256, 0, st>>>(g->ioff, inoff, n, g->row);
-  DB(cudaGetLastError());
+  if (bcsr) {
+    db_row<<<blocks, 256, 0, st>>>(g->ioff, inoff, n, g->row);
+    DB(cudaGetLastError());
+  } else {
+    DB(cudaMemcpyAsync(g->frow, g->ioff, 4 * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
+    DB(cudaMemcpyAsync(g->rrow, inoff, 4 * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
+  }
   if (m) {
     const int bits = n > 1 ? 32 - __builtin_clz((unsigned)(n - 1)) : 1;
     const int passes = (bits + 7) / 8;
@@ -676,14 +735,22 @@ wbpr_status build_bcsr_device(wbpr_graph* g, const wbpr_csr* in) {
       DB(cudaGetLastError());
       DBS(device_scan(hist, (long long)ntiles * 256, st));
       db_sort_scatter<<<sblocks, 256, 0, st>>>(kin, vin, m, 8 * p, ntiles, hist, kb[p & 1], vb[p & 1],
-                                               p == passes - 1 ? pos_of : nullptr);
+                                               bcsr && p == passes - 1 ? pos_of : nullptr);
       DB(cudaGetLastError());
     }
-    db_fill_fwd<<<blocks, 256, 0, st>>>(g->ioff, inoff, d_dst, d_cap, pos_of, n, m, g->arc, g->arx, uf);
-    db_fill_twin<<<blocks, 256, 0, st>>>(g->ioff, kb[(passes - 1) & 1], vb[(passes - 1) & 1], uf, m, g->arc,
-                                         g->arx);
+    if (bcsr) {
+      db_fill_fwd<<<blocks, 256, 0, st>>>(g->ioff, inoff, d_dst, d_cap, pos_of, n, m, g->arc, g->arx, uf);
+      db_fill_twin<<<blocks, 256, 0, st>>>(g->ioff, kb[(passes - 1) & 1], vb[(passes - 1) & 1], uf, m, g->arc,
+                                           g->arx);
+    } else {
+      int* tail = pos_of;  // free in this layout
+      db_rcsr_fwd<<<blocks, 256, 0, st>>>(g->ioff, d_dst, d_cap, n, m, g->farc, g->fcap, g->fcb, tail);
+      db_rcsr_rev<<<blocks, 256, 0, st>>>(vb[(passes - 1) & 1], tail, m, g->rarc);
+    }
     DB(cudaGetLastError());
   }
+  const int* o1 = bcsr ? g->row : g->frow;
+  const int* o2 = bcsr ? nullptr : g->rrow;
   // length classes in vertex order, by three stable compactions
   int* fl[3] = {vb[0], vb[1], kb[0]};  // free once the fill kernels have run (stream order)
   if ((size_t)m < (size_t)n + 1) {
@@ -695,7 +762,7 @@ wbpr_status build_bcsr_device(wbpr_graph* g, const wbpr_csr* in) {
       return WBPR_ERR_CUDA;
     }
   }
-  db_classify<<<blocks, 256, 0, st>>>(g->row, n, fl[0], fl[1], fl[2], cnt);
+  db_classify<<<blocks, 256, 0, st>>>(o1, o2, n, fl[0], fl[1], fl[2], cnt);
   DB(cudaGetLastError());
   for (int k = 0; k < 3; ++k) DBS(device_scan(fl[k], (long long)n + 1, st));
   int tot[3];
@@ -711,7 +778,7 @@ wbpr_status build_bcsr_device(wbpr_graph* g, const wbpr_csr* in) {
   g->total_deg = 2 * m;
   g->avg_deg = (double)g->total_deg / std::max<int64_t>(1, g->n_light + g->n_medium + g->n_heavy);
   DBS(dalloc(g, &g->cls, (size_t)(tot[0] + tot[1] + tot[2])));
-  db_cls_scatter<<<blocks, 256, 0, st>>>(g->row, n, fl[0], fl[1], fl[2], g->cls);
+  db_cls_scatter<<<blocks, 256, 0, st>>>(o1, o2, n, fl[0], fl[1], fl[2], g->cls);
   DB(cudaGetLastError());
   // static kChunk pieces of the heavy rows, in vertex order
   const int nh = tot[2];
@@ -726,7 +793,7 @@ wbpr_status build_bcsr_device(wbpr_graph* g, const wbpr_csr* in) {
     }
   }
   const int* hcls = g->cls + tot[0] + tot[1];
-  db_heavy_chunks<<<blocks, 256, 0, st>>>(g->row, hcls, nh, cbase);
+  db_heavy_chunks<<<blocks, 256, 0, st>>>(o1, o2, hcls, nh, cbase);
   DB(cudaGetLastError());
   DBS(device_scan(cbase, (long long)nh + 1, st));
   int nbch = 0;
@@ -734,7 +801,7 @@ wbpr_status build_bcsr_device(wbpr_graph* g, const wbpr_csr* in) {
   DB(cudaStreamSynchronize(st));
   g->n_bch = nbch;
   DBS(dalloc(g, &g->bch, (size_t)nbch));
-  if (nh) db_bch_fill<<<std::min(nh, blocks), 128, 0, st>>>(g->row, hcls, nh, cbase, g->bch);
+  if (nh) db_bch_fill<<<std::min(nh, blocks), 128, 0, st>>>(o1, o2, hcls, nh, cbase, g->bch);
   DB(cudaGetLastError());
   const size_t max_chunks = (size_t)hc[2] + 1;
   DBS(dalloc(g, &g->hown, max_chunks));
@@ -757,9 +824,7 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   if (layout != WBPR_LAYOUT_RCSR && layout != WBPR_LAYOUT_BCSR && layout != WBPR_LAYOUT_BCSR2)
     return WBPR_ERR_INVALID_ARG;
   if (2 * in->num_edges > std::numeric_limits<int32_t>::max()) return WBPR_ERR_OVERFLOW;
-  // BCSR checks incoming-capacity overflow on the device while it builds
-  if (layout == WBPR_LAYOUT_RCSR && wbpr::max_in_capacity(in) > std::numeric_limits<int32_t>::max())
-    return WBPR_ERR_OVERFLOW;
+  // incoming-capacity overflow is checked on the device while it builds
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();
@@ -796,92 +861,7 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   TRYC(cudaEventCreate(&g->ev2));
   TRYC(cudaEventCreate(&g->ev3));
   const int n = g->n;
-  const int64_t m = g->m;
-  std::vector<int32_t> deg((size_t)n);
-  std::vector<int32_t> row_host, rrow_host;
-  if (g->layout == WBPR_LAYOUT_BCSR) {
-    TRY(build_bcsr_device(g, in));
-  } else {
-    wbpr::Rcsr r;
-    TRY(wbpr::build_rcsr_dev(in, &r));
-    TRY(dalloc(g, &g->frow, (size_t)n + 1));
-    TRY(dalloc(g, &g->farc, (size_t)m));
-    TRY(dalloc(g, &g->fcb, (size_t)m));
-    TRY(dalloc(g, &g->fcap, (size_t)m));
-    TRY(dalloc(g, &g->rrow, (size_t)n + 1));
-    TRY(dalloc(g, &g->rarc, (size_t)m));
-    TRYC(cudaMemcpy(g->frow, r.frow.data(), 4 * ((size_t)n + 1), cudaMemcpyHostToDevice));
-    TRYC(cudaMemcpy(g->rrow, r.rrow.data(), 4 * ((size_t)n + 1), cudaMemcpyHostToDevice));
-    if (m) {
-      TRYC(cudaMemcpy(g->farc, r.farc.data(), 8 * (size_t)m, cudaMemcpyHostToDevice));
-      TRYC(cudaMemcpy(g->fcap, r.fcap.data(), 4 * (size_t)m, cudaMemcpyHostToDevice));
-      TRYC(cudaMemcpy(g->rarc, r.rarc.data(), 8 * (size_t)m, cudaMemcpyHostToDevice));
-      TRYC(cudaMemset(g->fcb, 0, 4 * (size_t)m));
-    }
-    for (int u = 0; u < n; ++u) deg[u] = (r.frow[u + 1] - r.frow[u]) + (r.rrow[u + 1] - r.rrow[u]);
-    rrow_host.swap(r.rrow);
-  }
-  if (g->layout == WBPR_LAYOUT_RCSR) {
-  TRY(dalloc(g, &g->ioff, (size_t)n + 1));
-  TRYC(cudaMemcpy(g->ioff, in->offsets, 4 * ((size_t)n + 1), cudaMemcpyHostToDevice));
-  // length classes for the BFS (isolated vertices are left out)
-  std::vector<int32_t> cls;
-  cls.reserve((size_t)n);
-  for (int pass = 0; pass < 3; ++pass)
-    for (int u = 0; u < n; ++u) {
-      const int d = deg[u];
-      if (d == 0) continue;
-      const int c = d <= kLightDeg ? 0 : (d <= kHeavyDeg ? 1 : 2);
-      if (c == pass) cls.push_back(u);
-    }
-  for (int u = 0; u < n; ++u) {
-    const int d = deg[u];
-    g->total_deg += d;
-    if (d == 0) continue;
-    if (d <= kLightDeg) ++g->n_light;
-    else if (d <= kHeavyDeg) ++g->n_medium;
-    else ++g->n_heavy;
-  }
-  g->avg_deg = n ? (double)g->total_deg / std::max<int64_t>(1, g->n_light + g->n_medium + g->n_heavy) : 0;
-  TRY(dalloc(g, &g->cls, cls.size()));
-  if (!cls.empty()) TRYC(cudaMemcpy(g->cls, cls.data(), 4 * cls.size(), cudaMemcpyHostToDevice));
-  // static chunks of the long rows for the bottom-up BFS, and the bound on
-  // the chunk items of the push phase (every row cut into kChunk pieces)
-  {
-    std::vector<int4> bch;
-    int64_t max_chunks = 1;
-    std::vector<int32_t> seg_b(2), seg_e(2);
-    for (int u = 0; u < n; ++u) {
-      const int d = deg[u];
-      max_chunks += (d + kChunk - 1) / kChunk;
-      if (d > kTdHeavy) {
-        ++g->n_td_heavy;
-        g->n_td_items += (d + kTdChunk - 1) / kTdChunk;
-      }
-      if (d <= kHeavyDeg) continue;
-      int nseg = 1;
-      if (g->layout == WBPR_LAYOUT_BCSR) {
-        seg_b[0] = row_host[u];
-        seg_e[0] = row_host[u] + d;
-      } else {
-        nseg = 2;
-        seg_b[0] = in->offsets[u];
-        seg_e[0] = in->offsets[u + 1];
-        seg_b[1] = rrow_host[u];
-        seg_e[1] = rrow_host[u + 1];
-      }
-      for (int k = 0; k < nseg; ++k)
-        for (int b = seg_b[k]; b < seg_e[k]; b += kChunk)
-          bch.push_back(make_int4(u, k, b, std::min(seg_e[k], b + kChunk)));
-    }
-    g->n_bch = (int)bch.size();
-    TRY(dalloc(g, &g->bch, bch.size()));
-    if (!bch.empty()) TRYC(cudaMemcpy(g->bch, bch.data(), sizeof(int4) * bch.size(), cudaMemcpyHostToDevice));
-    TRY(dalloc(g, &g->hown, (size_t)max_chunks));
-    TRY(dalloc(g, &g->hsum, (size_t)max_chunks));
-    TRY(dalloc(g, &g->hmin, (size_t)max_chunks));
-  }
-  }  // RCSR host classification
+  TRY(build_device(g, in));
   int** vec[] = {&g->h, &g->e, &g->rl_min, &g->rl_left, &g->lq[0], &g->lq[1], &g->hq[0], &g->hq[1],
                  &g->esnap, &g->dq, &g->dbase, &g->dE, &g->derem, &g->dmin0,
                  &g->qraw, &g->fr[0], &g->fr[1], &g->fr[2], &g->vlab};
@@ -1120,6 +1100,24 @@ wbpr_status wbpr_graph_destroy(wbpr_graph* g) {
 
 int64_t wbpr_graph_device_bytes(const wbpr_graph* g) { return g ? g->bytes : 0; }
 
+wbpr_status wbpr_graph_read_rcsr(const wbpr_graph* g, int32_t* roffsets, int32_t* rdestinations,
+                                 int32_t* flow_index) {
+  if (!g || g->layout != WBPR_LAYOUT_RCSR) return WBPR_ERR_INVALID_ARG;
+  CK(cudaSetDevice(g->device));
+  CK(cudaStreamSynchronize(g->stream));
+  if (roffsets) CK(cudaMemcpy(roffsets, g->rrow, 4 * ((size_t)g->n + 1), cudaMemcpyDeviceToHost));
+  const size_t m = (size_t)g->m;
+  if (m && (rdestinations || flow_index)) {
+    std::vector<int2> r(m);
+    CK(cudaMemcpy(r.data(), g->rarc, 8 * m, cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < m; ++k) {
+      if (rdestinations) rdestinations[k] = r[k].x;
+      if (flow_index) flow_index[k] = r[k].y;
+    }
+  }
+  return WBPR_OK;
+}
+
 wbpr_status wbpr_graph_read_bcsr(const wbpr_graph* g, int32_t* offsets, int32_t* destinations,
                                  int32_t* capacities, int32_t* backward_idx) {
   if (!g || g->layout != WBPR_LAYOUT_BCSR) return WBPR_ERR_INVALID_ARG;
@@ -1295,6 +1293,53 @@ wbpr_status wbpr_verify(wbpr_graph* g, wbpr_verify_report* rep) {
   return WBPR_OK;
 }
 
+}  // extern "C"
+
+// Phase 2: return the excess stranded at vertices that cannot reach t to s
+// (s absorbs, t is excluded), so the residual graph is that of a maximum flow.
+static wbpr_status return_stranded(wbpr_graph* g) {
+  RunCfg rc;
+  wbpr_status st = make_cfg(g, g->t, g->s, WBPR_ALGO_VC, nullptr, &rc);
+  if (st) return st;
+  rc.mode = kModeState;
+  rc.bfs_excl = g->t;
+  Stats hs;
+  return run(g, rc, &hs);
+}
+
+extern "C" {
+
+wbpr_status wbpr_complete_flow(wbpr_graph* g, float* ms) {
+  if (!g || g->s < 0 || g->t < 0) return WBPR_ERR_INVALID_ARG;
+  CK(cudaSetDevice(g->device));
+  CK(cudaEventRecord(g->ev0, g->stream));
+  wbpr_status st = return_stranded(g);
+  if (st) return st;
+  CK(cudaEventRecord(g->ev1, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  if (ms) CK(cudaEventElapsedTime(ms, g->ev0, g->ev1));
+  return WBPR_OK;
+}
+
+wbpr_status wbpr_cut_sides(wbpr_graph* g, int32_t side, int8_t* in_set) {
+  if (!g || !in_set || (side != 0 && side != 1) || g->s < 0 || g->t < 0) return WBPR_ERR_INVALID_ARG;
+  CK(cudaSetDevice(g->device));
+  wbpr_status st;
+  if (side == 0) {
+    st = bfs_labels(g, g->t, 0, -1);
+  } else {
+    st = return_stranded(g);
+    if (st) return st;
+    st = bfs_labels(g, g->s, 1, -1);
+  }
+  if (st) return st;
+  std::vector<int32_t> lab((size_t)g->n);
+  CK(cudaMemcpyAsync(lab.data(), g->vlab, 4 * (size_t)g->n, cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  for (int32_t v = 0; v < g->n; ++v) in_set[v] = lab[(size_t)v] < g->n ? 1 : 0;
+  return WBPR_OK;
+}
+
 wbpr_status wbpr_mincut_adjoint(wbpr_graph* g, int32_t side, int8_t* indicator, float* adjoint_ms) {
   if (!g || !indicator || (side != 0 && side != 1)) return WBPR_ERR_INVALID_ARG;
   if (g->s < 0 || g->t < 0) return WBPR_ERR_INVALID_ARG;
@@ -1308,15 +1353,7 @@ wbpr_status wbpr_mincut_adjoint(wbpr_graph* g, int32_t side, int8_t* indicator, 
   if (side == 0) {
     st = bfs_labels(g, g->t, 0, -1);
   } else {
-    // return the stranded excess to s (phase 2: s absorbs, t is excluded),
-    // so the residual graph is that of a maximum flow, then BFS from s
-    RunCfg rc;
-    st = make_cfg(g, g->t, g->s, WBPR_ALGO_VC, nullptr, &rc);
-    if (st) return st;
-    rc.mode = kModeState;
-    rc.bfs_excl = g->t;
-    Stats hs;
-    st = run(g, rc, &hs);
+    st = return_stranded(g);
     if (st) return st;
     st = bfs_labels(g, g->s, 1, -1);
   }

@@ -11,6 +11,7 @@
 #include <cstring>
 #include <limits>
 #include <new>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -212,17 +213,43 @@ wbpr_status triples_to_csr(int32_t n, const std::vector<int32_t>& us,
 }
 }  // namespace
 
+// Split [b, e) into up to T pieces that start at line starts.
+static std::vector<const char*> line_splits(const char* b, const char* e, int T) {
+  std::vector<const char*> cut{b};
+  const size_t len = (size_t)(e - b);
+  for (int k = 1; k < T; ++k) {
+    const char* q = b + len * k / T;
+    if (q <= cut.back()) continue;
+    while (q < e && q[-1] != '\n') ++q;
+    if (q > cut.back() && q < e) cut.push_back(q);
+  }
+  cut.push_back(e);
+  return cut;
+}
+
 // -v 2 : DIMACS max-flow (reference graph.cpp:151-214).  1-based ids are
-// shifted to 0-based; "n ID s" / "n ID t" set the terminals; arcs keep file
-// order inside each tail row.
+// shifted to 0-based; "n ID s" / "n ID t" set the terminals (the last one of
+// each kind counts); arcs keep file order inside each tail row.  The header
+// ("c", "p", "n" lines up to the first arc) is read in order; the arc lines
+// are parsed by all host threads, each over a piece of the file that starts
+// at a line start, and joined in file order.
 wbpr_status read_dimacs(const char* path, Csr* c) {
   std::string buf;
   if (!slurp(path, &buf)) return WBPR_ERR_IO;
   Lines L{buf.data(), buf.data() + buf.size()};
   const char *b, *e;
   int64_t n = -1, mdecl = -1;
-  std::vector<int32_t> us, vs, cs;
   int32_t s = -1, t = -1;
+  auto parse_n = [&](const char* p, const char* e2, int32_t* ss, int32_t* tt) {
+    int64_t id;
+    const char *wb, *we;
+    if (n < 0 || !parse_int(&p, e2, &id) || !parse_word(&p, e2, &wb, &we)) return false;
+    if (id < 1 || id > n) return false;
+    if (*wb == 's') *ss = (int32_t)(id - 1);
+    else if (*wb == 't') *tt = (int32_t)(id - 1);
+    return true;
+  };
+  const char* arcs_from = buf.data() + buf.size();
   while (L.next(&b, &e)) {
     const char* p = b;
     while (p < e && (*p == ' ' || *p == '\t')) ++p;
@@ -232,33 +259,87 @@ wbpr_status read_dimacs(const char* path, Csr* c) {
       const char *wb, *we;
       if (!parse_word(&p, e, &wb, &we)) return WBPR_ERR_IO;
       if (!parse_int(&p, e, &n) || !parse_int(&p, e, &mdecl)) return WBPR_ERR_IO;
-      if (n <= 0 || n > std::numeric_limits<int32_t>::max() - 2 || mdecl < 0)
-        return WBPR_ERR_IO;
-      us.reserve((size_t)mdecl);
-      vs.reserve((size_t)mdecl);
-      cs.reserve((size_t)mdecl);
+      if (n <= 0 || n > std::numeric_limits<int32_t>::max() - 2 || mdecl < 0) return WBPR_ERR_IO;
     } else if (kind == 'n') {
-      int64_t id;
-      const char *wb, *we;
-      if (n < 0 || !parse_int(&p, e, &id) || !parse_word(&p, e, &wb, &we)) return WBPR_ERR_IO;
-      if (id < 1 || id > n) return WBPR_ERR_IO;
-      if (*wb == 's') s = (int32_t)(id - 1);
-      else if (*wb == 't') t = (int32_t)(id - 1);
+      if (!parse_n(p, e, &s, &t)) return WBPR_ERR_IO;
     } else if (kind == 'a') {
-      int64_t u, v, cap;
-      if (n < 0 || !parse_int(&p, e, &u) || !parse_int(&p, e, &v) || !parse_int(&p, e, &cap))
-        return WBPR_ERR_IO;
-      if (u < 1 || u > n || v < 1 || v > n || cap < 0 || cap > std::numeric_limits<int32_t>::max())
-        return WBPR_ERR_IO;
-      us.push_back((int32_t)(u - 1));
-      vs.push_back((int32_t)(v - 1));
-      cs.push_back((int32_t)cap);
+      if (n < 0) return WBPR_ERR_IO;
+      arcs_from = b;
+      break;
     } else {
       return WBPR_ERR_IO;
     }
   }
   if (n < 0) return WBPR_ERR_IO;
-  if ((int64_t)us.size() > std::numeric_limits<int32_t>::max()) return WBPR_ERR_OVERFLOW;
+  const std::vector<const char*> cut = line_splits(arcs_from, buf.data() + buf.size(), host_threads());
+  const int P = (int)cut.size() - 1;
+  struct Piece {
+    std::vector<int32_t> us, vs, cs;
+    int32_t s = -1, t = -1;
+    bool bad = false;
+  };
+  std::vector<Piece> pc((size_t)std::max(P, 0));
+  auto work = [&](int k) {
+    Piece& q = pc[(size_t)k];
+    const size_t guess = (size_t)((cut[k + 1] - cut[k]) / 12 + 16);
+    q.us.reserve(guess);
+    q.vs.reserve(guess);
+    q.cs.reserve(guess);
+    Lines LL{cut[k], cut[k + 1]};
+    const char *lb, *le;
+    while (LL.next(&lb, &le)) {
+      const char* p = lb;
+      while (p < le && (*p == ' ' || *p == '\t')) ++p;
+      if (p >= le || *p == 'c') continue;
+      const char kind = *p++;
+      if (kind == 'a') {
+        int64_t u, v, cap;
+        if (!parse_int(&p, le, &u) || !parse_int(&p, le, &v) || !parse_int(&p, le, &cap) || u < 1 || u > n ||
+            v < 1 || v > n || cap < 0 || cap > std::numeric_limits<int32_t>::max()) {
+          q.bad = true;
+          return;
+        }
+        q.us.push_back((int32_t)(u - 1));
+        q.vs.push_back((int32_t)(v - 1));
+        q.cs.push_back((int32_t)cap);
+      } else if (kind == 'n') {
+        if (!parse_n(p, le, &q.s, &q.t)) {
+          q.bad = true;
+          return;
+        }
+      } else {
+        q.bad = true;  // a second problem line or an unknown line kind
+        return;
+      }
+    }
+  };
+  try {
+    std::vector<std::thread> th;
+    for (int k = 1; k < P; ++k) th.emplace_back(work, k);
+    if (P > 0) work(0);
+    for (auto& x : th) x.join();
+  } catch (const std::system_error&) {
+    return WBPR_ERR_IO;
+  }
+  size_t total = 0;
+  for (const Piece& q : pc) {
+    if (q.bad) return WBPR_ERR_IO;
+    total += q.us.size();
+    if (q.s >= 0) s = q.s;
+    if (q.t >= 0) t = q.t;
+  }
+  if (total > (size_t)std::numeric_limits<int32_t>::max()) return WBPR_ERR_OVERFLOW;
+  std::vector<int32_t> us(total), vs(total), cs(total);
+  size_t at = 0;
+  for (Piece& q : pc) {
+    std::copy(q.us.begin(), q.us.end(), us.begin() + at);
+    std::copy(q.vs.begin(), q.vs.end(), vs.begin() + at);
+    std::copy(q.cs.begin(), q.cs.end(), cs.begin() + at);
+    at += q.us.size();
+    std::vector<int32_t>().swap(q.us);
+    std::vector<int32_t>().swap(q.vs);
+    std::vector<int32_t>().swap(q.cs);
+  }
   triples_to_csr((int32_t)n, us, vs, cs, c);
   c->m_declared = mdecl;
   c->s = s;
@@ -339,6 +420,56 @@ wbpr_status read_snap_bin(const char* path, Csr* c) {
   wbpr_csr view{c->n, c->m, c->off.data(), c->dst.data(), c->cap.data(), -1, -1};
   if (check_csr(&view) != WBPR_OK) return WBPR_ERR_IO;
   return WBPR_OK;
+}
+
+// Graph cache (new; the reference's .bin has no capacities and no
+// terminals): "WBPRCSR1", int32 version 1, int32 flags (bit 0: capacities
+// present), int64 n, int64 m, int64 m_declared, int32 s, int32 t, then int32
+// offsets[n+1], destinations[m] and, with bit 0, capacities[m]; little endian.
+constexpr char kCacheMagic[8] = {'W', 'B', 'P', 'R', 'C', 'S', 'R', '1'};
+struct CacheHeader {
+  char magic[8];
+  int32_t version;
+  int32_t flags;
+  int64_t n, m, m_declared;
+  int32_t s, t;
+};
+static_assert(sizeof(CacheHeader) == 48, "cache header layout");
+
+wbpr_status read_graph_cache(const char* path, Csr* c) {
+  std::string buf;
+  if (!slurp(path, &buf)) return WBPR_ERR_IO;
+  CacheHeader h;
+  if (buf.size() < sizeof(h)) return WBPR_ERR_IO;
+  std::memcpy(&h, buf.data(), sizeof(h));
+  if (std::memcmp(h.magic, kCacheMagic, 8) != 0 || h.version != 1) return WBPR_ERR_IO;
+  if (h.n < 1 || h.n > std::numeric_limits<int32_t>::max() - 2 || h.m < 0 ||
+      h.m > std::numeric_limits<int32_t>::max())
+    return WBPR_ERR_IO;
+  const bool caps = h.flags & 1;
+  const size_t need = sizeof(h) + 4 * ((size_t)h.n + 1 + (size_t)h.m * (caps ? 2 : 1));
+  if (buf.size() != need) return WBPR_ERR_IO;
+  c->n = (int32_t)h.n;
+  c->m = h.m;
+  c->m_declared = h.m_declared;
+  c->s = h.s;
+  c->t = h.t;
+  const char* p = buf.data() + sizeof(h);
+  c->off.resize((size_t)h.n + 1);
+  std::memcpy(c->off.data(), p, 4 * ((size_t)h.n + 1));
+  p += 4 * ((size_t)h.n + 1);
+  c->dst.resize((size_t)h.m);
+  std::memcpy(c->dst.data(), p, 4 * (size_t)h.m);
+  p += 4 * (size_t)h.m;
+  if (caps) {
+    c->cap.resize((size_t)h.m);
+    std::memcpy(c->cap.data(), p, 4 * (size_t)h.m);
+  } else {
+    c->cap.assign((size_t)h.m, 1);
+  }
+  if ((c->s < -1 || c->s >= c->n) || (c->t < -1 || c->t >= c->n)) return WBPR_ERR_IO;
+  wbpr_csr view{c->n, c->m, c->off.data(), c->dst.data(), c->cap.data(), c->s, c->t};
+  return check_csr(&view) == WBPR_OK ? WBPR_OK : WBPR_ERR_IO;
 }
 
 // ---------------------------------------------------------------------------
@@ -820,7 +951,89 @@ wbpr_status wbpr_host_csr_copy(const wbpr_csr* in, wbpr_host_csr** out) {
 WBPR_READER(wbpr_read_dimacs, read_dimacs)
 WBPR_READER(wbpr_read_snap_txt, read_snap_txt)
 WBPR_READER(wbpr_read_snap_bin, read_snap_bin)
+WBPR_READER(wbpr_read_graph_cache, read_graph_cache)
 #undef WBPR_READER
+
+wbpr_status wbpr_write_graph_cache(const char* path, const wbpr_csr* g) {
+  wbpr_status st = check_csr(g);
+  if (st) return st;
+  FILE* f = path ? std::fopen(path, "wb") : nullptr;
+  if (!f) return WBPR_ERR_IO;
+  CacheHeader h;
+  std::memcpy(h.magic, kCacheMagic, 8);
+  h.version = 1;
+  h.flags = g->capacities ? 1 : 0;
+  h.n = g->num_nodes;
+  h.m = g->num_edges;
+  h.m_declared = g->num_edges;
+  h.s = g->source;
+  h.t = g->sink;
+  const size_t n1 = (size_t)g->num_nodes + 1, m = (size_t)g->num_edges;
+  bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1;
+  ok = ok && std::fwrite(g->offsets, 4, n1, f) == n1;
+  ok = ok && (m == 0 || std::fwrite(g->destinations, 4, m, f) == m);
+  if (g->capacities) ok = ok && (m == 0 || std::fwrite(g->capacities, 4, m, f) == m);
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? WBPR_OK : WBPR_ERR_IO;
+}
+
+wbpr_status wbpr_write_dimacs_flow(const char* path, const wbpr_csr* g, int64_t flow,
+                                   const int32_t* arc_flow) {
+  wbpr_status st = check_csr(g);
+  if (st) return st;
+  if (g->num_edges > 0 && !arc_flow) return WBPR_ERR_INVALID_ARG;
+  FILE* f = path ? std::fopen(path, "w") : nullptr;
+  if (!f) return WBPR_ERR_IO;
+  std::fprintf(f, "c maximum flow from %d to %d (1-based ids)\n", g->source + 1, g->sink + 1);
+  std::fprintf(f, "s %lld\n", (long long)flow);
+  for (int32_t u = 0; u < g->num_nodes; ++u)
+    for (int32_t i = g->offsets[u]; i < g->offsets[u + 1]; ++i)
+      if (arc_flow[i] > 0) std::fprintf(f, "f %d %d %d\n", u + 1, g->destinations[i] + 1, arc_flow[i]);
+  return std::fclose(f) == 0 ? WBPR_OK : WBPR_ERR_IO;
+}
+
+// Bipartite matching as maximum flow (the paper's super-source /
+// super-sink construction): left vertices 0..L-1, right vertices L..L+R-1,
+// s = L+R, t = L+R+1; s->l and r->t for every vertex, l->r for every listed
+// pair (duplicates kept once); all capacities 1.
+wbpr_status wbpr_bipartite_network(int32_t L, int32_t R, int64_t num_pairs, const int32_t* left,
+                                   const int32_t* right, wbpr_host_csr** out) {
+  if (!out) return WBPR_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (L < 1 || R < 1 || num_pairs < 0 || (num_pairs > 0 && (!left || !right))) return WBPR_ERR_INVALID_ARG;
+  if ((int64_t)L + R + 2 > std::numeric_limits<int32_t>::max() ||
+      (int64_t)L + R + num_pairs > std::numeric_limits<int32_t>::max() / 2)
+    return WBPR_ERR_OVERFLOW;
+  try {
+    std::vector<uint64_t> key((size_t)num_pairs);
+    for (int64_t k = 0; k < num_pairs; ++k) {
+      if (left[k] < 0 || left[k] >= L || right[k] < 0 || right[k] >= R) return WBPR_ERR_INVALID_ARG;
+      key[(size_t)k] = ((uint64_t)(uint32_t)left[k] << 32) | (uint32_t)right[k];
+    }
+    std::sort(key.begin(), key.end());
+    key.erase(std::unique(key.begin(), key.end()), key.end());
+    Csr c;
+    c.n = L + R + 2;
+    c.s = L + R;
+    c.t = L + R + 1;
+    c.off.assign((size_t)c.n + 1, 0);
+    for (uint64_t k : key) c.off[(size_t)(k >> 32) + 1]++;
+    for (int32_t r = 0; r < R; ++r) c.off[(size_t)L + r + 1] = 1;  // r -> t
+    c.off[(size_t)c.s + 1] = L;                                     // s -> every l
+    for (int32_t u = 0; u < c.n; ++u) c.off[u + 1] += c.off[u];
+    c.m = c.off[c.n];
+    c.m_declared = c.m;
+    c.dst.resize((size_t)c.m);
+    size_t at = 0;
+    for (uint64_t k : key) c.dst[at++] = L + (int32_t)(k & 0xffffffffu);
+    for (int32_t r = 0; r < R; ++r) c.dst[at++] = c.t;
+    for (int32_t l = 0; l < L; ++l) c.dst[at++] = l;
+    c.cap.assign((size_t)c.m, 1);
+    return to_host_csr(std::move(c), out);
+  } catch (const std::bad_alloc&) {
+    return WBPR_ERR_OVERFLOW;
+  }
+}
 
 wbpr_status wbpr_write_snap_bin(const char* path, const wbpr_csr* g) {
   wbpr_status st = check_csr(g);

@@ -3,8 +3,13 @@
 // scripts parse ("Total kernel time: X ms" and the maximum-flow line); every
 // device operation goes through the C ABI in wbpr.h.
 //
-//   maxflow [-h] -v {0,1,2} -f file [-s src] [-t sink] [-a {0,1}]
-//           [-l {rcsr,bcsr,bcsr2}] [-V] [-j]
+//   maxflow [-h] -v {0,1,2,3} -f file [-s src] [-t sink] [-a {0,1}]
+//           [-l {rcsr,bcsr,bcsr2}] [-V] [-j] [-o solution] [-c cache]
+//
+// Added beyond the reference: -v 3 reads the library's graph cache (with
+// capacities and terminals), -c writes the loaded graph to that cache, and
+// -o writes the maximum flow as a DIMACS solution ("s" and "f" lines) after
+// returning stranded excess to the source.
 //
 // As in the reference, -f loads the file with the -v given before it, and
 // -s / -t are ignored for DIMACS input (the file names the terminals).
@@ -27,6 +32,7 @@ static void usage(const char* prog) {
   printf("\t\t\t\t0: SNAP txt file (default)\n");
   printf("\t\t\t\t1: SNAP binary file\n");
   printf("\t\t\t\t2: DIMACS file\n");
+  printf("\t\t\t\t3: graph cache written by -c (capacities and terminals kept)\n");
   printf("\t-f filename\tSpecify the file path (binary or txt)\n");
   printf("\t-s source\tSource node\n");
   printf("\t-t sink\t\tSink node\n");
@@ -36,6 +42,8 @@ static void usage(const char* prog) {
   printf("\t-l layout\trcsr (default), bcsr or bcsr2\n");
   printf("\t-V\t\tVerify the result on the device (capacity, conservation, cut)\n");
   printf("\t-j\t\tAlso print one JSON line with the solve statistics\n");
+  printf("\t-o file\t\tWrite the maximum flow as a DIMACS solution (s / f lines)\n");
+  printf("\t-c file\t\tWrite the loaded graph to a cache file for -v 3\n");
 }
 
 // Degree statistics in the reference's format (graph.cpp:618-683).
@@ -67,10 +75,12 @@ static void print_status(const wbpr_host_csr* g) {
 int main(int argc, char** argv) {
   int file_type = 0, algo = 0, source = -1, sink = -1;
   bool verify = false, json = false;
+  const char* out_path = nullptr;
+  const char* cache_path = nullptr;
   wbpr_layout layout = WBPR_LAYOUT_RCSR;
   wbpr_host_csr* g = nullptr;
   int ch;
-  while ((ch = getopt(argc, argv, "hv:f:s:t:a:l:Vj")) != -1) {
+  while ((ch = getopt(argc, argv, "hv:f:s:t:a:l:Vjo:c:")) != -1) {
     switch (ch) {
       case 'h':
         usage(argv[0]);
@@ -94,6 +104,10 @@ int main(int argc, char** argv) {
             printf("Loading from DIMACS file: %s\n", optarg);
             st = wbpr_read_dimacs(optarg, &g);
             break;
+          case 3:
+            printf("Loading from graph cache: %s\n", optarg);
+            st = wbpr_read_graph_cache(optarg, &g);
+            break;
           default:
             printf("Invalid file type\n");
             return 1;
@@ -109,6 +123,12 @@ int main(int argc, char** argv) {
         break;
       case 't':
         if (file_type != 2) sink = atoi(optarg);
+        break;
+      case 'o':
+        out_path = optarg;
+        break;
+      case 'c':
+        cache_path = optarg;
         break;
       case 'a':
         algo = atoi(optarg);
@@ -137,7 +157,8 @@ int main(int argc, char** argv) {
     printf("No input file (-f)\n");
     return 1;
   }
-  if (file_type != 2) {
+  // DIMACS names its terminals; a cache keeps them unless -s / -t are given
+  if (file_type != 2 && !(file_type == 3 && source < 0 && sink < 0)) {
     g->source = source;
     g->sink = sink;
   }
@@ -148,6 +169,15 @@ int main(int argc, char** argv) {
     return 1;
   }
   print_status(g);
+  if (cache_path) {
+    wbpr_csr cv{g->num_nodes, g->num_edges, g->offsets, g->destinations, g->capacities, g->source, g->sink};
+    wbpr_status cs = wbpr_write_graph_cache(cache_path, &cv);
+    if (cs != WBPR_OK) {
+      fprintf(stderr, "Cannot write %s: %s\n", cache_path, wbpr_status_str(cs));
+      wbpr_host_csr_free(g);
+      return 1;
+    }
+  }
   if (algo == 0) printf("Using thread-centric push-relabel algorithm\n");
   else if (algo == 1) printf("Using vertex-centric push-relabel algorithm\n");
   else {
@@ -189,7 +219,19 @@ int main(int argc, char** argv) {
            (unsigned long long)res.pushes, (unsigned long long)res.relabels,
            res.solve_ms > 0 ? (double)g->num_edges / (res.solve_ms * 1e3) : 0.0);
   }
+  int rc = 0;
+  if (out_path) {
+    int32_t* flow = (int32_t*)malloc(sizeof(int32_t) * (g->num_edges > 0 ? (size_t)g->num_edges : 1));
+    st = flow ? wbpr_complete_flow(dg, nullptr) : WBPR_ERR_INVALID_ARG;
+    if (st == WBPR_OK) st = wbpr_read_state(dg, nullptr, nullptr, flow);
+    if (st == WBPR_OK) st = wbpr_write_dimacs_flow(out_path, &view, res.flow, flow);
+    if (st != WBPR_OK) {
+      fprintf(stderr, "Cannot write the solution to %s: %s\n", out_path, wbpr_status_str(st));
+      rc = 1;
+    }
+    free(flow);
+  }
   wbpr_graph_destroy(dg);
   wbpr_host_csr_free(g);
-  return 0;
+  return rc;
 }
