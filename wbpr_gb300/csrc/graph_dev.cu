@@ -405,8 +405,10 @@ __global__ void db_scan_add(int* data, long long count, const int* sums) {
 }
 
 // radix sort by head: one warp tile = kSortRounds x 32 arcs, striped so that
-// (round, lane) order is input order; lanes holding the same digit are found
-// with eight ballots (one per digit bit), which keeps the ranks stable
+// (round, lane) order is input order, so ranks among the lanes holding the
+// same digit keep the sort stable.  The histogram pass finds those lanes with
+// eight ballots (one per digit bit), the scatter pass with match.any (each
+// measured the faster of the two in its kernel on GB300)
 constexpr int kSortRounds = 64;
 constexpr int kSortTile = kSortRounds * 32;
 __device__ __forceinline__ unsigned digit_peers(int d, bool ok) {
@@ -454,7 +456,7 @@ __global__ void __launch_bounds__(256) db_sort_scatter(const int* kin, const int
     const bool ok = i < m;
     const int k = ok ? kin[i] : 0;
     const int d = (k >> shift) & 255;
-    const unsigned peers = digit_peers(d, ok);
+    const unsigned peers = __match_any_sync(0xffffffffu, ok ? d : 256);
     if (ok) {
       const int pos = off[w][d] + __popc(peers & lt);
       const int val = vin ? vin[i] : (int)i;
@@ -645,16 +647,20 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
     if ((rs = dalloc(g, &g->rarc, (size_t)m))) return rs;
   }
   if ((rs = dalloc(g, &g->ioff, (size_t)n + 1))) return rs;
-  std::vector<void*> tmp;
+  // every temporary is carved from one allocation (one cudaMalloc and one
+  // cudaFree per build instead of one per array)
+  char* slab = nullptr;
+  size_t slab_at = 0, slab_size = 0;
   auto cleanup = [&]() {
     cudaStreamSynchronize(st);
-    for (void* p : tmp) cudaFree(p);
-    tmp.clear();
+    if (slab) cudaFree(slab);
+    slab = nullptr;
   };
   auto talloc = [&](size_t bytes) -> void* {
-    void* p = nullptr;
-    if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
-    tmp.push_back(p);
+    bytes = (std::max<size_t>(bytes, 16) + 255) & ~(size_t)255;
+    if (!slab || slab_at + bytes > slab_size) return nullptr;
+    void* p = slab + slab_at;
+    slab_at += bytes;
     return p;
   };
 #define DB(x)                                                         \
@@ -675,16 +681,30 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
     }                   \
   } while (0)
   const int ntiles = (int)((m + kSortTile - 1) / kSortTile);
+  // sort buffers double as the three class-flag arrays, the histogram as the
+  // heavy-row chunk bases: size them for both uses
+  const size_t mv = std::max<size_t>((size_t)m, (size_t)n + 1);
+  const size_t nh_max = std::max<size_t>((size_t)ntiles * 256 + 1, (size_t)n + 1);
+  slab_size = 256 * 16 + 4 * (size_t)m * (in->capacities ? 2 : 1) + 4 * ((size_t)n + 1) +
+              8 * ((size_t)n + 1) + 64 + 16 * mv + 4 * nh_max + 4 * (size_t)m + 8 * (size_t)m;
+  if (cudaMalloc(&slab, slab_size) != cudaSuccess) {
+    cudaGetLastError();
+    slab = nullptr;
+    g_last_error = "device build: out of device memory";
+    return WBPR_ERR_CUDA;
+  }
   int* d_dst = (int*)talloc(4 * (size_t)m);
   int* d_cap = in->capacities ? (int*)talloc(4 * (size_t)m) : nullptr;
   int* inoff = (int*)talloc(4 * ((size_t)n + 1));
   auto* incap = (unsigned long long*)talloc(8 * ((size_t)n + 1));
   auto* cnt = (unsigned long long*)talloc(8 * 8);
-  int* kb[2] = {(int*)talloc(4 * (size_t)m), (int*)talloc(4 * (size_t)m)};
-  int* vb[2] = {(int*)talloc(4 * (size_t)m), (int*)talloc(4 * (size_t)m)};
-  int* hist = (int*)talloc(4 * ((size_t)ntiles * 256 + 1));
+  int* kb[2] = {(int*)talloc(4 * mv), (int*)talloc(4 * mv)};
+  int* vb[2] = {(int*)talloc(4 * mv), (int*)talloc(4 * mv)};
+  int* hist = (int*)talloc(4 * nh_max);
+  int* pos_of = (int*)talloc(4 * (size_t)m);
+  int2* uf = (int2*)talloc(8 * (size_t)m);
   if (!d_dst || (in->capacities && !d_cap) || !inoff || !incap || !cnt || !kb[0] || !kb[1] || !vb[0] || !vb[1] ||
-      !hist) {
+      !hist || !pos_of || !uf) {
     cudaGetLastError();
     g_last_error = "device build: out of device memory";
     cleanup();
@@ -720,14 +740,6 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
     const int bits = n > 1 ? 32 - __builtin_clz((unsigned)(n - 1)) : 1;
     const int passes = (bits + 7) / 8;
     const unsigned sblocks = (unsigned)((ntiles + 7) / 8);
-    int* pos_of = (int*)talloc(4 * (size_t)m);
-    int2* uf = (int2*)talloc(8 * (size_t)m);
-    if (!pos_of || !uf) {
-      cudaGetLastError();
-      g_last_error = "device build: out of device memory";
-      cleanup();
-      return WBPR_ERR_CUDA;
-    }
     for (int p = 0; p < passes; ++p) {
       const int* kin = p ? kb[(p - 1) & 1] : d_dst;
       const int* vin = p ? vb[(p - 1) & 1] : nullptr;
@@ -753,15 +765,6 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   const int* o2 = bcsr ? nullptr : g->rrow;
   // length classes in vertex order, by three stable compactions
   int* fl[3] = {vb[0], vb[1], kb[0]};  // free once the fill kernels have run (stream order)
-  if ((size_t)m < (size_t)n + 1) {
-    for (int k = 0; k < 3; ++k) fl[k] = (int*)talloc(4 * ((size_t)n + 1));
-    if (!fl[0] || !fl[1] || !fl[2]) {
-      cudaGetLastError();
-      g_last_error = "device build: out of device memory";
-      cleanup();
-      return WBPR_ERR_CUDA;
-    }
-  }
   db_classify<<<blocks, 256, 0, st>>>(o1, o2, n, fl[0], fl[1], fl[2], cnt);
   DB(cudaGetLastError());
   for (int k = 0; k < 3; ++k) DBS(device_scan(fl[k], (long long)n + 1, st));
@@ -782,16 +785,7 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   DB(cudaGetLastError());
   // static kChunk pieces of the heavy rows, in vertex order
   const int nh = tot[2];
-  int* cbase = hist;  // reused when it is large enough
-  if ((size_t)nh + 1 > (size_t)ntiles * 256 + 1) {
-    cbase = (int*)talloc(4 * ((size_t)nh + 1));
-    if (!cbase) {
-      cudaGetLastError();
-      g_last_error = "device build: out of device memory";
-      cleanup();
-      return WBPR_ERR_CUDA;
-    }
-  }
+  int* cbase = hist;  // holds at least n + 1 entries
   const int* hcls = g->cls + tot[0] + tot[1];
   db_heavy_chunks<<<blocks, 256, 0, st>>>(o1, o2, hcls, nh, cbase);
   DB(cudaGetLastError());
@@ -865,8 +859,18 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   int** vec[] = {&g->h, &g->e, &g->rl_min, &g->rl_left, &g->lq[0], &g->lq[1], &g->hq[0], &g->hq[1],
                  &g->esnap, &g->dq, &g->dbase, &g->dE, &g->derem, &g->dmin0,
                  &g->qraw, &g->fr[0], &g->fr[1], &g->fr[2], &g->vlab};
-  for (int** p : vec) TRY(dalloc(g, p, (size_t)n));
-  for (int k = 0; k < 3; ++k) TRY(dalloc(g, &g->frh[k], (size_t)g->n_td_items + 1));
+  {
+    // one allocation for the per-vertex scratch, one for the BFS chunk lists
+    const size_t nvec = sizeof(vec) / sizeof(vec[0]);
+    const size_t stride = ((size_t)n + 63) & ~(size_t)63;
+    int* base = nullptr;
+    TRY(dalloc(g, &base, stride * nvec));
+    for (size_t k = 0; k < nvec; ++k) *vec[k] = base + k * stride;
+    const size_t fstride = ((size_t)g->n_td_items + 1 + 31) & ~(size_t)31;
+    int2* fb = nullptr;
+    TRY(dalloc(g, &fb, 3 * fstride));
+    for (int k = 0; k < 3; ++k) g->frh[k] = fb + k * fstride;
+  }
   TRY(dalloc(g, &g->ctl, 1));
   TRY(dalloc(g, &g->st, 1));
   TRYC(cudaMemset(g->h, 0, 4 * (size_t)n));
