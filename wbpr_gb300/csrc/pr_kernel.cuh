@@ -530,6 +530,7 @@ __device__ __forceinline__ void tile_discharge(const Params<Topo>& p, int u, int
 // two passes see the same admissible set.
 constexpr int kItems = 8;
 constexpr int kChunk = 2048;
+constexpr int kFirst = 2048;  // arcs of a long row walked by one warp before it goes deep
 
 // Block-wide inclusive scan of x (saturated at cap); returns the inclusive
 // value of this thread and writes the exclusive one to *excl, the total to
@@ -704,7 +705,7 @@ __device__ __forceinline__ void deep_meta(const Params<Topo>& p, int k, DeepMeta
     s_m.hu = __ldcg(p.lab + s_m.u);
     s_m.j = k - s_m.base;
     s_m.r = vrow(p.g, s_m.u);
-    s_m.nch = (s_m.r.deg - kChunk + kChunk - 1) / kChunk;
+    s_m.nch = (s_m.r.deg - kFirst + kChunk - 1) / kChunk;
   }
   __syncthreads();
   *m = s_m;
@@ -717,7 +718,7 @@ template <class Topo>
 __device__ void deep_pass_a(const Params<Topo>& p, int k, BlockAcc& acc) {
   DeepMeta m;
   deep_meta(p, k, &m);
-  const int lo = (m.j + 1) * kChunk, hi = min(m.r.deg, lo + kChunk);
+  const int lo = kFirst + m.j * kChunk, hi = min(m.r.deg, lo + kChunk);
   const int th = m.hu - 1;
   unsigned long long sum = 0;
   int mn = kBig;
@@ -777,7 +778,7 @@ __device__ void deep_pass_b(const Params<Topo>& p, int k, int* rawcnt, BlockAcc&
   const long long prev = s_prev;
   __syncthreads();
   if (allot > 0) {
-    const int lo = (m.j + 1) * kChunk, hi = min(m.r.deg, lo + kChunk);
+    const int lo = kFirst + m.j * kChunk, hi = min(m.r.deg, lo + kChunk);
     int unused;
     ordered_push(p, m.r, lo, hi, m.hu, allot, &unused, rawcnt, acc);
   }
@@ -807,7 +808,7 @@ __device__ void push_first(const Params<Topo>& p, int cur, int raw, BlockAcc& ac
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int idx = gw; idx < nH;) {
-    tile_discharge<Topo, 32, 4>(p, __ldcg(p.hq[cur] + idx), kChunk, rawcnt, acc);
+    tile_discharge<Topo, 32, 4>(p, __ldcg(p.hq[cur] + idx), kFirst, rawcnt, acc);
     int nx = 0;
     if (lane == 0) nx = nwarps + atomicAdd(&c->heavy_next, 1);
     idx = __shfl_sync(0xffffffffu, nx, 0);
@@ -819,7 +820,7 @@ __device__ void push_first(const Params<Topo>& p, int cur, int raw, BlockAcc& ac
 #pragma unroll 1
     for (int r = 0; r < 2; ++r) {
       const int idx = base + r * kTpw + lane / W;
-      if (idx < nL) tile_discharge<Topo, W, 4>(p, __ldcg(p.lq[cur] + idx), kChunk, rawcnt, acc);
+      if (idx < nL) tile_discharge<Topo, W, 4>(p, __ldcg(p.lq[cur] + idx), kFirst, rawcnt, acc);
     }
     __syncwarp();
     int nx = 0;
