@@ -88,3 +88,20 @@ def test_read_back_matches_the_layout():
         with pytest.raises(W.WbprError) as ei:
             d.read_rcsr()
         assert ei.value.status == 1
+
+
+@pytest.mark.parametrize("layout", ["bcsr", "rcsr"])
+def test_device_build_rejects_invalid_input(layout):
+    # the O(n + m) input checks run on the device while it builds
+    def make(off, dst, cap):
+        return W.Graph(4, np.array(off, np.int32), np.array(dst, np.int32), np.array(cap, np.int32), 0, 3)
+    bad = [make([0, 2, 3, 4, 4], [1, 4, 2, 3], [1, 1, 1, 1]),     # head out of range
+           make([0, 2, 3, 4, 4], [1, 2, 2, 3], [1, -1, 1, 1]),    # negative capacity
+           make([0, 3, 1, 4, 4], [1, 2, 2, 3], [1, 1, 1, 1])]     # offsets decrease
+    for g in bad:
+        with pytest.raises(W.WbprError) as ei:
+            W.DeviceGraph(g, layout)
+        assert ei.value.status == 1
+    ok = make([0, 2, 3, 4, 4], [1, 2, 2, 3], [1, 1, 1, 1])
+    with W.DeviceGraph(ok, layout) as d:
+        assert d.solve("vc", 0, 3).flow == 1

@@ -347,12 +347,25 @@ __global__ void flow_kernel(const int* ioff, const int* row, const int2* arc, co
 // i + inoff[u], and the twin of the arc at position p of the arcs stably
 // sorted by head v is off[v + 1] + p.  The stable sort is an LSD radix sort
 // by head over warp tiles; its last pass also records each arc's position p.
-__global__ void db_count(const int* dst, const int* cap, long long m, int* indeg, unsigned long long* incap) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+// Also validates the input (what the host checks only for its own
+// builders): heads in [0, n), capacities >= 0, non-decreasing offsets.
+__global__ void db_count(const int* off, const int* dst, const int* cap, int n, long long m, int* indeg,
+                         unsigned long long* incap, unsigned long long* bad) {
+  const long long gs = (long long)gridDim.x * blockDim.x;
+  bool b = false;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += gs) {
     const int v = dst[i];
+    const int c = cap ? cap[i] : 1;
+    if (v < 0 || v >= n || c < 0) {
+      b = true;
+      continue;
+    }
     atomicAdd(indeg + v, 1);
-    atomicAdd(incap + v, (unsigned long long)(cap ? cap[i] : 1));
+    atomicAdd(incap + v, (unsigned long long)c);
   }
+  for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < n; u += gs)
+    if (off[u + 1] < off[u]) b = true;
+  if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1ull);
 }
 __global__ void db_max(const unsigned long long* incap, int n, unsigned long long* out) {
   unsigned long long mx = 0;
@@ -404,13 +417,15 @@ __global__ void db_scan_add(int* data, long long count, const int* sums) {
     data[i] += sums[i / kScanTile];
 }
 
-// radix sort by head: one warp tile = kSortRounds x 32 arcs, striped so that
-// (round, lane) order is input order, so ranks among the lanes holding the
-// same digit keep the sort stable.  The histogram pass finds those lanes with
-// eight ballots (one per digit bit), the scatter pass with match.any (each
-// measured the faster of the two in its kernel on GB300)
-constexpr int kSortRounds = 64;
-constexpr int kSortTile = kSortRounds * 32;
+// Radix sort by head, 8-bit digits, stable.  A tile is one block of 8 warps
+// x kSortRounds rounds x 32 arcs; warp w holds arcs [w * 32 * kSortRounds,
+// (w + 1) * 32 * kSortRounds) of the tile, round-major, so (warp, round,
+// lane) order is input order.  Lanes holding the same digit are found with
+// eight ballots (one per digit bit).  The scatter pass first sorts its tile
+// in shared memory (digit, then input order), then writes each digit's run
+// to its global place, so consecutive threads write consecutive slots.
+constexpr int kSortRounds = 16;
+constexpr int kSortTile = 8 * kSortRounds * 32;  // 4096 arcs
 __device__ __forceinline__ unsigned digit_peers(int d, bool ok) {
   unsigned peers = __ballot_sync(0xffffffffu, ok);
 #pragma unroll
@@ -422,51 +437,93 @@ __device__ __forceinline__ unsigned digit_peers(int d, bool ok) {
   return peers;
 }
 __global__ void __launch_bounds__(256) db_sort_hist(const int* key, long long m, int shift, int ntiles, int* hist) {
-  __shared__ int cnt[8][256];
+  __shared__ int cnt[256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int tile = blockIdx.x * 8 + w;
-  for (int b = lane; b < 256; b += 32) cnt[w][b] = 0;
-  __syncwarp();
-  if (tile >= ntiles) return;
-  const long long base = (long long)tile * kSortTile;
+  const int tile = blockIdx.x;
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const long long base = (long long)tile * kSortTile + (long long)w * kSortRounds * 32;
   for (int r = 0; r < kSortRounds; ++r) {
     const long long i = base + r * 32 + lane;
     const bool ok = i < m;
     const int d = ok ? (key[i] >> shift) & 255 : 0;
     const unsigned peers = digit_peers(d, ok);
-    if (ok && lane == __ffs(peers) - 1) cnt[w][d] += __popc(peers);
-    __syncwarp();
+    if (ok && lane == __ffs(peers) - 1) atomicAdd(&cnt[d], __popc(peers));
   }
-  for (int b = lane; b < 256; b += 32) hist[(long long)b * ntiles + tile] = cnt[w][b];
+  __syncthreads();
+  hist[(long long)threadIdx.x * ntiles + tile] = cnt[threadIdx.x];
 }
 // pos_of != nullptr on the last pass: also record each arc's sorted position
 __global__ void __launch_bounds__(256) db_sort_scatter(const int* kin, const int* vin, long long m, int shift,
                                                        int ntiles, const int* hist, int* kout, int* vout,
                                                        int* pos_of) {
-  __shared__ int off[8][256];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int tile = blockIdx.x * 8 + w;
-  if (tile >= ntiles) return;
-  for (int b = lane; b < 256; b += 32) off[w][b] = hist[(long long)b * ntiles + tile];
-  __syncwarp();
+  __shared__ int wc[8][256];     // per-warp digit counts, then each warp's start within its digit
+  __shared__ int dstart[256];    // tile-local start of each digit
+  __shared__ int gofs[256];      // global start of this tile's run of each digit
+  __shared__ int sk[kSortTile], sv[kSortTile];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, t = threadIdx.x;
+  const int tile = blockIdx.x;
   const unsigned lt = (1u << lane) - 1;
-  const long long base = (long long)tile * kSortTile;
+  for (int j = 0; j < 8; ++j) wc[j][t] = 0;
+  gofs[t] = hist[(long long)t * ntiles + tile];
+  __syncthreads();
+  const long long base = (long long)tile * kSortTile + (long long)w * kSortRounds * 32;
+  int key[kSortRounds], val[kSortRounds], rk[kSortRounds];
+#pragma unroll
   for (int r = 0; r < kSortRounds; ++r) {
     const long long i = base + r * 32 + lane;
     const bool ok = i < m;
-    const int k = ok ? kin[i] : 0;
+    key[r] = ok ? kin[i] : -1;
+    val[r] = ok ? (vin ? vin[i] : (int)i) : 0;
+  }
+#pragma unroll
+  for (int r = 0; r < kSortRounds; ++r) {
+    const bool ok = key[r] >= 0;
+    const int d = ok ? (key[r] >> shift) & 255 : 0;
+    const unsigned peers = digit_peers(d, ok);
+    rk[r] = ok ? wc[w][d] + __popc(peers & lt) : 0;
+    __syncwarp();
+    if (ok && lane == __ffs(peers) - 1) wc[w][d] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  // per digit t: each warp's start among the tile's arcs of that digit, and
+  // the digit's total; then the tile-local digit starts by a block scan
+  int tot = 0;
+  for (int j = 0; j < 8; ++j) {
+    const int c = wc[j][t];
+    wc[j][t] = tot;
+    tot += c;
+  }
+  int inc = tot;
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, d);
+    if (lane >= d) inc += y;
+  }
+  __shared__ int ws[8];
+  if (lane == 31) ws[w] = inc;
+  __syncthreads();
+  int wpre = 0;
+  for (int j = 0; j < w; ++j) wpre += ws[j];
+  dstart[t] = wpre + inc - tot;
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kSortRounds; ++r) {
+    if (key[r] < 0) continue;
+    const int d = (key[r] >> shift) & 255;
+    const int lp = dstart[d] + wc[w][d] + rk[r];
+    sk[lp] = key[r];
+    sv[lp] = val[r];
+  }
+  __syncthreads();
+  const int cnt = (int)min((long long)kSortTile, m - (long long)tile * kSortTile);
+  for (int i = t; i < cnt; i += 256) {
+    const int k = sk[i];
     const int d = (k >> shift) & 255;
-    const unsigned peers = __match_any_sync(0xffffffffu, ok ? d : 256);
-    if (ok) {
-      const int pos = off[w][d] + __popc(peers & lt);
-      const int val = vin ? vin[i] : (int)i;
-      kout[pos] = k;
-      vout[pos] = val;
-      if (pos_of) pos_of[val] = pos;
-    }
-    __syncwarp();
-    if (ok && lane == __ffs(peers) - 1) off[w][d] += __popc(peers);
-    __syncwarp();
+    const int pos = gofs[d] + (i - dstart[d]);
+    kout[pos] = k;
+    vout[pos] = sv[i];
+    if (pos_of) pos_of[sv[i]] = pos;
   }
 }
 
@@ -718,12 +775,17 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   DB(cudaMemsetAsync(inoff, 0, 4 * ((size_t)n + 1), st));
   DB(cudaMemsetAsync(incap, 0, 8 * ((size_t)n + 1), st));
   DB(cudaMemsetAsync(cnt, 0, 8 * 8, st));
-  if (m) db_count<<<blocks, 256, 0, st>>>(d_dst, d_cap, m, inoff, incap);
+  db_count<<<blocks, 256, 0, st>>>(g->ioff, d_dst, d_cap, n, m, inoff, incap, cnt + 6);
   db_max<<<blocks, 256, 0, st>>>(incap, n, cnt + 7);
   DB(cudaGetLastError());
-  unsigned long long maxcap = 0;
-  DB(cudaMemcpyAsync(&maxcap, cnt + 7, 8, cudaMemcpyDeviceToHost, st));
+  unsigned long long chk[2] = {0, 0};
+  DB(cudaMemcpyAsync(chk, cnt + 6, 16, cudaMemcpyDeviceToHost, st));
   DB(cudaStreamSynchronize(st));
+  if (chk[0]) {
+    cleanup();
+    return WBPR_ERR_INVALID_ARG;
+  }
+  const unsigned long long maxcap = chk[1];
   if (maxcap > 0x7fffffffull) {
     cleanup();
     return WBPR_ERR_OVERFLOW;
@@ -739,7 +801,7 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   if (m) {
     const int bits = n > 1 ? 32 - __builtin_clz((unsigned)(n - 1)) : 1;
     const int passes = (bits + 7) / 8;
-    const unsigned sblocks = (unsigned)((ntiles + 7) / 8);
+    const unsigned sblocks = (unsigned)ntiles;
     for (int p = 0; p < passes; ++p) {
       const int* kin = p ? kb[(p - 1) & 1] : d_dst;
       const int* vin = p ? vb[(p - 1) & 1] : nullptr;
@@ -812,7 +874,8 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
 wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out) {
   if (!out) return WBPR_ERR_INVALID_ARG;
   *out = nullptr;
-  wbpr_status st = wbpr::check_csr(in);
+  // the O(n + m) validation runs on the device while it builds
+  wbpr_status st = wbpr::check_csr_shape(in);
   if (st) return st;
   if (in->num_nodes < 2) return WBPR_ERR_INVALID_ARG;
   if (layout != WBPR_LAYOUT_RCSR && layout != WBPR_LAYOUT_BCSR && layout != WBPR_LAYOUT_BCSR2)

@@ -74,6 +74,19 @@ struct Stream {
 };
 
 // ---------------------------------------------------------------------------
+wbpr_status check_csr_shape(const wbpr_csr* g) {
+  if (!g || g->num_nodes < 0 || g->num_edges < 0) return WBPR_ERR_INVALID_ARG;
+  if (g->num_nodes > 0 && (!g->offsets)) return WBPR_ERR_INVALID_ARG;
+  if (g->num_edges > 0 && !g->destinations) return WBPR_ERR_INVALID_ARG;
+  if (g->num_edges > (int64_t)std::numeric_limits<int32_t>::max())
+    return WBPR_ERR_OVERFLOW;
+  const int32_t n = g->num_nodes;
+  if (n == 0) return g->num_edges == 0 ? WBPR_OK : WBPR_ERR_INVALID_ARG;
+  if (g->offsets[0] != 0 || (int64_t)g->offsets[n] != g->num_edges)
+    return WBPR_ERR_INVALID_ARG;
+  return WBPR_OK;
+}
+
 wbpr_status check_csr(const wbpr_csr* g) {
   if (!g || g->num_nodes < 0 || g->num_edges < 0) return WBPR_ERR_INVALID_ARG;
   if (g->num_nodes > 0 && (!g->offsets)) return WBPR_ERR_INVALID_ARG;

@@ -24,6 +24,9 @@ struct Csr {
 
 // Validate a caller CSR: monotone offsets, ids in range, capacities >= 0.
 wbpr_status check_csr(const wbpr_csr* g);
+// Only the O(1) part: pointers, sizes, offsets[0] == 0, offsets[n] == m (the
+// device build checks the rest while it reads the arrays).
+wbpr_status check_csr_shape(const wbpr_csr* g);
 
 // Convert between the C view and the owned form.
 wbpr_status to_host_csr(Csr&& c, wbpr_host_csr** out);
