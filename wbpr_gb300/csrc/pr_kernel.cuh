@@ -836,9 +836,12 @@ __device__ void push_deep(const Params<Topo>& p, int pass, int nD, int raw, Bloc
   int* ctr = pass == 0 ? &c->deep_next_a : &c->deep_next_b;
   __shared__ int s_item;
   for (int it = blockIdx.x; it < nD;) {
+    // claim the next item now, so the atomic's latency hides behind this one
+    int nx = 0;
+    if (threadIdx.x == 0) nx = (int)gridDim.x + atomicAdd(ctr, 1);
     if (pass == 0) deep_pass_a<Topo>(p, it, acc);
     else deep_pass_b<Topo>(p, it, rawcnt, acc);
-    if (threadIdx.x == 0) s_item = (int)gridDim.x + atomicAdd(ctr, 1);
+    if (threadIdx.x == 0) s_item = nx;
     __syncthreads();
     it = s_item;
     __syncthreads();
