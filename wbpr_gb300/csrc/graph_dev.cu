@@ -347,24 +347,36 @@ __global__ void flow_kernel(const int* ioff, const int* row, const int2* arc, co
 // i + inoff[u], and the twin of the arc at position p of the arcs stably
 // sorted by head v is off[v + 1] + p.  The stable sort is an LSD radix sort
 // by head over warp tiles; its last pass also records each arc's position p.
-// Also validates the input (what the host checks only for its own
-// builders): heads in [0, n), capacities >= 0, non-decreasing offsets.
-__global__ void db_count(const int* off, const int* dst, const int* cap, int n, long long m, int* indeg,
-                         unsigned long long* incap, unsigned long long* bad) {
+// In-degrees, validating heads and offsets on the way (what the host checks
+// only for its own builders): heads in [0, n), non-decreasing offsets.
+__global__ void db_count(const int* off, const int* dst, int n, long long m, int* indeg, unsigned long long* bad) {
+  const long long gs = (long long)gridDim.x * blockDim.x;
+  bool b = false;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += gs) {
+    const int v = dst[i];
+    if (v < 0 || v >= n) {
+      b = true;
+      continue;
+    }
+    atomicAdd(indeg + v, 1);
+  }
+  for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < n; u += gs)
+    if (off[u + 1] < off[u]) b = true;
+  if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1ull);
+}
+// Incoming capacity per vertex (its excess can never exceed it); capacities
+// must be >= 0.  Arcs with invalid heads were flagged by db_count.
+__global__ void db_count_cap(const int* dst, const int* cap, int n, long long m, unsigned long long* incap,
+                             unsigned long long* bad) {
   const long long gs = (long long)gridDim.x * blockDim.x;
   bool b = false;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += gs) {
     const int v = dst[i];
     const int c = cap ? cap[i] : 1;
-    if (v < 0 || v >= n || c < 0) {
-      b = true;
-      continue;
-    }
-    atomicAdd(indeg + v, 1);
+    if (c < 0) b = true;
+    if (v < 0 || v >= n || c <= 0) continue;
     atomicAdd(incap + v, (unsigned long long)c);
   }
-  for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < n; u += gs)
-    if (off[u + 1] < off[u]) b = true;
   if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1ull);
 }
 __global__ void db_max(const unsigned long long* incap, int n, unsigned long long* out) {
@@ -708,10 +720,17 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   // cudaFree per build instead of one per array)
   char* slab = nullptr;
   size_t slab_at = 0, slab_size = 0;
+  cudaStream_t side = nullptr;
+  cudaEvent_t side_done = nullptr;
   auto cleanup = [&]() {
     cudaStreamSynchronize(st);
+    if (side) cudaStreamSynchronize(side);
     if (slab) cudaFree(slab);
+    if (side_done) cudaEventDestroy(side_done);
+    if (side) cudaStreamDestroy(side);
     slab = nullptr;
+    side = nullptr;
+    side_done = nullptr;
   };
   auto talloc = [&](size_t bytes) -> void* {
     bytes = (std::max<size_t>(bytes, 16) + 255) & ~(size_t)255;
@@ -750,6 +769,12 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
     g_last_error = "device build: out of device memory";
     return WBPR_ERR_CUDA;
   }
+  if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&side_done, cudaEventDisableTiming) != cudaSuccess) {
+    g_last_error = std::string("device build: ") + cudaGetErrorString(cudaGetLastError());
+    cleanup();
+    return WBPR_ERR_CUDA;
+  }
   int* d_dst = (int*)talloc(4 * (size_t)m);
   int* d_cap = in->capacities ? (int*)talloc(4 * (size_t)m) : nullptr;
   int* inoff = (int*)talloc(4 * ((size_t)n + 1));
@@ -767,29 +792,15 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
     cleanup();
     return WBPR_ERR_CUDA;
   }
+  // Heads first: the in-degree count, the row offsets and the sort need only
+  // them, so they run while the capacities are copied on a second stream.
   DB(cudaMemcpyAsync(g->ioff, in->offsets, 4 * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
-  if (m) {
-    DB(cudaMemcpyAsync(d_dst, in->destinations, 4 * (size_t)m, cudaMemcpyHostToDevice, st));
-    if (d_cap) DB(cudaMemcpyAsync(d_cap, in->capacities, 4 * (size_t)m, cudaMemcpyHostToDevice, st));
-  }
+  if (m) DB(cudaMemcpyAsync(d_dst, in->destinations, 4 * (size_t)m, cudaMemcpyHostToDevice, st));
   DB(cudaMemsetAsync(inoff, 0, 4 * ((size_t)n + 1), st));
   DB(cudaMemsetAsync(incap, 0, 8 * ((size_t)n + 1), st));
   DB(cudaMemsetAsync(cnt, 0, 8 * 8, st));
-  db_count<<<blocks, 256, 0, st>>>(g->ioff, d_dst, d_cap, n, m, inoff, incap, cnt + 6);
-  db_max<<<blocks, 256, 0, st>>>(incap, n, cnt + 7);
+  db_count<<<blocks, 256, 0, st>>>(g->ioff, d_dst, n, m, inoff, cnt + 6);
   DB(cudaGetLastError());
-  unsigned long long chk[2] = {0, 0};
-  DB(cudaMemcpyAsync(chk, cnt + 6, 16, cudaMemcpyDeviceToHost, st));
-  DB(cudaStreamSynchronize(st));
-  if (chk[0]) {
-    cleanup();
-    return WBPR_ERR_INVALID_ARG;
-  }
-  const unsigned long long maxcap = chk[1];
-  if (maxcap > 0x7fffffffull) {
-    cleanup();
-    return WBPR_ERR_OVERFLOW;
-  }
   DBS(device_scan(inoff, (long long)n + 1, st));
   if (bcsr) {
     db_row<<<blocks, 256, 0, st>>>(g->ioff, inoff, n, g->row);
@@ -812,6 +823,31 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
                                                bcsr && p == passes - 1 ? pos_of : nullptr);
       DB(cudaGetLastError());
     }
+  }
+  // capacities: copied on the side stream (its host call may block while
+  // the sort above runs), then counted; then every input check is decided
+  if (m && d_cap) {
+    DB(cudaMemcpyAsync(d_cap, in->capacities, 4 * (size_t)m, cudaMemcpyHostToDevice, side));
+    DB(cudaEventRecord(side_done, side));
+    DB(cudaStreamWaitEvent(st, side_done, 0));
+  }
+  db_count_cap<<<blocks, 256, 0, st>>>(d_dst, d_cap, n, m, incap, cnt + 6);
+  db_max<<<blocks, 256, 0, st>>>(incap, n, cnt + 7);
+  DB(cudaGetLastError());
+  unsigned long long chk[2] = {0, 0};
+  DB(cudaMemcpyAsync(chk, cnt + 6, 16, cudaMemcpyDeviceToHost, st));
+  DB(cudaStreamSynchronize(st));
+  if (chk[0]) {
+    cleanup();
+    return WBPR_ERR_INVALID_ARG;
+  }
+  if (chk[1] > 0x7fffffffull) {
+    cleanup();
+    return WBPR_ERR_OVERFLOW;
+  }
+  if (m) {
+    const int bits = n > 1 ? 32 - __builtin_clz((unsigned)(n - 1)) : 1;
+    const int passes = (bits + 7) / 8;
     if (bcsr) {
       db_fill_fwd<<<blocks, 256, 0, st>>>(g->ioff, inoff, d_dst, d_cap, pos_of, n, m, g->arc, g->arx, uf);
       db_fill_twin<<<blocks, 256, 0, st>>>(g->ioff, kb[(passes - 1) & 1], vb[(passes - 1) & 1], uf, m, g->arc,
