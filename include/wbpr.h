@@ -231,6 +231,11 @@ wbpr_status wbpr_graph_create(const wbpr_csr* g, wbpr_layout layout,
 wbpr_status wbpr_graph_destroy(wbpr_graph* g);
 /* Bytes of device memory held by the handle. */
 int64_t wbpr_graph_device_bytes(const wbpr_graph* g);
+/* Queue the handle's device work on the caller's stream (a cudaStream_t of
+ * the handle's device; NULL returns to the handle's own stream).  Work queued
+ * before the switch is finished first.  Calls still return once their
+ * results are on the host. */
+wbpr_status wbpr_graph_set_stream(wbpr_graph* g, void* stream);
 /* Copy a BCSR handle's residual graph, as built on the device, back to host
  * buffers in the format of wbpr_build_bcsr (offsets[n+1], destinations[2m],
  * capacities[2m], backward_idx[2m]; any may be NULL).  The device build is
@@ -267,7 +272,8 @@ wbpr_status wbpr_verify(wbpr_graph* g, wbpr_verify_report* rep);
  * (super)gradient d maxflow / d cap(e).  side 0: sink-side cut (vertices that
  * can reach t form T, g = [u not in T and v in T]); side 1: source-side cut
  * (S = vertices reachable from s once the stranded excess is returned,
- * g = [u in S and v not in S]).  `indicator` is a host buffer of m bytes. */
+ * g = [u in S and v not in S]).  `indicator` is a host or device buffer of
+ * m bytes. */
 wbpr_status wbpr_mincut_adjoint(wbpr_graph* g, int32_t side, int8_t* indicator,
                                 float* adjoint_ms);
 /* Turn the maximum preflow of the last solve into a maximum flow: the excess

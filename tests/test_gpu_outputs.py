@@ -117,3 +117,26 @@ def test_cli_solution_and_cache(tmp_path):
     check_flow(g, f, v)
     r2 = subprocess.run([wb.CLI, "-v", "3", "-f", str(cache), "-a", "0"], capture_output=True, text=True)
     assert r2.returncode == 0 and f"is {v}, {v}" in r2.stdout
+
+
+def test_caller_stream_and_device_indicator():
+    torch = pytest.importorskip("torch")
+    g = W.gen_grid(48, 48, 6)
+    v = oracle.dinic(g.n, g.off, g.dst, g.cap, g.s, g.t)
+    with W.DeviceGraph(g, "bcsr") as d:
+        host0 = None
+        r = d.solve("vc", g.s, g.t)
+        host0, _ = d.mincut_adjoint(0)
+        s = torch.cuda.Stream()
+        d.set_stream(s.cuda_stream)
+        r2 = d.solve("vc", g.s, g.t)
+        assert r.flow == r2.flow == v
+        assert d.verify()["ok"]
+        dev = torch.zeros(g.m, dtype=torch.int8, device="cuda")
+        ms = W.api.C.c_float(0)
+        st = W.lib().wbpr_mincut_adjoint(d._h, 0, W.api.C.cast(dev.data_ptr(), W.api._i8p), W.api.C.byref(ms))
+        assert st == 0
+        torch.cuda.synchronize()
+        assert np.array_equal(dev.cpu().numpy(), host0)
+        d.set_stream(None)
+        assert d.solve("tc", g.s, g.t).flow == v

@@ -86,7 +86,7 @@ EXPORTED = [
     "wbpr_host_csr_copy", "wbpr_host_csr_free",
     "wbpr_gen_genrmf", "wbpr_gen_rmat", "wbpr_gen_bipartite", "wbpr_gen_layered", "wbpr_gen_grid",
     "wbpr_build_rcsr", "wbpr_build_bcsr", "wbpr_build_bcsr2", "wbpr_graph_create",
-    "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_graph_read_bcsr", "wbpr_graph_read_rcsr", "wbpr_solve", "wbpr_read_state",
+    "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_graph_read_bcsr", "wbpr_graph_read_rcsr", "wbpr_graph_set_stream", "wbpr_solve", "wbpr_read_state",
     "wbpr_verify", "wbpr_mincut_adjoint", "wbpr_rcsr_preflow", "wbpr_rcsr_push_relabel",
     "wbpr_read_trace", "wbpr_solve_bcsr_noalloc", "wbpr_batch_create", "wbpr_batch_destroy",
     "wbpr_batch_device_bytes", "wbpr_batch_solve", "wbpr_batch_instance_stats", "wbpr_batch_autotune",
@@ -140,6 +140,7 @@ def lib() -> C.CDLL:
         "wbpr_graph_device_bytes": (C.c_int64, [vp]),
         "wbpr_graph_read_bcsr": (C.c_int, [vp, _i32p, _i32p, _i32p, _i32p]),
         "wbpr_graph_read_rcsr": (C.c_int, [vp, _i32p, _i32p, _i32p]),
+        "wbpr_graph_set_stream": (C.c_int, [vp, vp]),
         "wbpr_solve": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int, C.POINTER(Tuning), C.POINTER(Result)]),
         "wbpr_read_state": (C.c_int, [vp, _i32p, _i32p, _i32p]),
         "wbpr_read_trace": (C.c_int32, [vp, C.POINTER(C.c_int64), C.c_int32]),
@@ -460,6 +461,12 @@ class DeviceGraph:
         f = np.zeros(max(self.m, 1), np.int32)
         _check(lib().wbpr_read_state(self._h, _p(h), _p(e), _p(f)), "wbpr_read_state")
         return h, e, f[:self.m]
+
+    def set_stream(self, stream: int | None) -> None:
+        """Queue this graph's device work on a caller's CUDA stream (a raw
+        cudaStream_t handle, e.g. torch.cuda.Stream().cuda_stream); None
+        returns to the graph's own stream."""
+        _check(lib().wbpr_graph_set_stream(self._h, stream), "wbpr_graph_set_stream")
 
     def complete_flow(self) -> float:
         """Return stranded excess to s so the arc flows form a maximum flow."""

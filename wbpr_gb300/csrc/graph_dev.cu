@@ -36,7 +36,8 @@ struct wbpr_graph {
   int32_t n = 0;
   int64_t m = 0;
   int32_t s = -1, t = -1;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;  // the stream all of the handle's work goes to
+  cudaStream_t own_stream = nullptr;  // the handle's own stream (destroyed with it)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   // BCSR16
   int* row = nullptr;
@@ -118,7 +119,7 @@ void release(wbpr_graph* g) {
   if (g->ev1) cudaEventDestroy(g->ev1);
   if (g->ev2) cudaEventDestroy(g->ev2);
   if (g->ev3) cudaEventDestroy(g->ev3);
-  if (g->stream) cudaStreamDestroy(g->stream);
+  if (g->own_stream) cudaStreamDestroy(g->own_stream);
   delete g;
 }
 
@@ -948,7 +949,8 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   } while (0)
   TRYC(cudaGetDevice(&g->device));
   TRYC(cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, g->device));
-  TRYC(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+  TRYC(cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking));
+  g->stream = g->own_stream;
   TRYC(cudaEventCreate(&g->ev0));
   TRYC(cudaEventCreate(&g->ev1));
   TRYC(cudaEventCreate(&g->ev2));
@@ -1202,6 +1204,14 @@ wbpr_status wbpr_graph_destroy(wbpr_graph* g) {
 }
 
 int64_t wbpr_graph_device_bytes(const wbpr_graph* g) { return g ? g->bytes : 0; }
+
+wbpr_status wbpr_graph_set_stream(wbpr_graph* g, void* stream) {
+  if (!g) return WBPR_ERR_INVALID_ARG;
+  CK(cudaSetDevice(g->device));
+  CK(cudaStreamSynchronize(g->stream));  // finish what was queued on the previous stream
+  g->stream = stream ? (cudaStream_t)stream : g->own_stream;
+  return WBPR_OK;
+}
 
 wbpr_status wbpr_graph_read_rcsr(const wbpr_graph* g, int32_t* roffsets, int32_t* rdestinations,
                                  int32_t* flow_index) {
@@ -1465,7 +1475,13 @@ wbpr_status wbpr_mincut_adjoint(wbpr_graph* g, int32_t side, int8_t* indicator, 
                                                       side, g->ind);
   CK(cudaGetLastError());
   CK(cudaEventRecord(g->ev1, g->stream));
-  CK(cudaMemcpyAsync(indicator, g->ind, (size_t)g->m, cudaMemcpyDeviceToHost, g->stream));
+  // the caller's buffer may be host or device memory
+  cudaPointerAttributes pa;
+  const bool on_device = cudaPointerGetAttributes(&pa, indicator) == cudaSuccess &&
+                         (pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged);
+  cudaGetLastError();
+  CK(cudaMemcpyAsync(indicator, g->ind, (size_t)g->m, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                     g->stream));
   CK(cudaStreamSynchronize(g->stream));
   if (adjoint_ms) CK(cudaEventElapsedTime(adjoint_ms, g->ev0, g->ev1));
   return WBPR_OK;

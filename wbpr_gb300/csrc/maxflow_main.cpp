@@ -4,7 +4,7 @@
 // device operation goes through the C ABI in wbpr.h.
 //
 //   maxflow [-h] -v {0,1,2,3} -f file [-s src] [-t sink] [-a {0,1}]
-//           [-l {rcsr,bcsr,bcsr2}] [-V] [-j] [-o solution] [-c cache]
+//           [-l {rcsr,bcsr,bcsr16,bcsr2}] [-V] [-j] [-o solution] [-c cache]
 //
 // Added beyond the reference: -v 3 reads the library's graph cache (with
 // capacities and terminals), -c writes the loaded graph to that cache, and
@@ -39,7 +39,7 @@ static void usage(const char* prog) {
   printf("\t-a algorithm\tSpecify the algorithm to use\n");
   printf("\t\t\t\t0: Thread-centric push-relabel (default)\n");
   printf("\t\t\t\t1: Vertex-centric push-relabel\n");
-  printf("\t-l layout\trcsr (default), bcsr or bcsr2\n");
+  printf("\t-l layout\trcsr (default), bcsr (also bcsr16) or bcsr2\n");
   printf("\t-V\t\tVerify the result on the device (capacity, conservation, cut)\n");
   printf("\t-j\t\tAlso print one JSON line with the solve statistics\n");
   printf("\t-o file\t\tWrite the maximum flow as a DIMACS solution (s / f lines)\n");
@@ -135,7 +135,7 @@ int main(int argc, char** argv) {
         break;
       case 'l':
         if (!strcmp(optarg, "rcsr")) layout = WBPR_LAYOUT_RCSR;
-        else if (!strcmp(optarg, "bcsr")) layout = WBPR_LAYOUT_BCSR;
+        else if (!strcmp(optarg, "bcsr") || !strcmp(optarg, "bcsr16")) layout = WBPR_LAYOUT_BCSR;
         else if (!strcmp(optarg, "bcsr2")) layout = WBPR_LAYOUT_BCSR2;
         else {
           printf("Invalid layout\n");
