@@ -321,7 +321,8 @@ def run_ours(args) -> None:
             "flow": flow,
             "solve_ms": {"mean": statistics.mean(r.solve_ms for r in res),
                          "min": min(r.solve_ms for r in res), "max": max(r.solve_ms for r in res)},
-            "gr_ms": last.gr_ms, "rounds_ms": last.kernel_ms, "rounds": last.rounds,
+            "gr_ms": last.gr_ms, "gr_share": last.gr_ms / max(last.solve_ms, 1e-9), "rounds_ms": last.kernel_ms,
+            "rounds": last.rounds,
             "global_relabels": last.global_relabels, "arcs_scanned": last.arcs_scanned,
             "pushes": last.pushes, "relabels": last.relabels, "stranded": last.stranded,
             "verified": True, "wall_s": wall, "gen_s": gen_s,
@@ -491,7 +492,7 @@ def config4(args):
         flows.append(r.flow)
         if sd == 0:
             rng = np.random.default_rng(0)
-            for e in rng.choice(g.m, 6, replace=False):
+            for e in rng.choice(g.m, min(g.m, args.fd_arcs), replace=False):
                 up = g.cap.copy()
                 up[e] += 1
                 dp = W.maxflow(W.Graph(g.n, g.off, g.dst, up, g.s, g.t)) - r.flow
@@ -532,6 +533,8 @@ def main() -> None:
                     help="1: the R-MAT benchmark (default); 0: GENRMF 8x16; 2: bipartite matching; "
                     "3: batched instances; 4: grids with the adjoint")
     ap.add_argument("--instances", type=int, default=0, help="instances/seeds/grids for --config 0/3/4")
+    ap.add_argument("--fd-arcs", type=int, default=6, help="--config 4: arcs of the first grid checked by "
+                    "+-1 finite-difference re-solves")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
