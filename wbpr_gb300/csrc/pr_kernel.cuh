@@ -1055,12 +1055,20 @@ __device__ void bfs_materialise(const Params<Topo>& p, int level, int fc, BlockA
   const int lane = threadIdx.x & 31;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   const int nall = p.n_light + p.n_medium + p.n_heavy;
-  for (int base = gt - lane; base < nall; base += gs) {
-    const int i = base + lane;
-    int v = -1;
-    if (i < nall) v = __ldg(p.cls + i);
-    const bool in = v >= 0 && __ldcg(p.lab + v) == level;
-    warp_frontier(p, &c->mcount, &c->mhcount, fc, v, in, acc);
+  // 4 entries per lane in flight: the scan is latency-bound, few entries hit
+  for (long long base = 4LL * (gt - lane); base < nall; base += 4LL * gs) {
+    int v[4];
+    bool in[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const long long i = base + q * 32 + lane;
+      v[q] = i < nall ? __ldg(p.cls + i) : -1;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) in[q] = v[q] >= 0 && __ldcg(p.lab + v[q]) == level;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (__any_sync(0xffffffffu, in[q])) warp_frontier(p, &c->mcount, &c->mhcount, fc, v[q], in[q], acc);
   }
 }
 
