@@ -252,6 +252,13 @@ wbpr_status wbpr_graph_read_rcsr(const wbpr_graph* g, int32_t* roffsets, int32_t
  * a maximum preflow.  Result flow = excess(t). s/t = -1 use the graph's. */
 wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo,
                        const wbpr_tuning* tuning, wbpr_result* out);
+/* Try tile widths {8, 16, 32} (VC; TC has one), global-relabel work factors
+ * {0.5, 0.75, 1.5, 3} and long-row thresholds {32, 64} on this graph and
+ * these terminals (the faster of two solves each); return the fastest tuning
+ * and its solve time.  Every tuning must give the same flow (WBPR_ERR_VERIFY
+ * otherwise).  The graph's state afterwards is that of the last solve. */
+wbpr_status wbpr_autotune(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, wbpr_tuning* best,
+                          float* best_ms);
 /* Read back the state after a solve (host buffers, any may be NULL):
  * height[n], excess[n], and per input arc flow = cap - residual (m). */
 wbpr_status wbpr_read_state(wbpr_graph* g, int32_t* height, int32_t* excess,

@@ -140,3 +140,16 @@ def test_caller_stream_and_device_indicator():
         assert np.array_equal(dev.cpu().numpy(), host0)
         d.set_stream(None)
         assert d.solve("tc", g.s, g.t).flow == v
+
+
+def test_single_graph_autotune():
+    for g in (W.gen_rmat(14, 16, seed=2), W.gen_genrmf(10, 10, 1, 1000, 3)):
+        v = oracle.dinic(g.n, g.off, g.dst, g.cap, g.s, g.t)
+        with W.DeviceGraph(g, "bcsr") as d:
+            best, ms = d.autotune("vc", g.s, g.t)
+            assert best.tile in (8, 16, 32) and best.gr_alpha in (0.5, 0.75, 1.5, 3.0)
+            assert best.heavy_degree in (32, 64) and ms > 0
+            r = d.solve("vc", g.s, g.t, tile=best.tile, gr_alpha=best.gr_alpha, heavy_degree=best.heavy_degree)
+            assert r.flow == v
+            tc, _ = d.autotune("tc", g.s, g.t)
+            assert tc.tile == 0

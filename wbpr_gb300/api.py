@@ -86,7 +86,7 @@ EXPORTED = [
     "wbpr_host_csr_copy", "wbpr_host_csr_free",
     "wbpr_gen_genrmf", "wbpr_gen_rmat", "wbpr_gen_bipartite", "wbpr_gen_layered", "wbpr_gen_grid",
     "wbpr_build_rcsr", "wbpr_build_bcsr", "wbpr_build_bcsr2", "wbpr_graph_create",
-    "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_graph_read_bcsr", "wbpr_graph_read_rcsr", "wbpr_graph_set_stream", "wbpr_solve", "wbpr_read_state",
+    "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_graph_read_bcsr", "wbpr_graph_read_rcsr", "wbpr_graph_set_stream", "wbpr_autotune", "wbpr_solve", "wbpr_read_state",
     "wbpr_verify", "wbpr_mincut_adjoint", "wbpr_rcsr_preflow", "wbpr_rcsr_push_relabel",
     "wbpr_read_trace", "wbpr_solve_bcsr_noalloc", "wbpr_batch_create", "wbpr_batch_destroy",
     "wbpr_batch_device_bytes", "wbpr_batch_solve", "wbpr_batch_instance_stats", "wbpr_batch_autotune",
@@ -141,6 +141,7 @@ def lib() -> C.CDLL:
         "wbpr_graph_read_bcsr": (C.c_int, [vp, _i32p, _i32p, _i32p, _i32p]),
         "wbpr_graph_read_rcsr": (C.c_int, [vp, _i32p, _i32p, _i32p]),
         "wbpr_graph_set_stream": (C.c_int, [vp, vp]),
+        "wbpr_autotune": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_float)]),
         "wbpr_solve": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int, C.POINTER(Tuning), C.POINTER(Result)]),
         "wbpr_read_state": (C.c_int, [vp, _i32p, _i32p, _i32p]),
         "wbpr_read_trace": (C.c_int32, [vp, C.POINTER(C.c_int64), C.c_int32]),
@@ -461,6 +462,14 @@ class DeviceGraph:
         f = np.zeros(max(self.m, 1), np.int32)
         _check(lib().wbpr_read_state(self._h, _p(h), _p(e), _p(f)), "wbpr_read_state")
         return h, e, f[:self.m]
+
+    def autotune(self, algo="vc", s: int | None = None, t: int | None = None):
+        """(best Tuning, its solve ms) over tile, relabel frequency and long-row threshold."""
+        tu = Tuning()
+        ms = C.c_float(0)
+        _check(lib().wbpr_autotune(self._h, -1 if s is None else s, -1 if t is None else t, ALGOS[algo],
+                                   C.byref(tu), C.byref(ms)), "wbpr_autotune")
+        return tu, float(ms.value)
 
     def set_stream(self, stream: int | None) -> None:
         """Queue this graph's device work on a caller's CUDA stream (a raw

@@ -87,7 +87,7 @@ def build(force: bool = False, ptxas_verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         for fut in [ex.submit(_run, j) for j in jobs]:
             fut.result()
-    _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-pthread"])
+    _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-pthread", "-ldl"])
     _run([cxx, "-O2", "-std=c++17", "-Wall", *inc, os.path.join(CSRC, "maxflow_main.cpp"),
           "-o", CLI, "-L", OUT, "-lwbpr", "-Wl,-rpath,$ORIGIN"])
     with open(stamp_file, "w") as f:

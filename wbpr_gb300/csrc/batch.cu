@@ -17,6 +17,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "pr_kernel.cuh"
 #include "wbpr_internal.h"
 
@@ -402,6 +404,10 @@ wbpr_status capture(wbpr_batch* b, int tile, int block, double alpha, int grr, l
 extern "C" {
 
 wbpr_status wbpr_batch_create(const wbpr_csr* graphs, int32_t count, wbpr_batch** out) {
+  nvtxRangePushA("wbpr_batch_create");
+  struct Pop {
+    ~Pop() { nvtxRangePop(); }
+  } pop_;
   if (!out || !graphs || count < 1) return WBPR_ERR_INVALID_ARG;
   *out = nullptr;
   int64_t tn = 0, tm = 0;
@@ -510,6 +516,10 @@ wbpr_status wbpr_batch_destroy(wbpr_batch* b) {
 int64_t wbpr_batch_device_bytes(const wbpr_batch* b) { return b ? b->bytes : 0; }
 
 wbpr_status wbpr_batch_solve(wbpr_batch* b, const wbpr_tuning* tu, int64_t* flows, float* solve_ms) {
+  nvtxRangePushA("wbpr_batch_solve");
+  struct Pop {
+    ~Pop() { nvtxRangePop(); }
+  } pop_;
   if (!b) return WBPR_ERR_INVALID_ARG;
   wbpr_tuning d;
   wbpr_default_tuning(&d);
@@ -551,6 +561,10 @@ wbpr_status wbpr_batch_instance_stats(wbpr_batch* b, float* inst_ms, int32_t* in
 }
 
 wbpr_status wbpr_batch_autotune(wbpr_batch* b, wbpr_tuning* best, float* best_ms) {
+  nvtxRangePushA("wbpr_batch_autotune");
+  struct Pop {
+    ~Pop() { nvtxRangePop(); }
+  } pop_;
   if (!b || !best) return WBPR_ERR_INVALID_ARG;
   const int tiles[] = {8, 16, 32};
   const int blocks[] = {256, 512};

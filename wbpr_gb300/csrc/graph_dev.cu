@@ -9,10 +9,18 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "pr_launch.h"
 #include "wbpr_internal.h"
 
 using namespace wbpr_dev;
+
+// NVTX range around an entry point (a no-op unless a profiler is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
 
 static thread_local std::string g_last_error;
 
@@ -698,6 +706,7 @@ wbpr_status device_scan(int* data, long long count, cudaStream_t st) {
 // BCSR row/arc/arx or RCSR frow/farc/fcb/fcap/rrow/rarc, plus ioff, the
 // length classes cls, the heavy-row chunks bch, hown/hsum/hmin and counts.
 wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
+  NvtxRange nvtx_("device build");
   const int n = g->n;
   const long long m = g->m;
   cudaStream_t st = g->stream;
@@ -1194,6 +1203,7 @@ int32_t wbpr_device_count(void) {
 }
 
 wbpr_status wbpr_graph_create(const wbpr_csr* g, wbpr_layout layout, wbpr_graph** out) {
+  NvtxRange nvtx_("wbpr_graph_create");
   return create_impl(g, layout, out);
 }
 
@@ -1204,6 +1214,46 @@ wbpr_status wbpr_graph_destroy(wbpr_graph* g) {
 }
 
 int64_t wbpr_graph_device_bytes(const wbpr_graph* g) { return g ? g->bytes : 0; }
+
+wbpr_status wbpr_autotune(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, wbpr_tuning* best,
+                          float* best_ms) {
+  NvtxRange nvtx_("wbpr_autotune");
+  if (!g || !best) return WBPR_ERR_INVALID_ARG;
+  const int tiles_vc[] = {8, 16, 32};
+  const int tiles_tc[] = {0};
+  const double alphas[] = {0.5, 0.75, 1.5, 3.0};
+  const int heavies[] = {32, 64};
+  const int* tiles = algo == WBPR_ALGO_TC ? tiles_tc : tiles_vc;
+  const int ntiles = algo == WBPR_ALGO_TC ? 1 : 3;
+  float bms = 0;
+  bool have = false;
+  int64_t flow = -1;
+  for (int ti = 0; ti < ntiles; ++ti)
+    for (double a : alphas)
+      for (int hd : heavies) {
+        wbpr_tuning tu;
+        wbpr_default_tuning(&tu);
+        tu.tile = tiles[ti];
+        tu.gr_alpha = a;
+        tu.heavy_degree = hd;
+        float ms = 0;
+        for (int rep = 0; rep < 2; ++rep) {  // the faster of two solves
+          wbpr_result r;
+          const wbpr_status st = wbpr_solve(g, s, t, algo, &tu, &r);
+          if (st) return st;
+          if (flow >= 0 && r.flow != flow) return WBPR_ERR_VERIFY;  // every tuning must agree
+          flow = r.flow;
+          ms = rep ? std::min(ms, r.solve_ms) : r.solve_ms;
+        }
+        if (!have || ms < bms) {
+          have = true;
+          bms = ms;
+          *best = tu;
+        }
+      }
+  if (best_ms) *best_ms = bms;
+  return WBPR_OK;
+}
 
 wbpr_status wbpr_graph_set_stream(wbpr_graph* g, void* stream) {
   if (!g) return WBPR_ERR_INVALID_ARG;
@@ -1253,6 +1303,7 @@ wbpr_status wbpr_graph_read_bcsr(const wbpr_graph* g, int32_t* offsets, int32_t*
 
 wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, const wbpr_tuning* tu,
                        wbpr_result* out) {
+  NvtxRange nvtx_("wbpr_solve");
   if (!g) return WBPR_ERR_INVALID_ARG;
   if (s < 0) s = g->s;
   if (t < 0) t = g->t;
@@ -1327,6 +1378,7 @@ int32_t wbpr_read_trace(wbpr_graph* g, int64_t* out, int32_t cap) {
 }
 
 wbpr_status wbpr_read_state(wbpr_graph* g, int32_t* height, int32_t* excess, int32_t* arc_flow) {
+  NvtxRange nvtx_("wbpr_read_state");
   if (!g) return WBPR_ERR_INVALID_ARG;
   CK(cudaSetDevice(g->device));
   CK(cudaStreamSynchronize(g->stream));
@@ -1360,6 +1412,7 @@ static wbpr_status bfs_labels(wbpr_graph* g, int root, int dir, int excl) {
 }
 
 wbpr_status wbpr_verify(wbpr_graph* g, wbpr_verify_report* rep) {
+  NvtxRange nvtx_("wbpr_verify");
   if (!g || !rep) return WBPR_ERR_INVALID_ARG;
   std::memset(rep, 0, sizeof(*rep));
   if (g->s < 0 || g->t < 0) return WBPR_ERR_INVALID_ARG;
@@ -1423,6 +1476,7 @@ static wbpr_status return_stranded(wbpr_graph* g) {
 extern "C" {
 
 wbpr_status wbpr_complete_flow(wbpr_graph* g, float* ms) {
+  NvtxRange nvtx_("wbpr_complete_flow");
   if (!g || g->s < 0 || g->t < 0) return WBPR_ERR_INVALID_ARG;
   CK(cudaSetDevice(g->device));
   CK(cudaEventRecord(g->ev0, g->stream));
@@ -1435,6 +1489,7 @@ wbpr_status wbpr_complete_flow(wbpr_graph* g, float* ms) {
 }
 
 wbpr_status wbpr_cut_sides(wbpr_graph* g, int32_t side, int8_t* in_set) {
+  NvtxRange nvtx_("wbpr_cut_sides");
   if (!g || !in_set || (side != 0 && side != 1) || g->s < 0 || g->t < 0) return WBPR_ERR_INVALID_ARG;
   CK(cudaSetDevice(g->device));
   wbpr_status st;
@@ -1454,6 +1509,7 @@ wbpr_status wbpr_cut_sides(wbpr_graph* g, int32_t side, int8_t* in_set) {
 }
 
 wbpr_status wbpr_mincut_adjoint(wbpr_graph* g, int32_t side, int8_t* indicator, float* adjoint_ms) {
+  NvtxRange nvtx_("wbpr_mincut_adjoint");
   if (!g || !indicator || (side != 0 && side != 1)) return WBPR_ERR_INVALID_ARG;
   if (g->s < 0 || g->t < 0) return WBPR_ERR_INVALID_ARG;
   CK(cudaSetDevice(g->device));

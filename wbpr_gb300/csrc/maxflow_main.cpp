@@ -212,12 +212,16 @@ int main(int argc, char** argv) {
   if (verify) printf("Verification: passed (capacity, conservation, cut == flow)\n");
   if (json) {
     printf("{\"value\": %lld, \"solve_ms\": %.4f, \"kernel_ms\": %.4f, \"gr_ms\": %.4f, "
-           "\"rounds\": %d, \"global_relabels\": %d, \"arcs_scanned\": %llu, \"pushes\": %llu, "
-           "\"relabels\": %llu, \"mteps\": %.3f}\n",
-           (long long)res.flow, res.solve_ms, res.kernel_ms, res.gr_ms, res.rounds,
-           res.global_relabels, (unsigned long long)res.arcs_scanned,
-           (unsigned long long)res.pushes, (unsigned long long)res.relabels,
-           res.solve_ms > 0 ? (double)g->num_edges / (res.solve_ms * 1e3) : 0.0);
+           "\"gr_share\": %.4f, \"rounds\": %d, \"global_relabels\": %d, \"arcs_scanned\": %llu, "
+           "\"pushes\": %llu, \"relabels\": %llu, \"mteps\": %.3f, \"alg_bytes\": %llu, "
+           "\"hbm_gbps\": %.1f}\n",
+           (long long)res.flow, res.solve_ms, res.kernel_ms, res.gr_ms,
+           res.solve_ms > 0 ? res.gr_ms / res.solve_ms : 0.0, res.rounds, res.global_relabels,
+           (unsigned long long)res.arcs_scanned, (unsigned long long)res.pushes,
+           (unsigned long long)res.relabels,
+           res.solve_ms > 0 ? (double)g->num_edges / (res.solve_ms * 1e3) : 0.0,
+           (unsigned long long)res.alg_bytes,
+           res.launch_ms > 0 ? (double)res.alg_bytes / (res.launch_ms * 1e6) : 0.0);
   }
   int rc = 0;
   if (out_path) {
