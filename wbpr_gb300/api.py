@@ -101,7 +101,9 @@ def lib() -> C.CDLL:
     if _lib is not None:
         return _lib
     path = _build.LIB
-    if not os.path.exists(path) or os.environ.get("WBPR_REBUILD"):
+    if os.environ.get("WBPR_CHECKED") == "1":  # bounds-checked solver kernels
+        path = _build.build_checked()
+    elif not os.path.exists(path) or os.environ.get("WBPR_REBUILD"):
         _build.build()
     L = C.CDLL(path)
     vp = C.c_void_p

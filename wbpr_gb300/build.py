@@ -21,6 +21,8 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libwbpr.so")
+LIB_CHECKED = os.path.join(OUT, "libwbpr_checked.so")
+CHECKED_SOURCES = ["pr_bcsr.cu", "pr_rcsr.cu"]  # the solver kernels
 CLI = os.path.join(OUT, "maxflow")
 
 ARCH = ["-gencode=arch=compute_103a,code=sm_103a"]
@@ -93,6 +95,38 @@ def build(force: bool = False, ptxas_verbose: bool = False) -> str:
     with open(stamp_file, "w") as f:
         f.write(stamp)
     return LIB
+
+
+def build_checked() -> str:
+    """libwbpr_checked.so: the solver kernels compiled with bounds-checked
+    arc and vertex accessors (-DWBPR_CHECKED), linked with the other objects
+    of the normal build.  An out-of-range index is counted instead of used,
+    and the solve returns WBPR_ERR_VERIFY.  Built on demand (debugging and
+    its GPU test), not by build()."""
+    build()
+    stamp = _stamp() + "checked"
+    stamp_file = os.path.join(OUT, "stamp_checked")
+    if os.path.exists(LIB_CHECKED) and os.path.exists(stamp_file) and open(stamp_file).read() == stamp:
+        return LIB_CHECKED
+    nvcc = _nvcc()
+    inc = ["-I", INCLUDE, "-I", CSRC]
+    jobs, objs = [], []
+    for src in CU_SOURCES:
+        if src in CHECKED_SOURCES:
+            obj = os.path.join(OUT, src + ".checked.o")
+            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, "-DWBPR_CHECKED", *inc, "-c", os.path.join(CSRC, src),
+                         "-o", obj])
+        else:
+            obj = os.path.join(OUT, src + ".o")
+        objs.append(obj)
+    objs += [os.path.join(OUT, src + ".o") for src in CPP_SOURCES]
+    with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        for fut in [ex.submit(_run, j) for j in jobs]:
+            fut.result()
+    _run([nvcc, *ARCH, "-shared", "-o", LIB_CHECKED, *objs, "-Xcompiler", "-pthread", "-ldl"])
+    with open(stamp_file, "w") as f:
+        f.write(stamp)
+    return LIB_CHECKED
 
 
 if __name__ == "__main__":

@@ -1035,6 +1035,9 @@ void topo_of(wbpr_graph* g, TopoB& b) {
   b.row = g->row;
   b.arc = g->arc;
   b.arx = g->arx;
+  b.bd.viol = &g->ctl->viol;
+  b.bd.na = 2 * g->m;
+  b.bd.n = g->n;
 }
 void topo_of(wbpr_graph* g, TopoR& r) {
   r.frow = g->frow;
@@ -1042,6 +1045,9 @@ void topo_of(wbpr_graph* g, TopoR& r) {
   r.fcb = g->fcb;
   r.rrow = g->rrow;
   r.rarc = g->rarc;
+  r.bd.viol = &g->ctl->viol;
+  r.bd.na = g->m;
+  r.bd.n = g->n;
 }
 
 // graphs with n + residual arcs up to this run on one block: its phases are
@@ -1122,6 +1128,10 @@ wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch
   if (launch_ms) CK(cudaEventElapsedTime(launch_ms, g->ev2, g->ev3));
   g->trace_n = rc.trace ? hs->trace_n : 0;
   if (hc.err) return (wbpr_status)hc.err;
+  if (hc.viol) {
+    g_last_error = "bounds check: " + std::to_string(hc.viol) + " out-of-range arc or vertex indices";
+    return WBPR_ERR_VERIFY;
+  }
   return WBPR_OK;
 }
 

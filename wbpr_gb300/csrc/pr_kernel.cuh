@@ -76,7 +76,8 @@ struct Ctl {
   int bu_found[3];  // vertices labelled by a bottom-up level, by level % 3
   int mcount;       // materialised frontier: short rows
   int mhcount;      //   long-row chunk items
-  alignas(128) int gr_ok;  // rounds since the last global relabel took at least half as long as it
+  alignas(128) int gr_ok;
+  int viol;  // out-of-range indices seen by the checked build  // rounds since the last global relabel took at least half as long as it
   // work done in rounds of even / odd parity; block b adds to slot b % 32
   alignas(128) unsigned long long work[2][kWorkSlots * 16];
 };
@@ -152,34 +153,67 @@ __device__ __forceinline__ long long ldv64(const long long* p) { return *(const 
 // Residual topologies.  load() returns (head, residual of u->head); push()
 // moves p units along the arc and its twin; twin_cf() is the residual of the
 // opposite arc head->u.
+// Bounds of a topology for the checked build (compiled with -DWBPR_CHECKED):
+// an arc index >= na or a vertex >= n is counted in *viol and replaced by 0,
+// so the kernel still finishes and the host reports WBPR_ERR_VERIFY.  With
+// viol == nullptr, or in the normal build, nothing is checked.
+struct Bounds {
+  int* viol = nullptr;
+  long long na = 0;
+  int n = 0;
+};
+__device__ __forceinline__ long long chk(const Bounds& b, long long i, long long lim) {
+#ifdef WBPR_CHECKED
+  if (b.viol && (unsigned long long)i >= (unsigned long long)lim) {
+    atomicAdd(b.viol, 1);
+    return 0;
+  }
+#endif
+  return i;
+}
+
 struct TopoB {  // BCSR16: row[n+1], arc {dst, cf}, arx {rev, cap}
   const int* row;
   int2* arc;
   const int2* arx;
+  Bounds bd;
   static constexpr int kSeg = 1;
   __device__ __forceinline__ void seg(int u, int, int& b, int& e) const {
+    u = (int)chk(bd, u, bd.n);
     b = __ldg(row + u);
     e = __ldg(row + u + 1);
   }
-  __device__ __forceinline__ int deg(int u) const { return __ldg(row + u + 1) - __ldg(row + u); }
+  __device__ __forceinline__ int deg(int u) const {
+    u = (int)chk(bd, u, bd.n);
+    return __ldg(row + u + 1) - __ldg(row + u);
+  }
   __device__ __forceinline__ void load(int, int a, int& dst, int& cf) const {
+    a = (int)chk(bd, a, bd.na);
     int2 r = __ldcg(arc + a);
-    dst = r.x;
+    dst = (int)chk(bd, r.x, bd.n);
     cf = r.y;
   }
-  __device__ __forceinline__ int head(int, int a) const { return __ldcg(&arc[a].x); }
+  __device__ __forceinline__ int head(int, int a) const {
+    a = (int)chk(bd, a, bd.na);
+    return (int)chk(bd, __ldcg(&arc[a].x), bd.n);
+  }
   __device__ __forceinline__ void push(int, int a, int cf, int p) const {
+    a = (int)chk(bd, a, bd.na);
     arc[a].y = cf - p;
-    int r = __ldg(&arx[a].x);
+    int r = (int)chk(bd, __ldg(&arx[a].x), bd.na);
     int* tc = &arc[r].y;
     *tc = __ldcg(tc) + p;
   }
   __device__ __forceinline__ int twin_cf(int, int a) const {
-    int r = __ldg(&arx[a].x);
+    a = (int)chk(bd, a, bd.na);
+    int r = (int)chk(bd, __ldg(&arx[a].x), bd.na);
     return __ldcg(&arc[r].y);
   }
   // address of the twin's residual (one load here, none for RCSR forward)
-  __device__ __forceinline__ const int* twin_ptr(int, int a) const { return &arc[__ldg(&arx[a].x)].y; }
+  __device__ __forceinline__ const int* twin_ptr(int, int a) const {
+    a = (int)chk(bd, a, bd.na);
+    return &arc[chk(bd, __ldg(&arx[a].x), bd.na)].y;
+  }
 };
 
 struct TopoR {  // RCSR: forward {dst, cf_f} + cf_b, reverse {tail, forward id}
@@ -188,46 +222,54 @@ struct TopoR {  // RCSR: forward {dst, cf_f} + cf_b, reverse {tail, forward id}
   int* fcb;
   const int* rrow;
   const int2* rarc;
+  Bounds bd;  // na = m (forward arcs and reverse entries alike)
   static constexpr int kSeg = 2;
   __device__ __forceinline__ void seg(int u, int k, int& b, int& e) const {
+    u = (int)chk(bd, u, bd.n);
     const int* r = k == 0 ? frow : rrow;
     b = __ldg(r + u);
     e = __ldg(r + u + 1);
   }
   __device__ __forceinline__ int deg(int u) const {
+    u = (int)chk(bd, u, bd.n);
     return __ldg(frow + u + 1) - __ldg(frow + u) + __ldg(rrow + u + 1) - __ldg(rrow + u);
   }
   __device__ __forceinline__ void load(int k, int a, int& dst, int& cf) const {
+    a = (int)chk(bd, a, bd.na);
     if (k == 0) {
       int2 r = __ldcg(farc + a);
-      dst = r.x;
+      dst = (int)chk(bd, r.x, bd.n);
       cf = r.y;
     } else {
       int2 r = __ldg(rarc + a);
-      dst = r.x;
-      cf = __ldcg(fcb + r.y);
+      dst = (int)chk(bd, r.x, bd.n);
+      cf = __ldcg(fcb + chk(bd, r.y, bd.na));
     }
   }
   __device__ __forceinline__ int head(int k, int a) const {
-    return k == 0 ? __ldcg(&farc[a].x) : __ldg(&rarc[a].x);
+    a = (int)chk(bd, a, bd.na);
+    return (int)chk(bd, k == 0 ? __ldcg(&farc[a].x) : __ldg(&rarc[a].x), bd.n);
   }
   __device__ __forceinline__ void push(int k, int a, int cf, int p) const {
+    a = (int)chk(bd, a, bd.na);
     if (k == 0) {
       farc[a].y = cf - p;
       fcb[a] = __ldcg(fcb + a) + p;
     } else {
-      int fi = __ldg(&rarc[a].y);
+      int fi = (int)chk(bd, __ldg(&rarc[a].y), bd.na);
       fcb[fi] = cf - p;
       farc[fi].y = __ldcg(&farc[fi].y) + p;
     }
   }
   __device__ __forceinline__ int twin_cf(int k, int a) const {
+    a = (int)chk(bd, a, bd.na);
     if (k == 0) return __ldcg(fcb + a);
-    int fi = __ldg(&rarc[a].y);
+    int fi = (int)chk(bd, __ldg(&rarc[a].y), bd.na);
     return __ldcg(&farc[fi].y);
   }
   __device__ __forceinline__ const int* twin_ptr(int k, int a) const {
-    return k == 0 ? fcb + a : &farc[__ldg(&rarc[a].y)].y;
+    a = (int)chk(bd, a, bd.na);
+    return k == 0 ? fcb + a : &farc[chk(bd, __ldg(&rarc[a].y), bd.na)].y;
   }
 };
 
