@@ -252,6 +252,16 @@ wbpr_status wbpr_graph_read_rcsr(const wbpr_graph* g, int32_t* roffsets, int32_t
  * a maximum preflow.  Result flow = excess(t). s/t = -1 use the graph's. */
 wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo,
                        const wbpr_tuning* tuning, wbpr_result* out);
+/* Many (source, sink) pairs in one solve, new: the preflow saturates the arcs
+ * of every source, every sink absorbs flow and roots the global relabel, and
+ * flows[i] receives the flow that ended at sinks[i].  When each pair lies in
+ * its own connected component -- many instances stored as one disjoint-union
+ * graph -- flows[i] is the maximum flow from sources[i] to sinks[i], and all
+ * instances are solved by the whole GPU at once.  Every vertex may hold at
+ * most one terminal role.  The handle's single-pair state (wbpr_verify,
+ * wbpr_mincut_adjoint, wbpr_complete_flow) does not apply to this solve. */
+wbpr_status wbpr_solve_pairs(wbpr_graph* g, int32_t k, const int32_t* sources, const int32_t* sinks,
+                             wbpr_algo algo, const wbpr_tuning* tuning, int64_t* flows, wbpr_result* out);
 /* Try tile widths {8, 16, 32} (VC; TC has one), global-relabel work factors
  * {0.5, 0.75, 1.5, 3} and long-row thresholds {32, 64} on this graph and
  * these terminals (the faster of two solves each); return the fastest tuning

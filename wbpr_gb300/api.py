@@ -86,7 +86,7 @@ EXPORTED = [
     "wbpr_host_csr_copy", "wbpr_host_csr_free",
     "wbpr_gen_genrmf", "wbpr_gen_rmat", "wbpr_gen_bipartite", "wbpr_gen_layered", "wbpr_gen_grid",
     "wbpr_build_rcsr", "wbpr_build_bcsr", "wbpr_build_bcsr2", "wbpr_graph_create",
-    "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_graph_read_bcsr", "wbpr_graph_read_rcsr", "wbpr_graph_set_stream", "wbpr_autotune", "wbpr_solve", "wbpr_read_state",
+    "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_graph_read_bcsr", "wbpr_graph_read_rcsr", "wbpr_graph_set_stream", "wbpr_autotune", "wbpr_solve_pairs", "wbpr_solve", "wbpr_read_state",
     "wbpr_verify", "wbpr_mincut_adjoint", "wbpr_rcsr_preflow", "wbpr_rcsr_push_relabel",
     "wbpr_read_trace", "wbpr_solve_bcsr_noalloc", "wbpr_batch_create", "wbpr_batch_destroy",
     "wbpr_batch_device_bytes", "wbpr_batch_solve", "wbpr_batch_instance_stats", "wbpr_batch_autotune",
@@ -143,6 +143,8 @@ def lib() -> C.CDLL:
         "wbpr_graph_read_bcsr": (C.c_int, [vp, _i32p, _i32p, _i32p, _i32p]),
         "wbpr_graph_read_rcsr": (C.c_int, [vp, _i32p, _i32p, _i32p]),
         "wbpr_graph_set_stream": (C.c_int, [vp, vp]),
+        "wbpr_solve_pairs": (C.c_int, [vp, C.c_int32, _i32p, _i32p, C.c_int, C.POINTER(Tuning),
+                                       C.POINTER(C.c_int64), C.POINTER(Result)]),
         "wbpr_autotune": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_float)]),
         "wbpr_solve": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int, C.POINTER(Tuning), C.POINTER(Result)]),
         "wbpr_read_state": (C.c_int, [vp, _i32p, _i32p, _i32p]),
@@ -465,6 +467,20 @@ class DeviceGraph:
         _check(lib().wbpr_read_state(self._h, _p(h), _p(e), _p(f)), "wbpr_read_state")
         return h, e, f[:self.m]
 
+    def solve_pairs(self, sources, sinks, algo="vc", **tuning):
+        """Flows for many (source, sink) pairs in one solve (exact per pair when
+        each pair has its own connected component); returns (flows, Result)."""
+        src = np.ascontiguousarray(sources, np.int32)
+        snk = np.ascontiguousarray(sinks, np.int32)
+        if src.shape != snk.shape or src.ndim != 1:
+            raise ValueError("sources and sinks must be 1-d and of the same length")
+        flows = np.zeros(len(src), np.int64)
+        r = Result()
+        tu = default_tuning(**tuning)
+        _check(lib().wbpr_solve_pairs(self._h, len(src), _p(src), _p(snk), ALGOS[algo], C.byref(tu),
+                                      flows.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(r)), "wbpr_solve_pairs")
+        return flows, r
+
     def autotune(self, algo="vc", s: int | None = None, t: int | None = None):
         """(best Tuning, its solve ms) over tile, relabel frequency and long-row threshold."""
         tu = Tuning()
@@ -551,6 +567,24 @@ class Batch:
         ms = C.c_float(0)
         _check(lib().wbpr_batch_autotune(self._h, C.byref(t), C.byref(ms)), "wbpr_batch_autotune")
         return t, float(ms.value)
+
+
+def disjoint_union(graphs: list):
+    """One graph holding every graph of the list as its own component: returns
+    (graph, sources, sinks) with each graph's terminals at their new ids."""
+    offs, dsts, caps, srcs, snks = [np.zeros(1, np.int64)], [], [], [], []
+    base, arc_base = 0, 0
+    for g in graphs:
+        offs.append(g.off[1:].astype(np.int64) + arc_base)
+        dsts.append(g.dst.astype(np.int64) + base)
+        caps.append(g.cap)
+        srcs.append(g.s + base)
+        snks.append(g.t + base)
+        base += g.n
+        arc_base += g.m
+    u = Graph(base, np.concatenate(offs).astype(np.int32), np.concatenate(dsts).astype(np.int32),
+              np.concatenate(caps).astype(np.int32), int(srcs[0]), int(snks[0]))
+    return u, np.array(srcs, np.int32), np.array(snks, np.int32)
 
 
 def maxflow(g: Graph, algo="vc", layout="bcsr", **tuning) -> int:

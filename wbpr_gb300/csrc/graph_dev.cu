@@ -46,6 +46,11 @@ struct wbpr_graph {
   int32_t s = -1, t = -1;
   cudaStream_t stream = nullptr;  // the stream all of the handle's work goes to
   cudaStream_t own_stream = nullptr;  // the handle's own stream (destroyed with it)
+  // terminal sets of the last multi-pair solve
+  signed char* term = nullptr;
+  int* pairs = nullptr;  // sources then sinks
+  int64_t pairs_cap = 0;
+  long long* pair_flow = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   // BCSR16
   int* row = nullptr;
@@ -322,6 +327,15 @@ __global__ void indicator_kernel(const int* ioff, const int* row, const int2* ar
       ind[i] = side == 0 ? (int8_t)(!uin && vin) : (int8_t)(uin && !vin);
     }
   }
+}
+
+// the excess of each sink of a multi-pair solve
+__global__ void sink_flows(const int* e, const int* sinks, int k, long long* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k; i += gridDim.x * blockDim.x) out[i] = e[sinks[i]];
+}
+__global__ void set_terms(signed char* term, const int* pairs, int k) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * k; i += gridDim.x * blockDim.x)
+    term[pairs[i]] = i < k ? 1 : 2;
 }
 
 // per input arc: flow = capacity - residual
@@ -1069,6 +1083,12 @@ struct RunCfg {
   int bfs_dir, bfs_root, bfs_excl;
   int* lab;
   bool trace;
+  // terminal sets (multi-pair solve); term == nullptr for one pair
+  const signed char* term;
+  const int* sources;
+  int n_sources;
+  const int* sinks;
+  int n_sinks;
 };
 
 template <class Topo>
@@ -1089,6 +1109,16 @@ wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch
   p.bfs_root = rc.bfs_root;
   p.bfs_excl = rc.bfs_excl;
   if (rc.lab) p.lab = rc.lab;
+  if (rc.term) {
+    p.term = rc.term;
+    p.sources = rc.sources;
+    p.n_sources = rc.n_sources;
+    p.sinks = rc.sinks;
+    p.n_sinks = rc.n_sinks;
+    p.s = -1;
+    p.t = -1;
+    p.bfs_excl = -1;
+  }
   if (rc.trace) {
     if (!g->trace) {
       g->trace_cap = 1 << 14;
@@ -1367,6 +1397,88 @@ wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, cons
     st = wbpr_verify(g, &rep);
     if (st) return st;
     if (!rep.ok) return WBPR_ERR_VERIFY;
+  }
+  return WBPR_OK;
+}
+
+wbpr_status wbpr_solve_pairs(wbpr_graph* g, int32_t k, const int32_t* sources, const int32_t* sinks,
+                             wbpr_algo algo, const wbpr_tuning* tu, int64_t* flows, wbpr_result* out) {
+  NvtxRange nvtx_("wbpr_solve_pairs");
+  if (!g || k < 1 || !sources || !sinks || !flows) return WBPR_ERR_INVALID_ARG;
+  {
+    // every vertex at most one terminal role, all in range
+    std::vector<signed char> seen((size_t)g->n, 0);
+    for (int i = 0; i < 2 * k; ++i) {
+      const int v = i < k ? sources[i] : sinks[i - k];
+      if (v < 0 || v >= g->n || seen[(size_t)v]) return WBPR_ERR_INVALID_ARG;
+      seen[(size_t)v] = 1;
+    }
+  }
+  RunCfg rc;
+  wbpr_status st = make_cfg(g, sources[0], sinks[0], algo, tu, &rc);
+  if (st) return st;
+  CK(cudaSetDevice(g->device));
+  if (!g->term) {
+    st = dalloc(g, &g->term, (size_t)g->n);
+    if (st) return st;
+  }
+  if (g->pairs_cap < k) {
+    // grow the pair arrays (the old ones stay with the handle until destroy)
+    const int64_t cap = std::max<int64_t>(k, 2 * g->pairs_cap);
+    if ((st = dalloc(g, &g->pairs, (size_t)(2 * cap))) || (st = dalloc(g, &g->pair_flow, (size_t)cap))) return st;
+    g->pairs_cap = cap;
+  }
+  CK(cudaMemsetAsync(g->term, 0, (size_t)g->n, g->stream));
+  CK(cudaMemcpyAsync(g->pairs, sources, 4 * (size_t)k, cudaMemcpyHostToDevice, g->stream));
+  CK(cudaMemcpyAsync(g->pairs + k, sinks, 4 * (size_t)k, cudaMemcpyHostToDevice, g->stream));
+  set_terms<<<std::max(1, std::min(g->sms * 4, (2 * k + 255) / 256)), 256, 0, g->stream>>>(g->term, g->pairs, k);
+  CK(cudaGetLastError());
+  rc.mode = kModeFresh;
+  rc.term = g->term;
+  rc.sources = g->pairs;
+  rc.n_sources = k;
+  rc.sinks = g->pairs + k;
+  rc.n_sinks = k;
+  CK(cudaEventRecord(g->ev0, g->stream));
+  if (g->layout == WBPR_LAYOUT_RCSR) {
+    if (g->m) reset_rcsr<<<g->sms * 8, 256, 0, g->stream>>>(g->farc, g->fcb, g->fcap, g->m);
+  } else {
+    if (g->m) reset_bcsr<<<g->sms * 8, 256, 0, g->stream>>>(g->arc, g->arx, 2 * g->m);
+  }
+  CK(cudaGetLastError());
+  Stats hs;
+  float launch_ms = 0;
+  st = run(g, rc, &hs, &launch_ms);
+  CK(cudaEventRecord(g->ev1, g->stream));
+  CK(cudaEventSynchronize(g->ev1));
+  if (st) return st;
+  sink_flows<<<std::max(1, std::min(g->sms * 4, (k + 255) / 256)), 256, 0, g->stream>>>(g->e, g->pairs + k, k,
+                                                                                        g->pair_flow);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(flows, g->pair_flow, 8 * (size_t)k, cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  if (out) {
+    std::memset(out, 0, sizeof(*out));
+    int64_t total = 0;
+    for (int i = 0; i < k; ++i) total += flows[i];
+    out->flow = total;
+    CK(cudaEventElapsedTime(&out->solve_ms, g->ev0, g->ev1));
+    out->kernel_ms = (float)(hs.round_ns * 1e-6);
+    out->gr_ms = (float)(hs.gr_ns * 1e-6);
+    out->arcs_scanned = hs.arcs_scanned;
+    out->pushes = hs.pushes;
+    out->relabels = hs.relabels;
+    out->vertex_visits = hs.vertex_visits;
+    out->bfs_arcs = hs.bfs_arcs;
+    out->bfs_vertices = hs.bfs_vertices;
+    out->rounds = hs.rounds;
+    out->global_relabels = hs.grs;
+    out->stranded = hs.stranded;
+    out->alg_bytes = alg_bytes(g, hs);
+    out->launch_ms = launch_ms;
+    out->push_ms = (float)(hs.push_ns * 1e-6);
+    out->bfs_levels = hs.bfs_levels;
+    out->bfs_bottom_up_levels = hs.bu_levels;
   }
   return WBPR_OK;
 }

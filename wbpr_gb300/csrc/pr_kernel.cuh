@@ -316,11 +316,33 @@ struct Params {
   int bfs_dir;   // 0: vertices that reach the root (to sink); 1: reached from the root
   int bfs_root;
   int bfs_excl;  // vertex the BFS never labels (the source during a solve), or -1
+  // Terminal sets (nullptr: the single pair s, t above).  term[v] is 1 for a
+  // source, 2 for a sink; the preflow saturates every source's arcs, every
+  // sink absorbs excess and roots the global relabel.
+  const signed char* term = nullptr;
+  const int* sources = nullptr;
+  int n_sources = 0;
+  const int* sinks = nullptr;
+  int n_sinks = 0;
   long long* trace;  // optional event records {kind | aux << 32, t_ns, v0, v1, max, min}
   unsigned long long* bt;  // per-block work time of the current phase (trace only)
   unsigned long long* bt2; // per-block time of the heavy part of the push phase (trace only)
   int trace_cap;
 };
+
+template <class Topo>
+__device__ __forceinline__ bool is_sink(const Params<Topo>& p, int v) {
+  return p.term ? p.term[v] == 2 : v == p.t;
+}
+template <class Topo>
+__device__ __forceinline__ bool is_terminal(const Params<Topo>& p, int v) {
+  return p.term ? p.term[v] != 0 : (v == p.s || v == p.t);
+}
+// vertices the BFS never labels: the excluded vertex, and every source
+template <class Topo>
+__device__ __forceinline__ bool bfs_skip(const Params<Topo>& p, int v) {
+  return v == p.bfs_excl || (p.term && p.term[v] == 1);
+}
 
 // Optional event trace (written by global thread 0 only; count in Stats).
 enum TraceKind : int {
@@ -523,6 +545,8 @@ __device__ __forceinline__ void tile_discharge(const Params<Topo>& p, int u, int
           ++npush;
           if (dst[q] == p.t) {
             atomicAdd(&acc.sink, pushed);
+          } else if (p.term && p.term[dst[q]] == 2) {
+            atomicAdd(p.e + dst[q], pushed);  // one of several sinks: never filed
           } else {
             int old = atomicAdd(p.e + dst[q], pushed);
             if (old == 0) append(p.qraw, rawcnt, dst[q]);
@@ -698,6 +722,8 @@ __device__ __forceinline__ unsigned ordered_push(const Params<Topo>& p, const VR
           ++npush;
           if (dst[it] == p.t) {
             atomicAdd(&acc.sink, pushed);
+          } else if (p.term && p.term[dst[it]] == 2) {
+            atomicAdd(p.e + dst[it], pushed);
           } else {
             int old = atomicAdd(p.e + dst[it], pushed);
             if (old == 0) append(p.qraw, rawcnt, dst[it]);
@@ -1044,7 +1070,7 @@ __device__ __forceinline__ void td_batch(const Params<Topo>& p, const VRow& r, i
     }
   }
 #pragma unroll
-  for (int q = 0; q < 4; ++q) ok[q] = ok[q] && cf[q] > 0 && lv[q] == p.n && dst[q] != p.bfs_excl;
+  for (int q = 0; q < 4; ++q) ok[q] = ok[q] && cf[q] > 0 && lv[q] == p.n && !bfs_skip(p, dst[q]);
   // step 3: claim
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
@@ -1134,7 +1160,7 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      todo[q] = xs[q] >= 0 && xs[q] != p.bfs_excl && __ldcg(p.lab + xs[q]) == p.n;
+      todo[q] = xs[q] >= 0 && !bfs_skip(p, xs[q]) && __ldcg(p.lab + xs[q]) == p.n;
       if (xs[q] >= 0) ++verts;
     }
 #pragma unroll
@@ -1191,7 +1217,7 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
         x = __ldg(p.cls + p.n_light + i);
         ++verts;
       }
-      const bool open = x >= 0 && x != p.bfs_excl && __ldcg(p.lab + x) == p.n;
+      const bool open = x >= 0 && !bfs_skip(p, x) && __ldcg(p.lab + x) == p.n;
       VRow r;
       r.b0 = r.d0 = r.b1 = r.deg = 0;
       if (open) r = vrow(p.g, x);
@@ -1280,7 +1306,7 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
   for (int it = blockIdx.x; it < p.n_bch;) {
     const int4 ch = __ldg(p.bch + it);  // {vertex, segment, begin, end}
     if (threadIdx.x == 0) {
-      s_skip = (ch.x == p.bfs_excl || __ldcg(p.lab + ch.x) != p.n);
+      s_skip = (bfs_skip(p, ch.x) || __ldcg(p.lab + ch.x) != p.n);
       s_item = (int)gridDim.x + atomicAdd(&c->bfs_heavy_next[cur3], 1);
     }
     __syncthreads();
@@ -1343,10 +1369,14 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
   Ctl* c = p.ctl;
   const int lane = threadIdx.x & 31;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
-  for (int v = gt; v < p.n; v += gs) p.lab[v] = (v == root) ? 0 : p.n;
+  // root < 0: every sink of the terminal sets is a root
+  for (int v = gt; v < p.n; v += gs) p.lab[v] = (root >= 0 ? v == root : is_sink(p, v)) ? 0 : p.n;
   if (gt == 0) {
-    const int d = p.g.deg(root);
-    if (d > kTdHeavy) {
+    const int d = root >= 0 ? p.g.deg(root) : 0;
+    if (root < 0) {
+      c->fhcount[0] = 0;
+      c->fcount[0] = 0;
+    } else if (d > kTdHeavy) {
       const int nch = (d + kTdChunk - 1) / kTdChunk;
       for (int j = 0; j < nch; ++j) p.frh[0][j] = make_int2(root, j);
       c->fhcount[0] = nch;
@@ -1374,6 +1404,19 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
     }
   }
   if (!grid_sync(c, p.bar_timeout_ns)) return false;
+  if (root < 0) {  // the sinks form level 0
+    for (int base = gt - lane; base < p.n_sinks; base += gs) {
+      const int i = base + lane;
+      const int v = i < p.n_sinks ? __ldg(p.sinks + i) : -1;
+      warp_frontier(p, &c->fcount[0], &c->fhcount[0], 0, v, v >= 0, acc);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && acc.fdeg) {
+      atomicAdd((unsigned long long*)&c->fdeg[0], (unsigned long long)acc.fdeg);
+      acc.fdeg = 0;
+    }
+    if (!grid_sync(c, p.bar_timeout_ns)) return false;
+  }
   // Every block derives the direction from values that are final at the
   // barrier (frontier size and arcs of this level), so all blocks agree.
   bool bu = false, prev_bu = false;
@@ -1434,7 +1477,7 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
       bool pred = false;
       if (i < nall) {
         v = __ldg(p.cls + i);
-        if (v != p.s && v != p.t) {
+        if (!is_terminal(p, v)) {
           ev = ldv(p.e + v);
           pred = ev > 0 && __ldcg(p.lab + v) < p.n;
         }
@@ -1479,15 +1522,33 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
     if (!grid_sync(c, p.bar_timeout_ns)) return;
     // preflow: saturate every residual arc out of s (reference preflow.cu:3-31,
     // with excess accumulated so parallel source arcs are kept)
-    for (int k = 0; k < Topo::kSeg; ++k) {
-      int b, e;
-      p.g.seg(p.s, k, b, e);
-      for (int a = b + gt; a < e; a += gs) {
-        int dst, cf;
-        p.g.load(k, a, dst, cf);
-        if (cf > 0 && dst != p.s) {
-          p.g.push(k, a, cf, cf);
-          atomicAdd(p.e + dst, cf);
+    if (p.term) {  // terminal sets: a block per source
+      for (int i = blockIdx.x; i < p.n_sources; i += gridDim.x) {
+        const int src = __ldg(p.sources + i);
+        for (int k = 0; k < Topo::kSeg; ++k) {
+          int b, e;
+          p.g.seg(src, k, b, e);
+          for (int a = b + threadIdx.x; a < e; a += blockDim.x) {
+            int dst, cf;
+            p.g.load(k, a, dst, cf);
+            if (cf > 0 && p.term[dst] != 1) {
+              p.g.push(k, a, cf, cf);
+              atomicAdd(p.e + dst, cf);
+            }
+          }
+        }
+      }
+    } else {
+      for (int k = 0; k < Topo::kSeg; ++k) {
+        int b, e;
+        p.g.seg(p.s, k, b, e);
+        for (int a = b + gt; a < e; a += gs) {
+          int dst, cf;
+          p.g.load(k, a, dst, cf);
+          if (cf > 0 && dst != p.s) {
+            p.g.push(k, a, cf, cf);
+            atomicAdd(p.e + dst, cf);
+          }
         }
       }
     }
@@ -1507,7 +1568,7 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
   for (;;) {
     if (need_gr) {
       const unsigned long long t0 = gtime();
-      if (!bfs<Topo, 0>(p, p.t, true, cur, acc)) break;
+      if (!bfs<Topo, 0>(p, p.term ? -1 : p.t, true, cur, acc)) break;
       if (threadIdx.x == 0 && blockIdx.x == 0) {
         gr_end = gtime();
         gr_last = gr_end - t0;
@@ -1557,7 +1618,7 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
       }
     }
     TRACE_BLOCK(p, tb);
-    flush_sink(p.e + p.t, acc);
+    if (p.t >= 0) flush_sink(p.e + p.t, acc);
     flush_work(acc, c, raw);
     if (!grid_sync(c, p.bar_timeout_ns)) break;
     if (gt == 0) {
@@ -1605,7 +1666,7 @@ __global__ void count_stranded(Params<Topo> p) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   int cnt = 0;
   for (int v = gt; v < p.n; v += gs)
-    if (v != p.s && v != p.t && p.e[v] > 0 && p.lab[v] >= p.n) ++cnt;
+    if (!is_terminal(p, v) && p.e[v] > 0 && p.lab[v] >= p.n) ++cnt;
   if (cnt) atomicAdd(&p.st->stranded, cnt);
 }
 
