@@ -216,3 +216,18 @@ def test_rmat20_certificate():
         r = d.solve("vc", g.s, g.t)
         rep = d.verify()
         assert rep["ok"] and rep["cut_value"] == r.flow == expected
+
+
+def test_long_path_is_not_relabel_bound():
+    """One unit of excess walks a 20,000-vertex path one arc per round; the
+    global relabel (20,000 BFS levels) must not run every few rounds."""
+    n = 20000
+    tail = np.arange(n - 1)
+    cap = np.full(n - 1, 2)
+    cap[0] = 1
+    g = W.Graph.from_arcs(n, tail, tail + 1, cap, 0, n - 1)
+    with W.DeviceGraph(g, "bcsr") as d:
+        r = d.solve("vc", 0, n - 1)
+        assert r.flow == 1
+        assert r.solve_ms < 5000.0, r.solve_ms
+        assert d.verify()["ok"]

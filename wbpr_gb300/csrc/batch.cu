@@ -96,7 +96,8 @@ struct BlockCtl {
   int qraw_count[2];
   int fcount[2];
   int item;
-  int stop;  // budget exhausted (decided by thread 0, read after a barrier)
+  int stop;   // budget exhausted (decided by thread 0, read after a barrier)
+  int gr_ok;  // rounds since the last global relabel took >= half its time
 };
 
 // Block-level BFS from t over residual arcs (top-down, warp per frontier
@@ -210,9 +211,15 @@ __global__ void __launch_bounds__(512, 2) pr_batch(BatchParams bp) {
     int cur = 0, raw = 0, rounds = 0, since = 0;
     unsigned long long work = 0;
     bool need_gr = true, failed = false;
+    unsigned long long gr_end = 0, gr_len = 0;  // thread 0 only
     for (;;) {
       if (need_gr) {
+        const unsigned long long g0 = gtime();
         batch_bfs(p, in.vbase, fr0, fr1, bc, acc);
+        if (threadIdx.x == 0) {
+          gr_end = gtime();
+          gr_len = gr_end - g0;
+        }
         if (threadIdx.x == 0) {
           bc.lcount[1] = 0;
           bc.qraw_count[0] = bc.qraw_count[1] = 0;
@@ -278,14 +285,18 @@ __global__ void __launch_bounds__(512, 2) pr_batch(BatchParams bp) {
         if (rl) atomicAdd(&acc.relabels, rl);
       }
       __syncthreads();
-      if (threadIdx.x == 0) bc.qraw_count[raw] = 0;
+      if (threadIdx.x == 0) {
+        bc.qraw_count[raw] = 0;
+        bc.gr_ok = 2 * (gtime() - gr_end) >= gr_len;
+      }
       work += acc.scanned + acc.visits - w0;
       __syncthreads();
       ++rounds;
       ++since;
       cur ^= 1;
       raw ^= 1;
-      if (work > gr_thr || since >= bp.gr_rounds) need_gr = true;
+      // relabel triggers balanced against relabel time, as in the one-instance solver
+      if ((work > gr_thr || since >= bp.gr_rounds) && bc.gr_ok) need_gr = true;
     }
     if (threadIdx.x == 0) {
       bp.flows[id] = failed ? -1 : (long long)ldv(bp.e + in.t);

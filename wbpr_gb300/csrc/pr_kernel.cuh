@@ -1645,11 +1645,12 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
     // Work-based trigger (Cherkassky-Goldberg) plus a round cap: tails where
     // a few stranded vertices ping-pong excess do little work per round
     // while their labels climb towards n two at a time.
-    // The work trigger waits until the rounds since the last relabel have
-    // taken at least half as long as that relabel did, so relabelling stays
-    // at most about two thirds of the time on graphs whose BFS is deep
-    // (512 x 512 grids: 38 -> 27 ms).
-    if ((work > p.gr_threshold && ldv(&c->gr_ok)) || since_gr >= p.gr_rounds) need_gr = true;
+    // Both triggers wait until the rounds since the last relabel have taken
+    // at least half as long as that relabel did, so relabelling stays at
+    // most about two thirds of the time on graphs whose BFS is deep (512 x
+    // 512 grids: 38 -> 27 ms; a 20,000-vertex path whose one unit of excess
+    // walks 20,000 rounds: 60 s of relabels every 48 rounds without it).
+    if ((work > p.gr_threshold || since_gr >= p.gr_rounds) && ldv(&c->gr_ok)) need_gr = true;
   }
   flush_acc(acc, p.st);
   if (gt == 0) {
