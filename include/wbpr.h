@@ -96,9 +96,10 @@ typedef struct wbpr_tuning {
   int32_t verify;        /* 1: run the device certificate check after the solve  */
   int32_t trace;         /* 1: record a per-level / per-phase event trace         */
   int32_t gr_rounds;     /* also relabel globally after this many rounds (0 = 48) */
-  int32_t grid_blocks;   /* blocks of the persistent grid (0 = auto: one block,   */
-                         /* with block-local barriers, when n + arcs <= 16384;    */
-                         /* otherwise every SM x blocks_per_sm)                   */
+  int32_t grid_blocks;   /* blocks of the persistent grid (0 = auto by size:      */
+                         /* n + arcs <= 16384: one block, block barriers only;    */
+                         /* <= 2^21: SMs / 2; <= 2^22: SMs; <= 2^24: 2 x SMs;     */
+                         /* larger: every SM x blocks_per_sm)                     */
 } wbpr_tuning;
 
 typedef struct wbpr_result {

@@ -1143,8 +1143,18 @@ wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch
   }
   const int bps = rc.blocks_per_sm > 0 ? std::min(occ, rc.blocks_per_sm) : occ;
   int blocks = g->sms * bps;
-  if (rc.grid_blocks > 0) blocks = std::min(blocks, rc.grid_blocks);
-  else if ((int64_t)g->n + g->total_deg <= kOneBlockUnits) blocks = 1;
+  if (rc.grid_blocks > 0) {
+    blocks = std::min(blocks, rc.grid_blocks);
+  } else {
+    // Smaller graphs run on fewer blocks: their rounds and BFS levels are
+    // latency-bound, and fewer blocks make every phase's barrier and idle
+    // block cheaper.  Bands measured on GB300 (GENRMF, layered, grids, R-MAT).
+    const int64_t units = (int64_t)g->n + g->total_deg;
+    if (units <= kOneBlockUnits) blocks = 1;
+    else if (units <= (int64_t)1 << 21) blocks = std::min(blocks, std::max(1, g->sms / 2));
+    else if (units <= (int64_t)1 << 22) blocks = std::min(blocks, g->sms);
+    else if (units <= (int64_t)1 << 24) blocks = std::min(blocks, 2 * g->sms);
+  }
   CK(cudaMemsetAsync(g->ctl, 0, sizeof(Ctl), g->stream));
   CK(cudaMemsetAsync(g->st, 0, sizeof(Stats), g->stream));
   CK(cudaEventRecord(g->ev2, g->stream));
