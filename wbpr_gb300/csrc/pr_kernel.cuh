@@ -1147,34 +1147,37 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   const int gw = gt >> 5, nwarps = gs >> 5;
   unsigned long long arcs = 0, verts = 0, found = 0, fdeg = 0;
-  // short rows (<= kLightDeg): a thread each; 4 rows advance together, 4 arcs
-  // of each in flight per step
-  for (int i0 = gt; i0 < p.n_light; i0 += 4 * gs) {
-    int xs[4];
-    bool todo[4];
-    VRow rr[4];
+  // short rows (<= kLightDeg): a thread each; kBuRows rows advance together,
+  // kBuArcs arcs of each in flight per step
+  constexpr int kBuRows = 4, kBuArcs = 4;
+  for (int i0 = gt; i0 < p.n_light; i0 += kBuRows * gs) {
+    int xs[kBuRows];
+    bool todo[kBuRows];
+    VRow rr[kBuRows];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < kBuRows; ++q) {
       const int i = i0 + q * gs;
       xs[q] = i < p.n_light ? __ldg(p.cls + i) : -1;
     }
+    bool any = false;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < kBuRows; ++q) {
       todo[q] = xs[q] >= 0 && !bfs_skip(p, xs[q]) && __ldcg(p.lab + xs[q]) == p.n;
       if (xs[q] >= 0) ++verts;
+      any |= todo[q];
     }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < kBuRows; ++q) {
       rr[q].b0 = rr[q].d0 = rr[q].b1 = rr[q].deg = 0;
       if (todo[q]) rr[q] = vrow(p.g, xs[q]);
     }
 #pragma unroll 1
-    for (int v0 = 0; todo[0] || todo[1] || todo[2] || todo[3]; v0 += 4) {
-      int dst[4][4], cf[4][4];
+    for (int v0 = 0; any; v0 += kBuArcs) {
+      int dst[kBuRows][kBuArcs], cf[kBuRows][kBuArcs];
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
+      for (int q = 0; q < kBuRows; ++q)
 #pragma unroll
-        for (int w = 0; w < 4; ++w) {
+        for (int w = 0; w < kBuArcs; ++w) {
           cf[q][w] = 0;
           dst[q][w] = 0;
           if (todo[q] && v0 + w < rr[q].deg) {
@@ -1185,18 +1188,20 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
             ++arcs;
           }
         }
+      any = false;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < kBuRows; ++q) {
         bool hit = false;
 #pragma unroll
-        for (int w = 0; w < 4; ++w)
+        for (int w = 0; w < kBuArcs; ++w)
           if (cf[q][w] > 0 && __ldcg(p.lab + dst[q][w]) == level) hit = true;
         if (todo[q] && hit) {
           p.lab[xs[q]] = level + 1;
           ++found;
           fdeg += (unsigned long long)rr[q].deg;
         }
-        if (hit || v0 + 4 >= rr[q].deg) todo[q] = false;
+        if (hit || v0 + kBuArcs >= rr[q].deg) todo[q] = false;
+        any |= todo[q];
       }
     }
   }
