@@ -208,14 +208,28 @@ def test_sparse_work_tail_terminates():
             assert r.flow == expected, tune
 
 
-def test_rmat20_certificate():
-    """Size-independent property at a large size: the device certificate."""
+@pytest.mark.parametrize("layout", ["bcsr", "rcsr"])
+def test_rmat20_certificate(layout):
+    """Size-independent property at a large size, where hub rows take the
+    chunked deep passes in both layouts: the device certificate, and the
+    completed flow conserving flow exactly."""
     g = W.gen_rmat(20, 16, seed=1)
     expected = oracle.fifo_pr(g.n, g.off, g.dst, g.cap, g.s, g.t)
-    with W.DeviceGraph(g, "bcsr") as d:
-        r = d.solve("vc", g.s, g.t)
-        rep = d.verify()
-        assert rep["ok"] and rep["cut_value"] == r.flow == expected
+    with W.DeviceGraph(g, layout) as d:
+        for algo in ("vc", "tc"):
+            r = d.solve(algo, g.s, g.t)
+            rep = d.verify()
+            assert rep["ok"] and rep["label_violations"] == 0 and rep["cut_value"] == r.flow == expected
+        d.complete_flow()
+        _, e, f = d.read_state()
+        inner = np.ones(g.n, bool)
+        inner[[g.s, g.t]] = False
+        assert np.all(e[inner] == 0)
+        tails = np.repeat(np.arange(g.n), np.diff(g.off))
+        net = np.zeros(g.n, np.int64)
+        np.add.at(net, tails, -f.astype(np.int64))
+        np.add.at(net, g.dst, f.astype(np.int64))
+        assert np.all(net[inner] == 0) and net[g.t] == expected
 
 
 def test_long_path_is_not_relabel_bound():
