@@ -292,3 +292,31 @@ def test_bipartite_network_shape():
         with pytest.raises(W.WbprError) as ei:
             W.bipartite_network(3, 2, left, right)
         assert ei.value.status == 1
+
+
+def test_header_is_plain_c_and_links(tmp_path):
+    """A C99 caller (the reference's host code is C-style) compiles against
+    include/wbpr.h and links libwbpr.so; calls with bad arguments return
+    status codes instead of exiting."""
+    src = tmp_path / "caller.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include "wbpr.h"
+int main(void) {
+  wbpr_tuning tu;
+  wbpr_graph* g = 0;
+  wbpr_default_tuning(&tu);
+  if (wbpr_graph_create(0, WBPR_LAYOUT_BCSR, &g) != WBPR_ERR_INVALID_ARG) return 1;
+  if (wbpr_solve(0, 0, 1, WBPR_ALGO_VC, &tu, 0) != WBPR_ERR_INVALID_ARG) return 2;
+  if (wbpr_read_dimacs("/nonexistent/file", 0) == WBPR_OK) return 3;
+  printf("abi %d tile %d gr_alpha %.2f\n", wbpr_abi_version(), tu.tile, tu.gr_alpha);
+  return 0;
+}
+""")
+    exe = tmp_path / "caller"
+    inc = os.path.join(ROOT, "include")
+    libdir = os.path.dirname(wb.LIB)
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", inc, str(src),
+                    "-L", libdir, "-lwbpr", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.startswith("abi "), (r.returncode, r.stdout, r.stderr)
