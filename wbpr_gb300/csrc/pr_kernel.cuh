@@ -939,12 +939,13 @@ __device__ __forceinline__ void warp_append(int* q, int* cnt, int v, bool pred) 
 
 // Warp-level filing of active vertices (all 32 lanes call it).
 template <class Topo>
-__device__ __forceinline__ void warp_file(const Params<Topo>& p, int nxt, int u, int eu, bool pred) {
+__device__ __forceinline__ void warp_file(const Params<Topo>& p, int nxt, int u, int eu, bool pred,
+                                         int dpre = -1) {
   Ctl* c = p.ctl;
   bool light = false;
   if (pred) {
     p.esnap[u] = eu;
-    light = p.g.deg(u) <= p.heavy_deg;
+    light = (dpre >= 0 ? dpre : p.g.deg(u)) <= p.heavy_deg;
   }
   warp_append(p.lq[nxt], &c->lcount[nxt], u, pred && light);
   warp_append(p.hq[nxt], &c->hcount[nxt], u, pred && !light);
@@ -961,15 +962,18 @@ __device__ void relabel_phase(const Params<Topo>& p, int cur, int nxt, int raw, 
   unsigned long long rl = 0;
   for (int base = gt - lane; base < nq; base += gs) {
     const int i = base + lane;
-    int u = -1, eu = 0, hu = p.n;
+    int u = -1, eu = 0, hu = p.n, du = 0;
     if (i < nq) {
       u = __ldcg(p.qraw + i);
+      // every load that depends only on u in one step
       int m = __ldcg(p.rl_min + u);
       hu = __ldcg(p.lab + u);
       eu = ldv(p.e + u);
+      const int left = __ldcg(p.rl_left + u);
+      du = p.g.deg(u);
       if (m != kNone) {
         p.rl_min[u] = kNone;
-        if (eu > __ldcg(p.rl_left + u) && hu + 1 < m) m = hu + 1;
+        if (eu > left && hu + 1 < m) m = hu + 1;
         int nh = (m >= p.n - 1) ? p.n : m + 1;
         if (nh <= hu) nh = hu + 1;
         if (nh > p.n) nh = p.n;
@@ -978,7 +982,7 @@ __device__ void relabel_phase(const Params<Topo>& p, int cur, int nxt, int raw, 
         ++rl;
       }
     }
-    warp_file(p, nxt, u, eu, u >= 0 && eu > 0 && hu < p.n);
+    warp_file(p, nxt, u, eu, u >= 0 && eu > 0 && hu < p.n, du);
   }
   if (rl) atomicAdd(&acc.relabels, rl);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
