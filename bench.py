@@ -505,20 +505,25 @@ def config4(args):
         adj.append(ms0 + ms1)
         flows.append(r.flow)
         if sd == 0:
+            # +-1 re-solves on one handle: only the capacities change
             rng = np.random.default_rng(0)
+            fd = W.DeviceGraph(g, "bcsr")
             for e in rng.choice(g.m, min(g.m, args.fd_arcs), replace=False):
                 up = g.cap.copy()
                 up[e] += 1
-                dp = W.maxflow(W.Graph(g.n, g.off, g.dst, up, g.s, g.t)) - r.flow
+                fd.set_capacities(up)
+                dp = fd.solve("vc", g.s, g.t).flow - r.flow
                 dm = 0
                 if g.cap[e] > 0:
                     dn = g.cap.copy()
                     dn[e] -= 1
-                    dm = r.flow - W.maxflow(W.Graph(g.n, g.off, g.dst, dn, g.s, g.t))
+                    fd.set_capacities(dn)
+                    dm = r.flow - fd.solve("vc", g.s, g.t).flow
                 for ind in (i0, i1):
                     if not (dp <= ind[e] and (g.cap[e] == 0 or ind[e] <= dm)):
                         raise AssertionError(f"finite difference at arc {e}")
                 fd_checked += 1
+            fd.close()
     pct = 100.0 * sum(adj) / sum(fwd)
     _line("adjoint ms as % of forward solve (512x512 grids)", pct, "%", False,
           f"{grids} grids 512x512, 4-connected, seeds 0..{grids - 1}", steps=grids, warmup=args.warmup,

@@ -232,6 +232,12 @@ wbpr_status wbpr_graph_create(const wbpr_csr* g, wbpr_layout layout,
 wbpr_status wbpr_graph_destroy(wbpr_graph* g);
 /* Bytes of device memory held by the handle. */
 int64_t wbpr_graph_device_bytes(const wbpr_graph* g);
+/* Replace the m capacities (input order; host or device buffer) of a built
+ * graph without rebuilding it: the same topology with new capacities, e.g.
+ * the next frame of a graph-cut pipeline.  Checked first (capacities >= 0:
+ * INVALID_ARG; incoming sums within int32: OVERFLOW), and the graph is left
+ * unchanged when a check fails.  Takes effect at the next wbpr_solve. */
+wbpr_status wbpr_graph_set_capacities(wbpr_graph* g, const int32_t* capacities);
 /* Queue the handle's device work on the caller's stream (a cudaStream_t of
  * the handle's device; NULL returns to the handle's own stream).  Work queued
  * before the switch is finished first.  Calls still return once their

@@ -153,3 +153,28 @@ def test_single_graph_autotune():
             assert r.flow == v
             tc, _ = d.autotune("tc", g.s, g.t)
             assert tc.tile == 0
+
+
+@pytest.mark.parametrize("layout", ["bcsr", "rcsr"])
+def test_new_capacities_without_rebuild(layout):
+    g = W.gen_grid(40, 30, 2)
+    rng = np.random.default_rng(3)
+    with W.DeviceGraph(g, layout) as d:
+        assert d.solve("vc", g.s, g.t).flow == oracle.dinic(g.n, g.off, g.dst, g.cap, g.s, g.t)
+        for trial in range(3):
+            cap = rng.integers(0, 2000, g.m).astype(np.int32)
+            d.set_capacities(cap)
+            v = oracle.dinic(g.n, g.off, g.dst, cap, g.s, g.t)
+            r = d.solve("vc", g.s, g.t)
+            assert r.flow == v and d.verify()["ok"]
+        # rejected updates leave the graph as it was
+        bad = cap.copy()
+        bad[5] = -1
+        with pytest.raises(W.WbprError) as ei:
+            d.set_capacities(bad)
+        assert ei.value.status == 1
+        big = np.full(g.m, 2**30, np.int32)
+        with pytest.raises(W.WbprError) as ei:
+            d.set_capacities(big)
+        assert ei.value.status == 4
+        assert d.solve("tc", g.s, g.t).flow == v

@@ -86,7 +86,7 @@ EXPORTED = [
     "wbpr_host_csr_copy", "wbpr_host_csr_free",
     "wbpr_gen_genrmf", "wbpr_gen_rmat", "wbpr_gen_bipartite", "wbpr_gen_layered", "wbpr_gen_grid",
     "wbpr_build_rcsr", "wbpr_build_bcsr", "wbpr_build_bcsr2", "wbpr_graph_create",
-    "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_graph_read_bcsr", "wbpr_graph_read_rcsr", "wbpr_graph_set_stream", "wbpr_autotune", "wbpr_solve_pairs", "wbpr_solve", "wbpr_read_state",
+    "wbpr_graph_destroy", "wbpr_graph_device_bytes", "wbpr_graph_read_bcsr", "wbpr_graph_read_rcsr", "wbpr_graph_set_stream", "wbpr_graph_set_capacities", "wbpr_autotune", "wbpr_solve_pairs", "wbpr_solve", "wbpr_read_state",
     "wbpr_verify", "wbpr_mincut_adjoint", "wbpr_rcsr_preflow", "wbpr_rcsr_push_relabel",
     "wbpr_read_trace", "wbpr_solve_bcsr_noalloc", "wbpr_batch_create", "wbpr_batch_destroy",
     "wbpr_batch_device_bytes", "wbpr_batch_solve", "wbpr_batch_instance_stats", "wbpr_batch_autotune",
@@ -143,6 +143,7 @@ def lib() -> C.CDLL:
         "wbpr_graph_read_bcsr": (C.c_int, [vp, _i32p, _i32p, _i32p, _i32p]),
         "wbpr_graph_read_rcsr": (C.c_int, [vp, _i32p, _i32p, _i32p]),
         "wbpr_graph_set_stream": (C.c_int, [vp, vp]),
+        "wbpr_graph_set_capacities": (C.c_int, [vp, _i32p]),
         "wbpr_solve_pairs": (C.c_int, [vp, C.c_int32, _i32p, _i32p, C.c_int, C.POINTER(Tuning),
                                        C.POINTER(C.c_int64), C.POINTER(Result)]),
         "wbpr_autotune": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_float)]),
@@ -488,6 +489,13 @@ class DeviceGraph:
         _check(lib().wbpr_autotune(self._h, -1 if s is None else s, -1 if t is None else t, ALGOS[algo],
                                    C.byref(tu), C.byref(ms)), "wbpr_autotune")
         return tu, float(ms.value)
+
+    def set_capacities(self, cap) -> None:
+        """New capacities (input order) for the same topology; used by the next solve."""
+        c = np.ascontiguousarray(cap, np.int32)
+        if c.shape != (self.m,):
+            raise ValueError("one capacity per input arc")
+        _check(lib().wbpr_graph_set_capacities(self._h, _p(c) if self.m else None), "wbpr_graph_set_capacities")
 
     def set_stream(self, stream: int | None) -> None:
         """Queue this graph's device work on a caller's CUDA stream (a raw

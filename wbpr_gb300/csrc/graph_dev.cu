@@ -51,6 +51,7 @@ struct wbpr_graph {
   int* pairs = nullptr;  // sources then sinks
   int64_t pairs_cap = 0;
   long long* pair_flow = nullptr;
+  int* cap_tmp = nullptr;  // staging for wbpr_graph_set_capacities
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   // BCSR16
   int* row = nullptr;
@@ -360,6 +361,41 @@ __global__ void flow_kernel(const int* ioff, const int* row, const int2* arc, co
       flow[i] = arx[a].y - arc[a].y;
     }
   }
+}
+
+// New capacities, in input order, for a built graph: pass 0 checks them
+// (non-negative; incoming sums per head within int32, summed into incap),
+// pass 1 writes them (BCSR forward slots' arx.y, RCSR fcap).
+__global__ void caps_kernel(const int* ioff, const int* row, const int2* arc, int2* arx, const int2* farc,
+                            int* fcap, const int* cap, int n, long long m, int pass, unsigned long long* incap,
+                            unsigned long long* bad) {
+  const int lane = threadIdx.x & 31;
+  bool b = false;
+  FOR_TILES(m) {
+    const TileRows tr = row ? tile_rows(ioff, n, base, m) : TileRows{0, 0};
+    for (int k = 0; k < kTile / 32; ++k) {
+      const long long i = base + k * 32 + lane;
+      if (i >= m) break;
+      const int c = cap[i];
+      int a = -1, v;
+      if (row) {
+        const int u = row_search(ioff, i, tr.lo, tr.hi);
+        a = row[u] + (int)(i - ioff[u]);
+        v = arc[a].x;
+      } else {
+        v = farc[i].x;
+      }
+      if (pass == 0) {
+        if (c < 0) b = true;
+        else if (c > 0) atomicAdd(incap + v, (unsigned long long)c);
+      } else if (row) {
+        arx[a].y = c;
+      } else {
+        fcap[i] = c;
+      }
+    }
+  }
+  if (__any_sync(0xffffffffu, b) && lane == 0) atomicOr(bad, 1ull);
 }
 
 // ---------------------------------------------------------------------------
@@ -1302,6 +1338,43 @@ wbpr_status wbpr_autotune(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, w
         }
       }
   if (best_ms) *best_ms = bms;
+  return WBPR_OK;
+}
+
+wbpr_status wbpr_graph_set_capacities(wbpr_graph* g, const int32_t* capacities) {
+  NvtxRange nvtx_("wbpr_graph_set_capacities");
+  if (!g || (g->m > 0 && !capacities)) return WBPR_ERR_INVALID_ARG;
+  if (g->m == 0) return WBPR_OK;
+  CK(cudaSetDevice(g->device));
+  const size_t m = (size_t)g->m, n = (size_t)g->n;
+  if (!g->cap_tmp) {
+    wbpr_status st = dalloc(g, &g->cap_tmp, m + 2 * (n + 1) + 8);
+    if (st) return st;
+  }
+  int* dcap = g->cap_tmp;
+  auto* incap = (unsigned long long*)(g->cap_tmp + ((m + 1) & ~(size_t)1));
+  unsigned long long* chk = incap + n + 1;  // [0] bad, [1] max incoming sum
+  cudaPointerAttributes pa;
+  const bool on_device = cudaPointerGetAttributes(&pa, capacities) == cudaSuccess &&
+                         (pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged);
+  cudaGetLastError();
+  CK(cudaMemcpyAsync(dcap, capacities, 4 * m, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                     g->stream));
+  CK(cudaMemsetAsync(incap, 0, 8 * (n + 1) + 16, g->stream));
+  const bool bcsr = g->layout == WBPR_LAYOUT_BCSR;
+  caps_kernel<<<g->sms * 8, 256, 0, g->stream>>>(g->ioff, bcsr ? g->row : nullptr, g->arc, g->arx, g->farc, g->fcap,
+                                                dcap, g->n, g->m, 0, incap, chk);
+  db_max<<<g->sms * 8, 256, 0, g->stream>>>(incap, g->n, chk + 1);
+  CK(cudaGetLastError());
+  unsigned long long h[2] = {0, 0};
+  CK(cudaMemcpyAsync(h, chk, 16, cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  if (h[0]) return WBPR_ERR_INVALID_ARG;
+  if (h[1] > 0x7fffffffull) return WBPR_ERR_OVERFLOW;
+  caps_kernel<<<g->sms * 8, 256, 0, g->stream>>>(g->ioff, bcsr ? g->row : nullptr, g->arc, g->arx, g->farc, g->fcap,
+                                                dcap, g->n, g->m, 1, incap, chk);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(g->stream));
   return WBPR_OK;
 }
 
