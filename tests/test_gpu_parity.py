@@ -115,6 +115,36 @@ def test_read_state_conservation():
         assert e[g.t] == r.flow
 
 
+@pytest.mark.parametrize("layout", ["bcsr", "rcsr"])
+def test_labels_after_repeated_global_relabels(layout):
+    """A global relabel marks the vertices that cannot reach the sink and
+    later relabels of the same solve skip them: with a relabel forced every
+    round the flow stays exact, every label read back lies in [0, n], and
+    every vertex that can reach the sink is labelled below n."""
+    graphs = [W.gen_rmat(15, 8, seed=9), W.gen_bipartite(20000, 20000, 2.0, 256, 3),
+              W.gen_genrmf(8, 16, 1, 10000, 5)]
+    most = 0
+    for g in graphs:
+        v = oracle.dinic(g.n, g.off, g.dst, g.cap, g.s, g.t)
+        with W.DeviceGraph(g, layout) as d:
+            for gr_rounds in (1, 4):
+                r = d.solve("vc", g.s, g.t, gr_rounds=gr_rounds)
+                assert r.flow == v
+                most = max(most, r.global_relabels)
+                h, e, f = d.read_state()
+                assert h.min() >= 0 and h.max() <= g.n
+                reach = d.cut_sides(0).astype(bool)
+                assert (h[reach] < g.n).all()
+                assert d.verify()["ok"]
+            d.complete_flow()
+            h, e, f = d.read_state()
+            assert h.min() >= 0 and h.max() <= g.n
+            inner = np.ones(g.n, bool)
+            inner[[g.s, g.t]] = False
+            assert np.all(e[inner] == 0)
+    assert most >= 3
+
+
 @pytest.mark.parametrize("algo", [0, 1])
 def test_reference_dropin(algo, golden):
     for c in golden[:20]:

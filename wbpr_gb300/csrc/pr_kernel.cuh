@@ -76,8 +76,9 @@ struct Ctl {
   int bu_found[3];  // vertices labelled by a bottom-up level, by level % 3
   int mcount;       // materialised frontier: short rows
   int mhcount;      //   long-row chunk items
-  alignas(128) int gr_ok;
-  int viol;  // out-of-range indices seen by the checked build  // rounds since the last global relabel took at least half as long as it
+  alignas(128) int gr_ok;  // the rounds since the last global relabel took at least half as long as it
+  int viol;                // out-of-range indices seen by the checked build
+  long long dead_deg;      // arcs of the vertices global relabels marked unable to reach the sink
   // work done in rounds of even / odd parity; block b adds to slot b % 32
   alignas(128) unsigned long long work[2][kWorkSlots * 16];
 };
@@ -1031,6 +1032,45 @@ __device__ __forceinline__ void warp_frontier(const Params<Topo>& p, int* fcnt, 
   if ((threadIdx.x & 31) == 0 && sd) atomicAdd((unsigned long long*)&acc.fdeg, sd);
 }
 
+// warp_frontier for four candidates per lane (v[q] with pred[q], degree
+// d[q]): one counter atomic per warp for all short rows, one degree sum.
+template <class Topo>
+__device__ __forceinline__ void warp_frontier4(const Params<Topo>& p, int* fcnt, int* fhcnt, int fn,
+                                               const int* v, const bool* pred, const int* d, BlockAcc& acc) {
+  const int lane = threadIdx.x & 31;
+  int nshort = 0;
+  unsigned long long sd = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    if (!pred[q]) continue;
+    sd += (unsigned long long)d[q];
+    if (d[q] <= kTdHeavy) {
+      ++nshort;
+    } else {
+      const int nch = (d[q] + kTdChunk - 1) / kTdChunk;
+      const int base = atomicAdd(fhcnt, nch);
+      for (int j = 0; j < nch; ++j) p.frh[fn][base + j] = make_int2(v[q], j);
+    }
+  }
+  int incl = nshort;  // inclusive scan of the short-row counts over the warp
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  if (total) {
+    int base = 0;
+    if (lane == 31) base = atomicAdd(fcnt, total);
+    base = __shfl_sync(0xffffffffu, base, 31) + incl - nshort;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (pred[q] && d[q] <= kTdHeavy) p.fr[fn][base++] = v[q];
+  }
+  for (int o = 16; o > 0; o >>= 1) sd += __shfl_down_sync(0xffffffffu, sd, o);
+  if (lane == 0 && sd) atomicAdd((unsigned long long*)&acc.fdeg, sd);
+}
+
 // Top-down step over arcs [base, base + 128) of virtual row r (4 arcs per
 // lane in flight); all 32 lanes call it.
 template <class Topo, int DIR>
@@ -1075,12 +1115,11 @@ __device__ __forceinline__ void td_batch(const Params<Topo>& p, const VRow& r, i
   }
 #pragma unroll
   for (int q = 0; q < 4; ++q) ok[q] = ok[q] && cf[q] > 0 && lv[q] == p.n && !bfs_skip(p, dst[q]);
-  // step 3: claim
+  // step 3: claim, the four CAS of a lane in flight together
+  bool won[4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const bool won = ok[q] && atomicCAS(p.lab + dst[q], p.n, level + 1) == p.n;
-    warp_frontier(p, &p.ctl->fcount[fn], &p.ctl->fhcount[fn], fn, dst[q], won, acc, dg[q]);
-  }
+  for (int q = 0; q < 4; ++q) won[q] = ok[q] && atomicCAS(p.lab + dst[q], p.n, level + 1) == p.n;
+  warp_frontier4(p, &p.ctl->fcount[fn], &p.ctl->fhcount[fn], fn, dst, won, dg, acc);
 }
 
 // does the arc a of row x make x adjacent to a vertex labelled `level`?
@@ -1103,11 +1142,16 @@ __device__ void bfs_top_down(const Params<Topo>& p, int level, int nf, int nfh, 
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   unsigned long long arcs = 0;
-  // chunk items of long rows: a warp per 1024-arc chunk
-  for (int i = gw; i < nfh; i += nwarps) {
-    const int2 it = __ldcg(p.frh[fc] + i);
+  // chunk items of long rows: a warp per 1024-arc chunk, or per part of one
+  // when the level has few of them (the sink's own row at level 0: a warp
+  // walking 1024 arcs is 8 dependent steps; 8 parts of 128 arcs take one)
+  int S = 1;
+  while (S < 8 && 2LL * nfh * S <= nwarps) S <<= 1;
+  const int part = kTdChunk / S;
+  for (int i = gw; i < nfh * S; i += nwarps) {
+    const int2 it = __ldcg(p.frh[fc] + i / S);
     const VRow r = vrow(p.g, it.x);
-    const int lo = it.y * kTdChunk, hi = min(r.deg, lo + kTdChunk);
+    const int lo = it.y * kTdChunk + (i % S) * part, hi = min(r.deg, lo + part);
     for (int b = lo; b < hi; b += 128) td_batch<Topo, DIR>(p, r, b, hi, level, fn, acc, arcs);
   }
   // short rows (<= kTdHeavy arcs): a warp per row
@@ -1374,12 +1418,20 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
 // `queues` is set, the active lists `cur` are rebuilt from the new labels
 // (vertices with excess and label < n, other than s and t).
 template <class Topo, int DIR>
-__device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, BlockAcc& acc) {
+__device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, BlockAcc& acc,
+                    bool keep_dead = false) {
   Ctl* c = p.ctl;
   const int lane = threadIdx.x & 31;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
-  // root < 0: every sink of the terminal sets is a root
-  for (int v = gt; v < p.n; v += gs) p.lab[v] = (root >= 0 ? v == root : is_sink(p, v)) ? 0 : p.n;
+  // root < 0: every sink of the terminal sets is a root.  With keep_dead,
+  // vertices an earlier global relabel of this launch marked dead (label
+  // n + 1, see the end of this function) keep the mark: both directions
+  // look only for label n, so their rows are never scanned again.
+  for (int v = gt; v < p.n; v += gs) {
+    if (root >= 0 ? v == root : is_sink(p, v)) p.lab[v] = 0;
+    else if (!keep_dead || __ldcg(p.lab + v) <= p.n) p.lab[v] = p.n;
+  }
+  const long long dead = keep_dead ? ldv64(&c->dead_deg) : 0;
   if (gt == 0) {
     const int d = root >= 0 ? p.g.deg(root) : 0;
     if (root < 0) {
@@ -1438,7 +1490,7 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
     if (nf == 0) break;
     const long long fdeg = ldv64(&c->fdeg[fc]);
     visited += fdeg;
-    const long long rem = p.total_deg - visited;
+    const long long rem = p.total_deg - dead - visited;
     if (!bu && fdeg * kBfsAlpha > rem) bu = true;
     else if (bu && (long long)nf * kBfsBeta < (long long)p.n) bu = false;
     const bool mat = !bu && prev_bu;
@@ -1479,7 +1531,12 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
     prev_bu = bu;
   }
   if (queues) {
+    // File the active vertices, and mark dead the ones left unreached: the
+    // vertices that cannot reach a sink form a closed set (no residual arc
+    // leaves it), and a push into or out of it would need an active vertex
+    // labelled above n, so it stays closed for the rest of the phase.
     const int nall = p.n_light + p.n_medium + p.n_heavy;
+    unsigned long long dd = 0;
     for (int base = gt - lane; base < nall; base += gs) {
       const int i = base + lane;
       int v = -1, ev = 0;
@@ -1487,12 +1544,24 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
       if (i < nall) {
         v = __ldg(p.cls + i);
         if (!is_terminal(p, v)) {
+          const int lv = __ldcg(p.lab + v);
+          if (lv == p.n) {
+            p.lab[v] = p.n + 1;
+            dd += (unsigned long long)p.g.deg(v);
+          }
           ev = ldv(p.e + v);
-          pred = ev > 0 && __ldcg(p.lab + v) < p.n;
+          pred = ev > 0 && lv < p.n;
         }
       }
       warp_file(p, cur, v, ev, pred);
     }
+    for (int o = 16; o > 0; o >>= 1) dd += __shfl_down_sync(0xffffffffu, dd, o);
+    __shared__ unsigned long long s_dd;
+    if (threadIdx.x == 0) s_dd = 0;
+    __syncthreads();
+    if (lane == 0 && dd) atomicAdd(&s_dd, dd);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_dd) atomicAdd((unsigned long long*)&c->dead_deg, s_dd);
     if (!grid_sync(c, p.bar_timeout_ns)) return false;
   }
   return true;
@@ -1574,10 +1643,12 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
   int since_gr = 0;
   unsigned long long gr_ns = 0, round_ns = 0, push_ns = 0;
   unsigned long long gr_end = 0, gr_last = 0;  // global thread 0 only
+  bool marked = false;  // a global relabel has marked dead vertices (label n + 1)
   for (;;) {
     if (need_gr) {
       const unsigned long long t0 = gtime();
-      if (!bfs<Topo, 0>(p, p.term ? -1 : p.t, true, cur, acc)) break;
+      if (!bfs<Topo, 0>(p, p.term ? -1 : p.t, true, cur, acc, marked)) break;
+      marked = true;
       if (threadIdx.x == 0 && blockIdx.x == 0) {
         gr_end = gtime();
         gr_last = gr_end - t0;
@@ -1661,6 +1732,11 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
     // walks 20,000 rounds: 60 s of relabels every 48 rounds without it).
     if ((work > p.gr_threshold || since_gr >= p.gr_rounds) && ldv(&c->gr_ok)) need_gr = true;
   }
+  // callers see label n for every vertex that cannot reach the sink (every
+  // block has left the loop after the same barrier and reads no label now)
+  if (marked)
+    for (int v = gt; v < p.n; v += gs)
+      if (__ldcg(p.lab + v) > p.n) p.lab[v] = p.n;
   flush_acc(acc, p.st);
   if (gt == 0) {
     p.st->rounds = rounds;
