@@ -232,6 +232,15 @@ wbpr_status wbpr_graph_create(const wbpr_csr* g, wbpr_layout layout,
 wbpr_status wbpr_graph_destroy(wbpr_graph* g);
 /* Bytes of device memory held by the handle. */
 int64_t wbpr_graph_device_bytes(const wbpr_graph* g);
+/* Device memory of graphs and batches comes from a stream-ordered pool per
+ * device owned by the library.  Memory freed by wbpr_graph_destroy /
+ * wbpr_batch_destroy (and the build's temporaries) stays reserved in the pool
+ * up to max_bytes (16 GiB by default), so the next graph of a similar size is
+ * created without mapping memory, and destroyed without unmapping it.  This
+ * sets max_bytes for the current device's pool (and for pools created later)
+ * and releases reserved memory above it now; 0 returns all free memory to the
+ * driver.  Negative max_bytes: WBPR_ERR_INVALID_ARG. */
+wbpr_status wbpr_memory_cache(int64_t max_bytes);
 /* Replace the m capacities (input order; host or device buffer) of a built
  * graph without rebuilding it: the same topology with new capacities, e.g.
  * the next frame of a graph-cut pipeline.  Checked first (capacities >= 0:

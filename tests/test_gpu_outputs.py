@@ -178,3 +178,28 @@ def test_new_capacities_without_rebuild(layout):
             d.set_capacities(big)
         assert ei.value.status == 4
         assert d.solve("tc", g.s, g.t).flow == v
+
+
+def test_memory_pool_keeps_and_releases():
+    """Graphs take device memory from the library's pool: what a destroyed
+    graph held stays reserved for the next one (same results), and
+    memory_cache(0) hands it back to the driver."""
+    torch = pytest.importorskip("torch")
+    g = W.gen_rmat(17, 16, seed=2)
+    v = oracle.fifo_pr(g.n, g.off, g.dst, g.cap, g.s, g.t)
+    W.memory_cache(16 << 30)
+    held = 0
+    for layout in ("bcsr", "rcsr", "bcsr"):
+        with W.DeviceGraph(g, layout) as d:
+            assert d.solve("vc", g.s, g.t).flow == v
+            assert d.verify()["ok"]
+            held = max(held, d.device_bytes)
+    free_kept = torch.cuda.mem_get_info()[0]
+    W.memory_cache(0)
+    free_released = torch.cuda.mem_get_info()[0]
+    assert free_released - free_kept >= held // 2
+    W.memory_cache(16 << 30)
+    with W.DeviceGraph(g, "bcsr") as d:
+        assert d.solve("vc", g.s, g.t).flow == v
+    with pytest.raises(W.WbprError):
+        W.memory_cache(-1)

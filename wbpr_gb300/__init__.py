@@ -5,14 +5,16 @@ include/wbpr.h); this package only binds it.
 """
 from .api import (ALGOS, EXPORTED, LAYOUTS, Batch, DeviceGraph, Graph, WbprError, bipartite_matching,
                   bipartite_network, build_bcsr, build_bcsr2, build_rcsr, default_tuning, device_count,
-                  disjoint_union, gen_bipartite, gen_genrmf, gen_grid, gen_layered, gen_rmat, lib, maxflow, rcsr_preflow,
+                  disjoint_union, gen_bipartite, gen_genrmf, gen_grid, gen_layered, gen_rmat, lib, maxflow,
+                  memory_cache, rcsr_preflow,
                   rcsr_push_relabel, read_dimacs, read_graph, read_graph_cache, read_snap_bin, read_snap_txt,
                   status_str, write_dimacs, write_dimacs_flow, write_graph_cache, write_snap_bin)
 
 __all__ = [
     "ALGOS", "EXPORTED", "LAYOUTS", "Batch", "DeviceGraph", "Graph", "WbprError", "bipartite_matching",
     "bipartite_network", "build_bcsr", "build_bcsr2", "build_rcsr", "default_tuning", "device_count",
-    "disjoint_union", "gen_bipartite", "gen_genrmf", "gen_grid", "gen_layered", "gen_rmat", "lib", "maxflow", "rcsr_preflow",
+    "disjoint_union", "gen_bipartite", "gen_genrmf", "gen_grid", "gen_layered", "gen_rmat", "lib", "maxflow",
+    "memory_cache", "rcsr_preflow",
     "rcsr_push_relabel", "read_dimacs", "read_graph", "read_graph_cache", "read_snap_bin", "read_snap_txt",
     "status_str", "write_dimacs", "write_dimacs_flow", "write_graph_cache", "write_snap_bin",
 ]

@@ -90,6 +90,7 @@ EXPORTED = [
     "wbpr_verify", "wbpr_mincut_adjoint", "wbpr_rcsr_preflow", "wbpr_rcsr_push_relabel",
     "wbpr_read_trace", "wbpr_solve_bcsr_noalloc", "wbpr_batch_create", "wbpr_batch_destroy",
     "wbpr_batch_device_bytes", "wbpr_batch_solve", "wbpr_batch_instance_stats", "wbpr_batch_autotune",
+    "wbpr_memory_cache",
 ]
 
 _lib = None
@@ -140,6 +141,7 @@ def lib() -> C.CDLL:
         "wbpr_graph_create": (C.c_int, [C.POINTER(CsrView), C.c_int, C.POINTER(vp)]),
         "wbpr_graph_destroy": (C.c_int, [vp]),
         "wbpr_graph_device_bytes": (C.c_int64, [vp]),
+        "wbpr_memory_cache": (C.c_int, [C.c_int64]),
         "wbpr_graph_read_bcsr": (C.c_int, [vp, _i32p, _i32p, _i32p, _i32p]),
         "wbpr_graph_read_rcsr": (C.c_int, [vp, _i32p, _i32p, _i32p]),
         "wbpr_graph_set_stream": (C.c_int, [vp, vp]),
@@ -186,6 +188,12 @@ def _check(st: int, what: str) -> None:
 
 def device_count() -> int:
     return int(lib().wbpr_device_count())
+
+
+def memory_cache(max_bytes: int) -> None:
+    """Keep at most max_bytes of freed device memory reserved in the
+    library's pool on the current device (0 returns it all to the driver)."""
+    _check(lib().wbpr_memory_cache(int(max_bytes)), "wbpr_memory_cache")
 
 
 def _p(a: np.ndarray):

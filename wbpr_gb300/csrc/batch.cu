@@ -19,6 +19,7 @@
 
 #include <nvtx3/nvToolsExt.h>
 
+#include "devmem.h"
 #include "pr_kernel.cuh"
 #include "wbpr_internal.h"
 
@@ -311,9 +312,10 @@ template <class T>
 wbpr_status balloc(wbpr_batch* b, T** p, size_t count) {
   void* q = nullptr;
   size_t bytes = sizeof(T) * std::max<size_t>(count, 1);
-  cudaError_t e = cudaMalloc(&q, bytes);
+  cudaError_t e = wbpr::pool_alloc(&q, bytes, b->stream);
   if (e != cudaSuccess) {
-    wbpr::set_last_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    cudaGetLastError();
+    wbpr::set_last_error(std::string("device allocation: ") + cudaGetErrorString(e));
     return WBPR_ERR_CUDA;
   }
   b->allocs.push_back(q);
@@ -325,9 +327,12 @@ wbpr_status balloc(wbpr_batch* b, T** p, size_t count) {
 void batch_release(wbpr_batch* b) {
   if (!b) return;
   cudaSetDevice(b->device);
-  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->stream) {
+    cudaStreamSynchronize(b->stream);
+    for (void* q : b->allocs) cudaFreeAsync(q, b->stream);
+    cudaStreamSynchronize(b->stream);
+  }
   if (b->exec) cudaGraphExecDestroy(b->exec);
-  for (void* q : b->allocs) cudaFree(q);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
   if (b->stream) cudaStreamDestroy(b->stream);

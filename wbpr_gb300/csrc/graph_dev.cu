@@ -6,11 +6,13 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <string>
 #include <vector>
 
 #include <nvtx3/nvToolsExt.h>
 
+#include "devmem.h"
 #include "pr_launch.h"
 #include "wbpr_internal.h"
 
@@ -26,6 +28,54 @@ static thread_local std::string g_last_error;
 
 namespace wbpr {
 void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[kMaxDevices] = {};
+unsigned long long g_cache_bytes = 16ull << 30;  // release threshold of new pools
+}  // namespace
+
+cudaMemPool_t device_pool(int device) {
+  if (device < 0 || device >= kMaxDevices) return nullptr;
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  if (!g_pools[device]) {
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    unsigned long long thr = g_cache_bytes;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    g_pools[device] = pool;
+  }
+  return g_pools[device];
+}
+
+cudaError_t pool_alloc_on(void** p, size_t bytes, cudaStream_t stream) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  cudaMemPool_t pool = device_pool(dev);
+  if (!pool) return cudaErrorMemoryAllocation;
+  return cudaMallocFromPoolAsync(p, bytes, pool, stream);
+}
+
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t stream) {
+  cudaError_t e = pool_alloc_on(p, bytes, stream);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(*p, stream);
+    *p = nullptr;
+  }
+  return e;
+}
 }  // namespace wbpr
 
 #define CK(call)                                                            \
@@ -113,9 +163,10 @@ template <class T>
 wbpr_status dalloc(wbpr_graph* g, T** p, size_t count) {
   void* q = nullptr;
   size_t bytes = sizeof(T) * std::max<size_t>(count, 1);
-  cudaError_t e = cudaMalloc(&q, bytes);
+  cudaError_t e = wbpr::pool_alloc(&q, bytes, g->stream);
   if (e != cudaSuccess) {
-    g_last_error = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    cudaGetLastError();
+    g_last_error = std::string("device allocation: ") + cudaGetErrorString(e);
     return WBPR_ERR_CUDA;
   }
   g->allocs.push_back(q);
@@ -127,8 +178,12 @@ wbpr_status dalloc(wbpr_graph* g, T** p, size_t count) {
 void release(wbpr_graph* g) {
   if (!g) return;
   cudaSetDevice(g->device);
-  if (g->stream) cudaStreamSynchronize(g->stream);
-  for (void* q : g->allocs) cudaFree(q);
+  if (g->stream) {
+    // back into the library's pool, in stream order after the handle's work
+    cudaStreamSynchronize(g->stream);
+    for (void* q : g->allocs) cudaFreeAsync(q, g->stream);
+    cudaStreamSynchronize(g->stream);
+  }
   if (g->ev0) cudaEventDestroy(g->ev0);
   if (g->ev1) cudaEventDestroy(g->ev1);
   if (g->ev2) cudaEventDestroy(g->ev2);
@@ -738,7 +793,7 @@ wbpr_status device_scan(int* data, long long count, cudaStream_t st) {
     return WBPR_OK;
   }
   int* sums = nullptr;
-  CK(cudaMallocAsync(&sums, sizeof(int) * tiles, st));
+  CK(wbpr::pool_alloc_on((void**)&sums, sizeof(int) * tiles, st));
   db_scan_tiles<<<(unsigned)tiles, 1024, 0, st>>>(data, count, sums);
   cudaError_t e = cudaGetLastError();
   wbpr_status r = e == cudaSuccess ? device_scan(sums, tiles, st) : WBPR_ERR_CUDA;
@@ -776,8 +831,8 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
     if ((rs = dalloc(g, &g->rarc, (size_t)m))) return rs;
   }
   if ((rs = dalloc(g, &g->ioff, (size_t)n + 1))) return rs;
-  // every temporary is carved from one allocation (one cudaMalloc and one
-  // cudaFree per build instead of one per array)
+  // every temporary is carved from one pool allocation, freed when the
+  // build ends
   char* slab = nullptr;
   size_t slab_at = 0, slab_size = 0;
   cudaStream_t side = nullptr;
@@ -785,7 +840,7 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   auto cleanup = [&]() {
     cudaStreamSynchronize(st);
     if (side) cudaStreamSynchronize(side);
-    if (slab) cudaFree(slab);
+    if (slab) cudaFreeAsync(slab, st);
     if (side_done) cudaEventDestroy(side_done);
     if (side) cudaStreamDestroy(side);
     slab = nullptr;
@@ -823,7 +878,7 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   const size_t nh_max = std::max<size_t>((size_t)ntiles * 256 + 1, (size_t)n + 1);
   slab_size = 256 * 16 + 4 * (size_t)m * (in->capacities ? 2 : 1) + 4 * ((size_t)n + 1) +
               8 * ((size_t)n + 1) + 64 + 16 * mv + 4 * nh_max + 4 * (size_t)m + 8 * (size_t)m;
-  if (cudaMalloc(&slab, slab_size) != cudaSuccess) {
+  if (wbpr::pool_alloc((void**)&slab, slab_size, st) != cudaSuccess) {
     cudaGetLastError();
     slab = nullptr;
     g_last_error = "device build: out of device memory";
@@ -1301,6 +1356,28 @@ wbpr_status wbpr_graph_destroy(wbpr_graph* g) {
 
 int64_t wbpr_graph_device_bytes(const wbpr_graph* g) { return g ? g->bytes : 0; }
 
+wbpr_status wbpr_memory_cache(int64_t max_bytes) {
+  if (max_bytes < 0) return WBPR_ERR_INVALID_ARG;
+  int ndev = 0, dev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return WBPR_ERR_NO_DEVICE;
+  }
+  {
+    std::lock_guard<std::mutex> lk(wbpr::g_pool_mu);
+    wbpr::g_cache_bytes = (unsigned long long)max_bytes;
+  }
+  cudaMemPool_t pool = wbpr::device_pool(dev);
+  if (!pool) {
+    g_last_error = "wbpr_memory_cache: no memory pool on this device";
+    return WBPR_ERR_CUDA;
+  }
+  unsigned long long thr = (unsigned long long)max_bytes;
+  CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  CK(cudaMemPoolTrimTo(pool, (size_t)max_bytes));
+  return WBPR_OK;
+}
+
 wbpr_status wbpr_autotune(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, wbpr_tuning* best,
                           float* best_ms) {
   NvtxRange nvtx_("wbpr_autotune");
@@ -1625,10 +1702,10 @@ wbpr_status wbpr_verify(wbpr_graph* g, wbpr_verify_report* rep) {
   wbpr_status st = bfs_labels(g, g->t, 0, -1);
   if (st) return st;
   VerifyAcc* dacc = nullptr;
-  CK(cudaMalloc(&dacc, sizeof(VerifyAcc)));
+  CK(wbpr::pool_alloc_on((void**)&dacc, sizeof(VerifyAcc), g->stream));
   cudaMemsetAsync(dacc, 0, sizeof(VerifyAcc), g->stream);
   long long* net = nullptr;
-  CK(cudaMallocAsync(&net, 8 * (size_t)g->n, g->stream));
+  CK(wbpr::pool_alloc_on((void**)&net, 8 * (size_t)g->n, g->stream));
   cudaMemsetAsync(net, 0, 8 * (size_t)g->n, g->stream);
   if (g->layout == WBPR_LAYOUT_RCSR)
     verify_arcs_rcsr<<<g->sms * 8, 256, 0, g->stream>>>(g->frow, g->farc, g->fcb, g->fcap, g->rrow, g->rarc,
@@ -1645,7 +1722,7 @@ wbpr_status wbpr_verify(wbpr_graph* g, wbpr_verify_report* rep) {
   if (ce == cudaSuccess) ce = cudaMemcpyAsync(&ls, g->vlab + g->s, 4, cudaMemcpyDeviceToHost, g->stream);
   if (ce == cudaSuccess) ce = cudaMemcpyAsync(&et, g->e + g->t, 4, cudaMemcpyDeviceToHost, g->stream);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(g->stream);
-  cudaFree(dacc);
+  cudaFreeAsync(dacc, g->stream);
   if (ce != cudaSuccess) {
     g_last_error = std::string("verify: ") + cudaGetErrorString(ce);
     return WBPR_ERR_CUDA;
