@@ -285,9 +285,13 @@ def run_ours(args) -> None:
     dg.close()
     # e2e through the C ABI from host buffers: the input CSR sits in pinned
     # host memory (set up once, outside the timed region); every step copies
-    # it to the device, builds the residual graph there, solves, reads back
+    # it to the device, builds the residual graph there, solves, reads back.
+    # One untimed step first, like the warm-up of the device-timed steps.
     e2e_steps = min(args.steps, args.e2e_steps)
     gp = pinned_copy(g)
+    if e2e_steps > 0:
+        with W.DeviceGraph(gp, args.layout) as dd:
+            dd.solve(args.algo, g.s, g.t, **tuning)
     e2e_s = create_s = 0.0
     for _ in range(e2e_steps):
         t1 = time.perf_counter()
@@ -301,7 +305,7 @@ def run_ours(args) -> None:
     e2e = None
     if e2e_steps > 0:
         e2e = {"value": world * e2e_steps * g.m / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": 8 + 128, "steps": e2e_steps,
+               "d2h_bytes_per_step": 8 + 128, "steps": e2e_steps, "warmup": 1,
                "create_ms": create_s * 1e3 / e2e_steps, "ms_per_step": e2e_s * 1e3 / e2e_steps,
                "pinned": gp is not g,
                "path": "wbpr_graph_create (H2D of the input CSR from pinned host memory, residual graph "

@@ -460,38 +460,28 @@ __global__ void caps_kernel(const int* ioff, const int* row, const int2* arc, in
 // row[u] = off[u] + inoff[u], the forward slot of input arc i (tail u) is
 // i + inoff[u], and the twin of the arc at position p of the arcs stably
 // sorted by head v is off[v + 1] + p.  The stable sort is an LSD radix sort
-// by head over warp tiles; its last pass also records each arc's position p.
-// In-degrees, validating heads and offsets on the way (what the host checks
-// only for its own builders): heads in [0, n), non-decreasing offsets.
-__global__ void db_count(const int* off, const int* dst, int n, long long m, int* indeg, unsigned long long* bad) {
-  const long long gs = (long long)gridDim.x * blockDim.x;
+// by head over block tiles; the in-degree pass records each arc's position p.
+// The input is validated on the way (what the host
+// checks only for its own builders): non-decreasing offsets here, heads in
+// [0, n) by the sort's first histogram, capacities >= 0 by the forward fill.
+__global__ void db_check_off(const int* off, int n, unsigned long long* bad) {
   bool b = false;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += gs) {
-    const int v = dst[i];
-    if (v < 0 || v >= n) {
-      b = true;
-      continue;
-    }
-    atomicAdd(indeg + v, 1);
-  }
-  for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < n; u += gs)
+  for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < n; u += (long long)gridDim.x * blockDim.x)
     if (off[u + 1] < off[u]) b = true;
   if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1ull);
 }
-// Incoming capacity per vertex (its excess can never exceed it); capacities
-// must be >= 0.  Arcs with invalid heads were flagged by db_count.
-__global__ void db_count_cap(const int* dst, const int* cap, int n, long long m, unsigned long long* incap,
-                             unsigned long long* bad) {
-  const long long gs = (long long)gridDim.x * blockDim.x;
-  bool b = false;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += gs) {
-    const int v = dst[i];
-    const int c = cap ? cap[i] : 1;
-    if (c < 0) b = true;
-    if (v < 0 || v >= n || c <= 0) continue;
-    atomicAdd(incap + v, (unsigned long long)c);
+// In-degrees from the heads sorted ascending (all checked to lie in [0, n)):
+// the first position p0 of a head's run adds -p0, its last position p1 adds
+// p1 + 1, so indeg[v] ends as the run length.  Two atomics per head, on
+// distinct words, instead of one per arc on a few hot ones.  pos_of (BCSR):
+// the sorted position of every arc, pos_of[sval[p]] = p.
+__global__ void db_indeg_sorted(const int* skey, const int* sval, long long m, int* indeg, int* pos_of) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < m; p += (long long)gridDim.x * blockDim.x) {
+    const int v = skey[p];
+    if (p == 0 || skey[p - 1] != v) atomicAdd(indeg + v, -(int)p);
+    if (p == m - 1 || skey[p + 1] != v) atomicAdd(indeg + v, (int)p + 1);
+    if (pos_of) pos_of[sval[p]] = (int)p;
   }
-  if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1ull);
 }
 __global__ void db_max(const unsigned long long* incap, int n, unsigned long long* out) {
   unsigned long long mx = 0;
@@ -562,27 +552,31 @@ __device__ __forceinline__ unsigned digit_peers(int d, bool ok) {
   }
   return peers;
 }
-__global__ void __launch_bounds__(256) db_sort_hist(const int* key, long long m, int shift, int ntiles, int* hist) {
+// n_check > 0 (the first pass): also flag keys outside [0, n_check)
+__global__ void __launch_bounds__(256) db_sort_hist(const int* key, long long m, int shift, int ntiles, int* hist,
+                                                    int n_check, unsigned long long* bad) {
   __shared__ int cnt[256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int tile = blockIdx.x;
   cnt[threadIdx.x] = 0;
   __syncthreads();
   const long long base = (long long)tile * kSortTile + (long long)w * kSortRounds * 32;
+  bool b = false;
   for (int r = 0; r < kSortRounds; ++r) {
     const long long i = base + r * 32 + lane;
     const bool ok = i < m;
-    const int d = ok ? (key[i] >> shift) & 255 : 0;
+    const int k = ok ? key[i] : 0;
+    if (n_check > 0 && (k < 0 || k >= n_check)) b = true;
+    const int d = (k >> shift) & 255;
     const unsigned peers = digit_peers(d, ok);
     if (ok && lane == __ffs(peers) - 1) atomicAdd(&cnt[d], __popc(peers));
   }
+  if (__any_sync(0xffffffffu, b) && lane == 0) atomicOr(bad, 1ull);
   __syncthreads();
   hist[(long long)threadIdx.x * ntiles + tile] = cnt[threadIdx.x];
 }
-// pos_of != nullptr on the last pass: also record each arc's sorted position
 __global__ void __launch_bounds__(256) db_sort_scatter(const int* kin, const int* vin, long long m, int shift,
-                                                       int ntiles, const int* hist, int* kout, int* vout,
-                                                       int* pos_of) {
+                                                       int ntiles, const int* hist, int* kout, int* vout) {
   __shared__ int wc[8][256];     // per-warp digit counts, then each warp's start within its digit
   __shared__ int dstart[256];    // tile-local start of each digit
   __shared__ int gofs[256];      // global start of this tile's run of each digit
@@ -649,15 +643,16 @@ __global__ void __launch_bounds__(256) db_sort_scatter(const int* kin, const int
     const int pos = gofs[d] + (i - dstart[d]);
     kout[pos] = k;
     vout[pos] = sv[i];
-    if (pos_of) pos_of[sv[i]] = pos;
   }
 }
 
 // forward slots, arc-parallel (tails as in the tile walk above); records
-// (tail, forward slot) per arc for the twin pass
+// {tail, forward slot, capacity} per arc for the twin pass; flags negative
+// capacities
 __global__ void db_fill_fwd(const int* off, const int* inoff, const int* dst, const int* cap, const int* pos_of,
-                            int n, long long m, int2* arc, int2* arx, int2* uf) {
+                            int n, long long m, int2* arc, int2* arx, int4* uf, unsigned long long* bad) {
   const int lane = threadIdx.x & 31;
+  bool b = false;
   FOR_TILES(m) {
     const TileRows tr = tile_rows(off, n, base, m);
 #pragma unroll 4
@@ -666,24 +661,51 @@ __global__ void db_fill_fwd(const int* off, const int* inoff, const int* dst, co
       if (i >= m) break;
       const int u = row_search(off, i, tr.lo, tr.hi);
       const int v = dst[i], c = cap ? cap[i] : 1;
+      if (c < 0) b = true;
       const int f = (int)i + __ldg(inoff + u);
       const int r = __ldg(off + v + 1) + pos_of[i];
       arc[f] = make_int2(v, c);
       arx[f] = make_int2(r, c);
-      uf[i] = make_int2(u, f);
+      uf[i] = make_int4(u, f, c, 0);
     }
   }
+  if (__any_sync(0xffffffffu, b) && lane == 0) atomicOr(bad, 1ull);
+}
+// Sum of x over the lanes from this one to the end of its run of equal keys
+// (keys ascending across the warp, so a run is a block of adjacent lanes);
+// the first lane of a run gets the run's sum.
+__device__ __forceinline__ unsigned long long run_suffix_sum(int key, unsigned long long x) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned long long y = __shfl_down_sync(0xffffffffu, x, d);
+    const int ky = __shfl_down_sync(0xffffffffu, key, d);
+    if (lane + d < 32 && ky == key) x += y;
+  }
+  return x;
 }
 // twin slots in sorted order: the twin of sorted position p is off[v + 1] + p,
-// so consecutive p write consecutive slots
-__global__ void db_fill_twin(const int* off, const int* skey, const int* sval, const int2* uf, long long m,
-                             int2* arc, int2* arx) {
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < m; p += (long long)gridDim.x * blockDim.x) {
-    const int v = skey[p];
-    const int2 t = uf[sval[p]];
-    const int r = __ldg(off + v + 1) + (int)p;
-    arc[r] = make_int2(t.x, 0);
-    arx[r] = make_int2(t.y, 0);
+// so consecutive p write consecutive slots; every head also gets the sum of
+// its incoming capacities (one atomic per run of the head within a warp)
+__global__ void db_fill_twin(const int* off, const int* skey, const int* sval, const int4* uf, long long m,
+                             int2* arc, int2* arx, unsigned long long* incap) {
+  const int lane = threadIdx.x & 31;
+  const long long gs = (long long)gridDim.x * blockDim.x;
+  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < m; base += gs) {
+    const long long p = base + lane;
+    int v = -1;
+    unsigned long long c = 0;
+    if (p < m) {
+      v = skey[p];
+      const int4 t = uf[sval[p]];
+      const int r = __ldg(off + v + 1) + (int)p;
+      arc[r] = make_int2(t.x, 0);
+      arx[r] = make_int2(t.y, 0);
+      c = t.z > 0 ? (unsigned long long)t.z : 0ull;
+    }
+    const unsigned long long sum = run_suffix_sum(v, c);
+    const int vp = __shfl_up_sync(0xffffffffu, v, 1);
+    if (v >= 0 && (lane == 0 || vp != v) && sum) atomicAdd(incap + v, sum);
   }
 }
 
@@ -757,10 +779,12 @@ __global__ void db_bch_fill(const int* o1, const int* o2, const int* hcls, int n
   }
 }
 
-// RCSR forward arcs in input order, and the tail of every input arc
+// RCSR forward arcs in input order, and the tail of every input arc; flags
+// negative capacities
 __global__ void db_rcsr_fwd(const int* off, const int* dst, const int* cap, int n, long long m, int2* farc,
-                            int* fcap, int* fcb, int* tail) {
+                            int* fcap, int* fcb, int* tail, unsigned long long* bad) {
   const int lane = threadIdx.x & 31;
+  bool b = false;
   FOR_TILES(m) {
     const TileRows tr = tile_rows(off, n, base, m);
 #pragma unroll 4
@@ -768,19 +792,36 @@ __global__ void db_rcsr_fwd(const int* off, const int* dst, const int* cap, int 
       const long long i = base + k * 32 + lane;
       if (i >= m) break;
       const int c = cap ? cap[i] : 1;
+      if (c < 0) b = true;
       farc[i] = make_int2(dst[i], c);
       fcap[i] = c;
       fcb[i] = 0;
       tail[i] = row_search(off, i, tr.lo, tr.hi);
     }
   }
+  if (__any_sync(0xffffffffu, b) && lane == 0) atomicOr(bad, 1ull);
 }
 // RCSR reverse entries: position p of the arcs stably sorted by head holds
-// {tail, forward arc id} (the reference's rdestinations / flow_index)
-__global__ void db_rcsr_rev(const int* sval, const int* tail, long long m, int2* rarc) {
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < m; p += (long long)gridDim.x * blockDim.x) {
-    const int i = sval[p];
-    rarc[p] = make_int2(__ldg(tail + i), i);
+// {tail, forward arc id} (the reference's rdestinations / flow_index); every
+// head gets the sum of its incoming capacities as in db_fill_twin
+__global__ void db_rcsr_rev(const int* skey, const int* sval, const int* tail, const int* fcap, long long m,
+                            int2* rarc, unsigned long long* incap) {
+  const int lane = threadIdx.x & 31;
+  const long long gs = (long long)gridDim.x * blockDim.x;
+  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < m; base += gs) {
+    const long long p = base + lane;
+    int v = -1;
+    unsigned long long c = 0;
+    if (p < m) {
+      v = skey[p];
+      const int i = sval[p];
+      rarc[p] = make_int2(__ldg(tail + i), i);
+      const int ci = __ldg(fcap + i);
+      c = ci > 0 ? (unsigned long long)ci : 0ull;
+    }
+    const unsigned long long sum = run_suffix_sum(v, c);
+    const int vp = __shfl_up_sync(0xffffffffu, v, 1);
+    if (v >= 0 && (lane == 0 || vp != v) && sum) atomicAdd(incap + v, sum);
   }
 }
 
@@ -877,7 +918,7 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   const size_t mv = std::max<size_t>((size_t)m, (size_t)n + 1);
   const size_t nh_max = std::max<size_t>((size_t)ntiles * 256 + 1, (size_t)n + 1);
   slab_size = 256 * 16 + 4 * (size_t)m * (in->capacities ? 2 : 1) + 4 * ((size_t)n + 1) +
-              8 * ((size_t)n + 1) + 64 + 16 * mv + 4 * nh_max + 4 * (size_t)m + 8 * (size_t)m;
+              8 * ((size_t)n + 1) + 64 + 16 * mv + 4 * nh_max + 4 * (size_t)m + 16 * (size_t)m;
   if (wbpr::pool_alloc((void**)&slab, slab_size, st) != cudaSuccess) {
     cudaGetLastError();
     slab = nullptr;
@@ -898,24 +939,58 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   int* kb[2] = {(int*)talloc(4 * mv), (int*)talloc(4 * mv)};
   int* vb[2] = {(int*)talloc(4 * mv), (int*)talloc(4 * mv)};
   int* hist = (int*)talloc(4 * nh_max);
-  int* pos_of = (int*)talloc(4 * (size_t)m);
-  int2* uf = (int2*)talloc(8 * (size_t)m);
+  int* tail = (int*)talloc(4 * (size_t)m);  // BCSR: sorted position of each arc; RCSR: its tail
+  int4* uf = (int4*)talloc(16 * (size_t)m);
   if (!d_dst || (in->capacities && !d_cap) || !inoff || !incap || !cnt || !kb[0] || !kb[1] || !vb[0] || !vb[1] ||
-      !hist || !pos_of || !uf) {
+      !hist || !tail || !uf) {
     cudaGetLastError();
     g_last_error = "device build: out of device memory";
     cleanup();
     return WBPR_ERR_CUDA;
   }
-  // Heads first: the in-degree count, the row offsets and the sort need only
-  // them, so they run while the capacities are copied on a second stream.
+  // Heads first: the sort needs only them, so it runs while the capacities
+  // are copied on a second stream.  The in-degrees come from the sorted heads.
   DB(cudaMemcpyAsync(g->ioff, in->offsets, 4 * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
   if (m) DB(cudaMemcpyAsync(d_dst, in->destinations, 4 * (size_t)m, cudaMemcpyHostToDevice, st));
   DB(cudaMemsetAsync(inoff, 0, 4 * ((size_t)n + 1), st));
   DB(cudaMemsetAsync(incap, 0, 8 * ((size_t)n + 1), st));
   DB(cudaMemsetAsync(cnt, 0, 8 * 8, st));
-  db_count<<<blocks, 256, 0, st>>>(g->ioff, d_dst, n, m, inoff, cnt + 6);
+  db_check_off<<<blocks, 256, 0, st>>>(g->ioff, n, cnt + 6);
   DB(cudaGetLastError());
+  const int bits = n > 1 ? 32 - __builtin_clz((unsigned)(n - 1)) : 1;
+  const int passes = (bits + 7) / 8;
+  const int* skey = kb[(passes - 1) & 1];
+  const int* sval = vb[(passes - 1) & 1];
+  if (m) {
+    const unsigned sblocks = (unsigned)ntiles;
+    for (int p = 0; p < passes; ++p) {
+      const int* kin = p ? kb[(p - 1) & 1] : d_dst;
+      const int* vin = p ? vb[(p - 1) & 1] : nullptr;
+      db_sort_hist<<<sblocks, 256, 0, st>>>(kin, m, 8 * p, ntiles, hist, p == 0 ? n : 0, cnt + 6);
+      DB(cudaGetLastError());
+      DBS(device_scan(hist, (long long)ntiles * 256, st));
+      db_sort_scatter<<<sblocks, 256, 0, st>>>(kin, vin, m, 8 * p, ntiles, hist, kb[p & 1], vb[p & 1]);
+      DB(cudaGetLastError());
+    }
+  }
+  // capacities: copied on the side stream (its host call may block while
+  // the sort above runs)
+  if (m && d_cap) {
+    DB(cudaMemcpyAsync(d_cap, in->capacities, 4 * (size_t)m, cudaMemcpyHostToDevice, side));
+    DB(cudaEventRecord(side_done, side));
+  }
+  // heads and offsets must be valid before anything indexes with them
+  unsigned long long chk[2] = {0, 0};
+  DB(cudaMemcpyAsync(chk, cnt + 6, 8, cudaMemcpyDeviceToHost, st));
+  DB(cudaStreamSynchronize(st));
+  if (chk[0]) {
+    cleanup();
+    return WBPR_ERR_INVALID_ARG;
+  }
+  if (m) {
+    db_indeg_sorted<<<blocks, 256, 0, st>>>(skey, sval, m, inoff, bcsr ? tail : nullptr);
+    DB(cudaGetLastError());
+  }
   DBS(device_scan(inoff, (long long)n + 1, st));
   if (bcsr) {
     db_row<<<blocks, 256, 0, st>>>(g->ioff, inoff, n, g->row);
@@ -924,56 +999,19 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
     DB(cudaMemcpyAsync(g->frow, g->ioff, 4 * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
     DB(cudaMemcpyAsync(g->rrow, inoff, 4 * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
   }
+  if (m && d_cap) DB(cudaStreamWaitEvent(st, side_done, 0));
   if (m) {
-    const int bits = n > 1 ? 32 - __builtin_clz((unsigned)(n - 1)) : 1;
-    const int passes = (bits + 7) / 8;
-    const unsigned sblocks = (unsigned)ntiles;
-    for (int p = 0; p < passes; ++p) {
-      const int* kin = p ? kb[(p - 1) & 1] : d_dst;
-      const int* vin = p ? vb[(p - 1) & 1] : nullptr;
-      db_sort_hist<<<sblocks, 256, 0, st>>>(kin, m, 8 * p, ntiles, hist);
-      DB(cudaGetLastError());
-      DBS(device_scan(hist, (long long)ntiles * 256, st));
-      db_sort_scatter<<<sblocks, 256, 0, st>>>(kin, vin, m, 8 * p, ntiles, hist, kb[p & 1], vb[p & 1],
-                                               bcsr && p == passes - 1 ? pos_of : nullptr);
-      DB(cudaGetLastError());
-    }
-  }
-  // capacities: copied on the side stream (its host call may block while
-  // the sort above runs), then counted; then every input check is decided
-  if (m && d_cap) {
-    DB(cudaMemcpyAsync(d_cap, in->capacities, 4 * (size_t)m, cudaMemcpyHostToDevice, side));
-    DB(cudaEventRecord(side_done, side));
-    DB(cudaStreamWaitEvent(st, side_done, 0));
-  }
-  db_count_cap<<<blocks, 256, 0, st>>>(d_dst, d_cap, n, m, incap, cnt + 6);
-  db_max<<<blocks, 256, 0, st>>>(incap, n, cnt + 7);
-  DB(cudaGetLastError());
-  unsigned long long chk[2] = {0, 0};
-  DB(cudaMemcpyAsync(chk, cnt + 6, 16, cudaMemcpyDeviceToHost, st));
-  DB(cudaStreamSynchronize(st));
-  if (chk[0]) {
-    cleanup();
-    return WBPR_ERR_INVALID_ARG;
-  }
-  if (chk[1] > 0x7fffffffull) {
-    cleanup();
-    return WBPR_ERR_OVERFLOW;
-  }
-  if (m) {
-    const int bits = n > 1 ? 32 - __builtin_clz((unsigned)(n - 1)) : 1;
-    const int passes = (bits + 7) / 8;
     if (bcsr) {
-      db_fill_fwd<<<blocks, 256, 0, st>>>(g->ioff, inoff, d_dst, d_cap, pos_of, n, m, g->arc, g->arx, uf);
-      db_fill_twin<<<blocks, 256, 0, st>>>(g->ioff, kb[(passes - 1) & 1], vb[(passes - 1) & 1], uf, m, g->arc,
-                                           g->arx);
+      db_fill_fwd<<<blocks, 256, 0, st>>>(g->ioff, inoff, d_dst, d_cap, tail, n, m, g->arc, g->arx, uf, cnt + 6);
+      db_fill_twin<<<blocks, 256, 0, st>>>(g->ioff, skey, sval, uf, m, g->arc, g->arx, incap);
     } else {
-      int* tail = pos_of;  // free in this layout
-      db_rcsr_fwd<<<blocks, 256, 0, st>>>(g->ioff, d_dst, d_cap, n, m, g->farc, g->fcap, g->fcb, tail);
-      db_rcsr_rev<<<blocks, 256, 0, st>>>(vb[(passes - 1) & 1], tail, m, g->rarc);
+      db_rcsr_fwd<<<blocks, 256, 0, st>>>(g->ioff, d_dst, d_cap, n, m, g->farc, g->fcap, g->fcb, tail, cnt + 6);
+      db_rcsr_rev<<<blocks, 256, 0, st>>>(skey, sval, tail, g->fcap, m, g->rarc, incap);
     }
     DB(cudaGetLastError());
   }
+  db_max<<<blocks, 256, 0, st>>>(incap, n, cnt + 7);
+  DB(cudaGetLastError());
   const int* o1 = bcsr ? g->row : g->frow;
   const int* o2 = bcsr ? nullptr : g->rrow;
   // length classes in vertex order, by three stable compactions
@@ -985,7 +1023,16 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   unsigned long long hc[3];
   for (int k = 0; k < 3; ++k) DB(cudaMemcpyAsync(tot + k, fl[k] + n, 4, cudaMemcpyDeviceToHost, st));
   DB(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+  DB(cudaMemcpyAsync(chk, cnt + 6, 16, cudaMemcpyDeviceToHost, st));
   DB(cudaStreamSynchronize(st));
+  if (chk[0]) {  // a negative capacity
+    cleanup();
+    return WBPR_ERR_INVALID_ARG;
+  }
+  if (chk[1] > 0x7fffffffull) {  // some vertex's incoming capacities pass int32
+    cleanup();
+    return WBPR_ERR_OVERFLOW;
+  }
   g->n_light = tot[0];
   g->n_medium = tot[1];
   g->n_heavy = tot[2];
