@@ -352,7 +352,7 @@ wbpr_status wbpr_batch_autotune(wbpr_batch* b, wbpr_tuning* best, float* best_ms
  * holds the final residual on return), d_arx (2 ints per residual arc: twin
  * arc, capacity), as produced by wbpr_build_bcsr -- and receives the maximum
  * flow in *flow (host).  All solver scratch lives in one fixed file-scope
- * device array (about 7.4 MB per device, held until exit), so no allocation
+ * device array (about 5.6 MB per device, held until exit), so no allocation
  * happens.  Limits: n <= 65536 vertices and num_residual_arcs <= 1048576;
  * larger inputs return WBPR_ERR_INVALID_ARG (see wbpr_last_error).  The first
  * call on a device looks up the array's address; make it before any stream

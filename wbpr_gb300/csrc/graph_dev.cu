@@ -124,12 +124,8 @@ struct wbpr_graph {
   int* lq[2] = {nullptr, nullptr};
   int* hq[2] = {nullptr, nullptr};
   int* esnap = nullptr;
-  int* dq = nullptr;
-  int* dbase = nullptr;
-  int* dE = nullptr;
-  int* derem = nullptr;
   int* dmin0 = nullptr;
-  int* hown = nullptr;
+  int4* hrec = nullptr;
   int* hsum = nullptr;
   int* hmin = nullptr;
   int4* bch = nullptr;
@@ -850,7 +846,7 @@ wbpr_status device_scan(int* data, long long count, cudaStream_t st) {
 
 // Builds the residual graph of g->layout in HBM from the input CSR:
 // BCSR row/arc/arx or RCSR frow/farc/fcb/fcap/rrow/rarc, plus ioff, the
-// length classes cls, the heavy-row chunks bch, hown/hsum/hmin and counts.
+// length classes cls, the heavy-row chunks bch, hrec/hsum/hmin and counts.
 wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   NvtxRange nvtx_("device build");
   const int n = g->n;
@@ -1058,7 +1054,7 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   if (nh) db_bch_fill<<<std::min(nh, blocks), 128, 0, st>>>(o1, o2, hcls, nh, cbase, g->bch);
   DB(cudaGetLastError());
   const size_t max_chunks = (size_t)hc[2] + 1;
-  DBS(dalloc(g, &g->hown, max_chunks));
+  DBS(dalloc(g, &g->hrec, 3 * max_chunks));
   DBS(dalloc(g, &g->hsum, max_chunks));
   DBS(dalloc(g, &g->hmin, max_chunks));
   DB(cudaStreamSynchronize(st));
@@ -1119,7 +1115,7 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   const int n = g->n;
   TRY(build_device(g, in));
   int** vec[] = {&g->h, &g->e, &g->rl_min, &g->rl_left, &g->lq[0], &g->lq[1], &g->hq[0], &g->hq[1],
-                 &g->esnap, &g->dq, &g->dbase, &g->dE, &g->derem, &g->dmin0,
+                 &g->esnap, &g->dmin0,
                  &g->qraw, &g->fr[0], &g->fr[1], &g->fr[2], &g->vlab};
   {
     // one allocation for the per-vertex scratch, one for the BFS chunk lists
@@ -1155,12 +1151,8 @@ void fill_common(wbpr_graph* g, Params<Topo>& p) {
     p.hq[k] = g->hq[k];
   }
   p.esnap = g->esnap;
-  p.dq = g->dq;
-  p.dbase = g->dbase;
-  p.dE = g->dE;
-  p.derem = g->derem;
   p.dmin0 = g->dmin0;
-  p.hown = g->hown;
+  p.hrec = g->hrec;
   p.hsum = g->hsum;
   p.hmin = g->hmin;
   p.bch = g->bch;

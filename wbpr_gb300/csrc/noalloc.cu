@@ -9,7 +9,7 @@
 //
 // Limits: at most kNoAllocMaxVertices vertices and kNoAllocMaxArcs residual
 // arcs (two per input arc); larger graphs are refused with
-// WBPR_ERR_INVALID_ARG.  The array occupies about 7.4 MB on every device that
+// WBPR_ERR_INVALID_ARG.  The array occupies about 5.6 MB on every device that
 // loads the library, until the process exits.
 //
 // Set-up: the first call on a device (with that device current) looks up the
@@ -39,16 +39,17 @@ constexpr long long align_ints(long long x) { return (x + 63) & ~63LL; }
 constexpr long long kCtlWords = align_ints((sizeof(Ctl) + 3) / 4);
 constexpr long long kStatWords = align_ints((sizeof(Stats) + 3) / 4);
 constexpr long long kCountWords = 64;  // classification counters
-constexpr int kVertexArrays = 19;      // per-vertex int arrays, indexed as in wbpr_solve_bcsr_noalloc
+constexpr int kVertexArrays = 15;      // per-vertex int arrays, indexed as in wbpr_solve_bcsr_noalloc
 constexpr long long kTdItems = kNoAllocMaxArcs / kTdChunk + kNoAllocMaxVertices;
-constexpr long long kChunkItems = kNoAllocMaxArcs / kChunk + kNoAllocMaxVertices;
+// deep entries are rows longer than kFirst, each filed at most once a round
+constexpr long long kChunkItems = kNoAllocMaxArcs / kChunk + kNoAllocMaxArcs / (kFirst + 1) + 1;
 constexpr long long kBchItems = kNoAllocMaxArcs / kChunk + kNoAllocMaxArcs / (kHeavyDeg + 1) + 1;
 constexpr long long kOffStat = kCtlWords;
 constexpr long long kOffCount = kOffStat + kStatWords;
 constexpr long long kOffVert = kOffCount + kCountWords;
 constexpr long long kOffFrh = kOffVert + (long long)kVertexArrays * kNoAllocMaxVertices;
 constexpr long long kOffChunk = kOffFrh + 3 * 2 * kTdItems;
-constexpr long long kOffBch = kOffChunk + 3 * kChunkItems;
+constexpr long long kOffBch = kOffChunk + 14 * kChunkItems;  // hrec (3 x int4), hsum, hmin per item
 constexpr long long kScratchWords = align_ints(kOffBch + 4 * kBchItems);
 
 static __device__ __align__(256) int g_noalloc_scratch[kScratchWords];
@@ -149,7 +150,7 @@ extern "C" wbpr_status wbpr_solve_bcsr_noalloc(int32_t n, int64_t num_residual_a
   if (num_residual_arcs > 0) na_reset<<<sms * 4, 256, 0, st>>>(arc, arx, num_residual_arcs);
   int* vert = base + kOffVert;
   auto va = [&](int i) { return vert + (long long)i * kNoAllocMaxVertices; };
-  int* cls = va(18);
+  int* cls = va(14);
   int4* bch = (int4*)(base + kOffBch);
   na_count<<<sms * 2, 256, 0, st>>>(d_row, n, counts);
   na_fill<<<sms * 2, 256, 0, st>>>(d_row, n, counts, cls, bch);
@@ -179,15 +180,11 @@ extern "C" wbpr_status wbpr_solve_bcsr_noalloc(int32_t n, int64_t num_residual_a
   p.fr[0] = va(10);
   p.fr[1] = va(11);
   p.fr[2] = va(12);
-  p.dq = va(13);
-  p.dbase = va(14);
-  p.dE = va(15);
-  p.derem = va(16);
-  p.dmin0 = va(17);
+  p.dmin0 = va(13);
   p.cls = cls;
   for (int k = 0; k < 3; ++k) p.frh[k] = (int2*)(base + kOffFrh) + (long long)k * kTdItems;
-  p.hown = base + kOffChunk;
-  p.hsum = p.hown + kChunkItems;
+  p.hrec = (int4*)(base + kOffChunk);
+  p.hsum = base + kOffChunk + 12 * kChunkItems;
   p.hmin = p.hsum + kChunkItems;
   p.bch = bch;
   p.n_light = hc[0];

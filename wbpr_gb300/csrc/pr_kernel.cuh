@@ -287,12 +287,9 @@ struct Params {
   int* lq[2];
   int* hq[2];      // heavy active vertices (rows longer than heavy_deg)
   int* esnap;      // excess of each active vertex when it was filed for the round
-  int* dq;         // deep entries: heavy vertices with excess left after chunk 0
-  int* dbase;      //   first chunk item of the entry
-  int* dE;         //   excess snapshot of the round
-  int* derem;      //   excess left after chunk 0
-  int* dmin0;      //   min label over chunk 0's remaining residual arcs
-  int* hown;       // chunk item -> deep entry
+  int* dmin0;      // deep entry -> min label over the first part's remaining residual arcs
+  int4* hrec;      // chunk item -> 3 x int4: {u, first item, E, E left}, {label, items, entry, 0},
+                   //   the vertex's row {b0, d0, b1, deg}: all a block needs, in one load
   int* hsum;       // chunk item -> admissible residual (saturated)
   int* hmin;       // chunk item -> min label over other residual arcs
   int* qraw;
@@ -377,15 +374,25 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ unsigned atom_add_release(unsigned* p, unsigned x) {
+  unsigned old;
+  asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(x) : "memory");
+  return old;
+}
+// The block's writes are ordered before thread 0's arrival by the block
+// barrier and the release of the arrival; the acquire load that sees bit 31
+// flip (or, for the last arrival, the count complete) orders the block's
+// later reads after every other block's arrival.  Measured on GB300: 2.1 us
+// per barrier at 456 blocks, against 2.4 us with full fences around a
+// relaxed atomic.
 __device__ __forceinline__ bool grid_sync(Ctl* c, unsigned long long timeout_ns) {
   __syncthreads();
   if (gridDim.x == 1) return ldv(&c->err) == 0;  // a one-block grid: the block barrier is enough
   if (threadIdx.x == 0) {
     const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
-    __threadfence();
-    const unsigned old = atomicAdd(&c->bar, add);
+    const unsigned old = atom_add_release(&c->bar, add);
     if (((old + add) ^ old) & 0x80000000u) {
-      // last arrival: nothing to wait for
+      ld_acquire(&c->bar);  // last arrival
     } else {
       const unsigned long long t0 = gtime();
       while (!((ld_acquire(&c->bar) ^ old) & 0x80000000u)) {
@@ -395,7 +402,6 @@ __device__ __forceinline__ bool grid_sync(Ctl* c, unsigned long long timeout_ns)
         }
       }
     }
-    __threadfence();
   }
   __syncthreads();
   return ldv(&c->err) == 0;
@@ -476,8 +482,8 @@ __device__ __forceinline__ void vidx(const VRow& r, int vi, int& k, int& a) {
 // than `limit` and that keeps excess becomes a deep entry: its remaining
 // chunks are processed by whole blocks (deep passes A and B).
 template <class Topo>
-__device__ __forceinline__ void make_deep(const Params<Topo>& p, int u, int E, int erem, int mn, int from,
-                                          int deg);
+__device__ __forceinline__ void make_deep(const Params<Topo>& p, int u, int E, int erem, int mn, int from, int hu,
+                                          const VRow& r);
 
 template <class Topo, int W, int Q>
 __device__ __forceinline__ void tile_discharge(const Params<Topo>& p, int u, int limit, int* rawcnt,
@@ -563,7 +569,7 @@ __device__ __forceinline__ void tile_discharge(const Params<Topo>& p, int u, int
   if (lane == 0) {
     atomicAdd(&acc.scanned, scanned);
     if (erem > 0 && r.deg > hi) {
-      make_deep(p, u, eu, (int)erem, minh, hi, r.deg);
+      make_deep(p, u, eu, (int)erem, minh, hi, hu, r);
     } else {
       const int D = eu - (int)erem;
       bool self = true;
@@ -743,18 +749,20 @@ __device__ __forceinline__ unsigned ordered_push(const Params<Topo>& p, const VR
 // A vertex that kept excess after the first `from` arcs of its row: its
 // remaining arcs are cut into kChunk chunks for the deep passes.
 template <class Topo>
-__device__ __forceinline__ void make_deep(const Params<Topo>& p, int u, int E, int erem, int mn, int from,
-                                          int deg) {
+__device__ __forceinline__ void make_deep(const Params<Topo>& p, int u, int E, int erem, int mn, int from, int hu,
+                                          const VRow& r) {
   Ctl* c = p.ctl;
-  const int nch = (deg - from + kChunk - 1) / kChunk;
+  const int nch = (r.deg - from + kChunk - 1) / kChunk;
   const unsigned long long old = atomicAdd(&c->dpack, (1ull << 32) | (unsigned long long)nch);
   const int di = (int)(old >> 32), base = (int)(old & 0xffffffffu);
-  p.dq[di] = u;
-  p.dbase[di] = base;
-  p.dE[di] = E;
-  p.derem[di] = erem;
   p.dmin0[di] = mn;
-  for (int j = 0; j < nch; ++j) p.hown[base + j] = di;
+  const int4 a = make_int4(u, base, E, erem), b = make_int4(hu, nch, di, 0), rr = make_int4(r.b0, r.d0, r.b1, r.deg);
+  for (int j = 0; j < nch; ++j) {
+    int4* q = p.hrec + 3LL * (base + j);
+    q[0] = a;
+    q[1] = b;
+    q[2] = rr;
+  }
 }
 
 struct DeepMeta {
@@ -766,15 +774,20 @@ template <class Topo>
 __device__ __forceinline__ void deep_meta(const Params<Topo>& p, int k, DeepMeta* m) {
   __shared__ DeepMeta s_m;
   if (threadIdx.x == 0) {
-    s_m.di = __ldcg(p.hown + k);
-    s_m.u = __ldcg(p.dq + s_m.di);
-    s_m.base = __ldcg(p.dbase + s_m.di);
-    s_m.E = __ldcg(p.dE + s_m.di);
-    s_m.Er = __ldcg(p.derem + s_m.di);
-    s_m.hu = __ldcg(p.lab + s_m.u);
+    const int4* q = p.hrec + 3LL * k;
+    const int4 a = __ldcg(q), b = __ldcg(q + 1), rr = __ldcg(q + 2);
+    s_m.u = a.x;
+    s_m.base = a.y;
+    s_m.E = a.z;
+    s_m.Er = a.w;
+    s_m.hu = b.x;
+    s_m.nch = b.y;
+    s_m.di = b.z;
     s_m.j = k - s_m.base;
-    s_m.r = vrow(p.g, s_m.u);
-    s_m.nch = (s_m.r.deg - kFirst + kChunk - 1) / kChunk;
+    s_m.r.b0 = rr.x;
+    s_m.r.d0 = rr.y;
+    s_m.r.b1 = rr.z;
+    s_m.r.deg = rr.w;
   }
   __syncthreads();
   *m = s_m;
