@@ -1223,8 +1223,7 @@ struct RunCfg {
 
 template <class Topo>
 wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch_ms) {
-  Params<Topo> p;
-  std::memset(&p, 0, sizeof(p));
+  Params<Topo> p{};  // every field zero unless it has its own initializer
   topo_of(g, p.g);
   fill_common(g, p);
   p.s = rc.s;

@@ -159,8 +159,7 @@ extern "C" wbpr_status wbpr_solve_bcsr_noalloc(int32_t n, int64_t num_residual_a
   NA_CK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st));
   NA_CK(cudaStreamSynchronize(st));
 
-  Params<TopoB> p;
-  std::memset(&p, 0, sizeof(p));
+  Params<TopoB> p{};  // every field zero unless it has its own initializer
   p.g.row = d_row;
   p.g.arc = arc;
   p.g.arx = arx;
