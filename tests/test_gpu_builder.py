@@ -76,6 +76,21 @@ def test_device_overflow_check(layout):
     # at the limit exactly it builds
     g = W.Graph.from_arcs(3, [0, 1], [2, 2], [2**31 - 2, 1], 0, 2)
     same_as_host(g)
+    # a head whose 100 incoming arcs span several warps of the sorted order,
+    # between arcs into other vertices: exactly at the limit, then one above
+    k = 100
+    c = (2**31 - 1) // k
+    tails = [0] * k + [2] * 40
+    heads = [1] * k + [3] * 40
+    caps = [c] * (k - 1) + [2**31 - 1 - c * (k - 1)] + [7] * 40
+    order = np.random.default_rng(1).permutation(len(tails))
+    g = W.Graph.from_arcs(4, np.array(tails)[order], np.array(heads)[order], np.array(caps)[order], 0, 3)
+    same_as_host(g)
+    caps[0] += 1
+    g = W.Graph.from_arcs(4, np.array(tails)[order], np.array(heads)[order], np.array(caps)[order], 0, 3)
+    with pytest.raises(W.WbprError) as ei:
+        W.DeviceGraph(g, layout)
+    assert ei.value.status == 4
 
 
 def test_read_back_matches_the_layout():
@@ -97,7 +112,8 @@ def test_device_build_rejects_invalid_input(layout):
         return W.Graph(4, np.array(off, np.int32), np.array(dst, np.int32), np.array(cap, np.int32), 0, 3)
     bad = [make([0, 2, 3, 4, 4], [1, 4, 2, 3], [1, 1, 1, 1]),     # head out of range
            make([0, 2, 3, 4, 4], [1, 2, 2, 3], [1, -1, 1, 1]),    # negative capacity
-           make([0, 3, 1, 4, 4], [1, 2, 2, 3], [1, 1, 1, 1])]     # offsets decrease
+           make([0, 3, 1, 4, 4], [1, 2, 2, 3], [1, 1, 1, 1]),     # offsets decrease
+           make([0, 2, 3, 4, 4], [1, -1, 2, 3], [1, 1, 1, 1])]    # negative head
     for g in bad:
         with pytest.raises(W.WbprError) as ei:
             W.DeviceGraph(g, layout)
