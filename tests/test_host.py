@@ -40,6 +40,16 @@ def test_no_device_is_reported_not_faked(has_gpu):
     with pytest.raises(W.WbprError) as ei:
         W.DeviceGraph(g, "bcsr")
     assert ei.value.status == 7  # WBPR_ERR_NO_DEVICE
+    with pytest.raises(W.WbprError) as ei:
+        W.memory_cache(1 << 30)
+    assert ei.value.status == 7
+
+
+def test_memory_cache_rejects_negative_sizes():
+    # checked before any device is touched
+    with pytest.raises(W.WbprError) as ei:
+        W.memory_cache(-1)
+    assert ei.value.status == 1
 
 
 def test_dimacs_roundtrip(tmp_path, golden):
