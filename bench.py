@@ -280,8 +280,8 @@ def run_ours(args) -> None:
     achieved = alg / (launch_ms * 1e-3) / 1e9
     prof = profile_traffic()
     traffic = prof.get("dram_bytes_per_launch") if prof else None
-    # the input CSR crosses once (offsets, heads, capacities); BCSR is built in HBM
-    h2d = 8 * g.m + 4 * (g.n + 1) if args.layout == "bcsr" else 32 * g.m + 8 * (g.n + 1)
+    # the input CSR crosses once (offsets, heads, capacities); either layout is built in HBM
+    h2d = 8 * g.m + 4 * (g.n + 1)
     dg.close()
     # e2e through the C ABI from host buffers: the input CSR sits in pinned
     # host memory (set up once, outside the timed region); every step copies
