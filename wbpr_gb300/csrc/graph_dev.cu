@@ -63,7 +63,16 @@ cudaError_t pool_alloc_on(void** p, size_t bytes, cudaStream_t stream) {
   if (e != cudaSuccess) return e;
   cudaMemPool_t pool = device_pool(dev);
   if (!pool) return cudaErrorMemoryAllocation;
-  return cudaMallocFromPoolAsync(p, bytes, pool, stream);
+  e = cudaMallocFromPoolAsync(p, bytes, pool, stream);
+  if (e == cudaErrorMemoryAllocation) {
+    // the free blocks the pool keeps may be of other sizes: hand them back
+    // to the driver (blocks in use stay) and map the request anew
+    cudaGetLastError();
+    cudaStreamSynchronize(stream);
+    cudaMemPoolTrimTo(pool, 0);
+    e = cudaMallocFromPoolAsync(p, bytes, pool, stream);
+  }
+  return e;
 }
 
 cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t stream) {
