@@ -5,6 +5,7 @@
 // host threads.
 #include <algorithm>
 #include <atomic>
+#include <cerrno>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -14,6 +15,11 @@
 #include <system_error>
 #include <thread>
 #include <vector>
+
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include "wbpr_internal.h"
 
@@ -145,22 +151,60 @@ wbpr_status to_host_csr(Csr&& c, wbpr_host_csr** out) {
 }
 
 // ---------------------------------------------------------------------------
-// File readers.  The whole file is read once and parsed by hand; malformed or
-// truncated input returns WBPR_ERR_IO instead of the reference's undefined
-// behaviour.
-static bool slurp(const char* path, std::string* buf) {
-  if (!path) return false;
-  FILE* f = std::fopen(path, "rb");
-  if (!f) return false;
-  std::fseek(f, 0, SEEK_END);
-  long sz = std::ftell(f);
-  std::fseek(f, 0, SEEK_SET);
-  if (sz < 0) { std::fclose(f); return false; }
-  buf->resize((size_t)sz);
-  size_t got = sz ? std::fread(&(*buf)[0], 1, (size_t)sz, f) : 0;
-  std::fclose(f);
-  return got == (size_t)sz;
-}
+// File readers.  The file's bytes are mapped (read into memory when they
+// cannot be) and parsed by hand; malformed or truncated input returns
+// WBPR_ERR_IO instead of the reference's undefined behaviour.
+namespace {
+class FileBytes {
+ public:
+  FileBytes() = default;
+  FileBytes(const FileBytes&) = delete;
+  FileBytes& operator=(const FileBytes&) = delete;
+  ~FileBytes() {
+    if (map_) munmap(map_, len_);
+  }
+  // A regular file is mapped read-only (no copy, pages fault in on the
+  // threads that parse them); anything else is read.
+  bool open(const char* path) {
+    if (!path) return false;
+    const int fd = ::open(path, O_RDONLY);
+    if (fd < 0) return false;
+    struct stat st;
+    if (fstat(fd, &st) == 0 && S_ISREG(st.st_mode) && st.st_size > 0) {
+      void* q = mmap(nullptr, (size_t)st.st_size, PROT_READ, MAP_PRIVATE, fd, 0);
+      if (q != MAP_FAILED) {
+        madvise(q, (size_t)st.st_size, MADV_WILLNEED);
+        map_ = q;
+        len_ = (size_t)st.st_size;
+        ::close(fd);
+        return true;
+      }
+    }
+    std::string buf;
+    char chunk[1 << 16];
+    for (;;) {
+      const ssize_t r = ::read(fd, chunk, sizeof(chunk));
+      if (r < 0 && errno == EINTR) continue;
+      if (r < 0) {
+        ::close(fd);
+        return false;
+      }
+      if (r == 0) break;
+      buf.append(chunk, (size_t)r);
+    }
+    ::close(fd);
+    own_.swap(buf);
+    return true;
+  }
+  const char* data() const { return map_ ? (const char*)map_ : own_.data(); }
+  size_t size() const { return map_ ? len_ : own_.size(); }
+
+ private:
+  void* map_ = nullptr;
+  size_t len_ = 0;
+  std::string own_;
+};
+}  // namespace
 
 namespace {
 struct Lines {
@@ -247,8 +291,8 @@ static std::vector<const char*> line_splits(const char* b, const char* e, int T)
 // are parsed by all host threads, each over a piece of the file that starts
 // at a line start, and joined in file order.
 wbpr_status read_dimacs(const char* path, Csr* c) {
-  std::string buf;
-  if (!slurp(path, &buf)) return WBPR_ERR_IO;
+  FileBytes buf;
+  if (!buf.open(path)) return WBPR_ERR_IO;
   Lines L{buf.data(), buf.data() + buf.size()};
   const char *b, *e;
   int64_t n = -1, mdecl = -1;
@@ -290,70 +334,137 @@ wbpr_status read_dimacs(const char* path, Csr* c) {
     std::vector<int32_t> us, vs, cs;
     int32_t s = -1, t = -1;
     bool bad = false;
+    bool sorted = true;  // tails non-decreasing inside the piece
   };
   std::vector<Piece> pc((size_t)std::max(P, 0));
+  // One pass per line: "a u v c" lines are parsed where they stand (a newline
+  // is neither blank nor a digit, so a short line fails its own parse);
+  // comment lines are skipped to their newline.
   auto work = [&](int k) {
     Piece& q = pc[(size_t)k];
     const size_t guess = (size_t)((cut[k + 1] - cut[k]) / 12 + 16);
     q.us.reserve(guess);
     q.vs.reserve(guess);
     q.cs.reserve(guess);
-    Lines LL{cut[k], cut[k + 1]};
-    const char *lb, *le;
-    while (LL.next(&lb, &le)) {
-      const char* p = lb;
-      while (p < le && (*p == ' ' || *p == '\t')) ++p;
-      if (p >= le || *p == 'c') continue;
-      const char kind = *p++;
+    const char* p = cut[k];
+    const char* const end = cut[k + 1];
+    auto to_next_line = [&]() {
+      const void* nl = std::memchr(p, '\n', (size_t)(end - p));
+      p = nl ? (const char*)nl + 1 : end;
+    };
+    int32_t last = -1;
+    while (p < end) {
+      while (p < end && (*p == ' ' || *p == '\t')) ++p;
+      if (p >= end) break;
+      const char kind = *p;
+      if (kind == '\n' || (kind == '\r' && (p + 1 == end || p[1] == '\n')) || kind == 'c') {
+        to_next_line();
+        continue;
+      }
+      ++p;
       if (kind == 'a') {
         int64_t u, v, cap;
-        if (!parse_int(&p, le, &u) || !parse_int(&p, le, &v) || !parse_int(&p, le, &cap) || u < 1 || u > n ||
+        if (!parse_int(&p, end, &u) || !parse_int(&p, end, &v) || !parse_int(&p, end, &cap) || u < 1 || u > n ||
             v < 1 || v > n || cap < 0 || cap > std::numeric_limits<int32_t>::max()) {
           q.bad = true;
           return;
         }
-        q.us.push_back((int32_t)(u - 1));
+        const int32_t tu = (int32_t)(u - 1);
+        if (tu < last) q.sorted = false;
+        last = tu;
+        q.us.push_back(tu);
         q.vs.push_back((int32_t)(v - 1));
         q.cs.push_back((int32_t)cap);
+        to_next_line();  // the rest of the line is ignored
       } else if (kind == 'n') {
+        const char* le = (const char*)std::memchr(p, '\n', (size_t)(end - p));
+        if (!le) le = end;
+        if (le > p && le[-1] == '\r') --le;
         if (!parse_n(p, le, &q.s, &q.t)) {
           q.bad = true;
           return;
         }
+        p = le;
+        to_next_line();
       } else {
         q.bad = true;  // a second problem line or an unknown line kind
         return;
       }
     }
   };
-  try {
+  auto run_pieces = [&](auto&& f) {
     std::vector<std::thread> th;
-    for (int k = 1; k < P; ++k) th.emplace_back(work, k);
-    if (P > 0) work(0);
+    for (int k = 1; k < P; ++k) th.emplace_back(f, k);
+    if (P > 0) f(0);
     for (auto& x : th) x.join();
+  };
+  try {
+    run_pieces(work);
   } catch (const std::system_error&) {
     return WBPR_ERR_IO;
   }
   size_t total = 0;
-  for (const Piece& q : pc) {
+  bool sorted = true;
+  int32_t prev_last = -1;
+  std::vector<size_t> at((size_t)std::max(P, 0) + 1, 0);
+  std::vector<int32_t> tail_before((size_t)std::max(P, 0), -1);  // tail of the arc before each piece
+  for (int k = 0; k < P; ++k) {
+    const Piece& q = pc[(size_t)k];
     if (q.bad) return WBPR_ERR_IO;
+    at[(size_t)k] = total;
+    tail_before[(size_t)k] = prev_last;
     total += q.us.size();
     if (q.s >= 0) s = q.s;
     if (q.t >= 0) t = q.t;
+    if (!q.sorted || (!q.us.empty() && q.us.front() < prev_last)) sorted = false;
+    if (!q.us.empty()) prev_last = q.us.back();
   }
+  at[(size_t)std::max(P, 0)] = total;
   if (total > (size_t)std::numeric_limits<int32_t>::max()) return WBPR_ERR_OVERFLOW;
-  std::vector<int32_t> us(total), vs(total), cs(total);
-  size_t at = 0;
-  for (Piece& q : pc) {
-    std::copy(q.us.begin(), q.us.end(), us.begin() + at);
-    std::copy(q.vs.begin(), q.vs.end(), vs.begin() + at);
-    std::copy(q.cs.begin(), q.cs.end(), cs.begin() + at);
-    at += q.us.size();
-    std::vector<int32_t>().swap(q.us);
-    std::vector<int32_t>().swap(q.vs);
-    std::vector<int32_t>().swap(q.cs);
+  if (sorted) {
+    // Arcs already grouped by tail (the usual layout of DIMACS files): every
+    // piece goes straight into place, and writes the row offsets of the
+    // tails it starts (off[x] for prev tail < x <= first tail of a run).
+    c->n = (int32_t)n;
+    c->m = (int64_t)total;
+    c->off.assign((size_t)n + 1, 0);
+    c->dst.resize(total);
+    c->cap.resize(total);
+    auto place = [&](int k) {
+      Piece& q = pc[(size_t)k];
+      const size_t base = at[(size_t)k];
+      std::copy(q.vs.begin(), q.vs.end(), c->dst.begin() + (std::ptrdiff_t)base);
+      std::copy(q.cs.begin(), q.cs.end(), c->cap.begin() + (std::ptrdiff_t)base);
+      int32_t prev = tail_before[(size_t)k];
+      for (size_t j = 0; j < q.us.size(); ++j) {
+        const int32_t u = q.us[j];
+        for (int32_t x = prev + 1; x <= u; ++x) c->off[(size_t)x] = (int32_t)(base + j);
+        prev = u;
+      }
+    };
+    try {
+      run_pieces(place);
+    } catch (const std::system_error&) {
+      return WBPR_ERR_IO;
+    }
+    for (int64_t x = (int64_t)prev_last + 1; x <= n; ++x) c->off[(size_t)x] = (int32_t)total;
+  } else {
+    std::vector<int32_t> us(total), vs(total), cs(total);
+    auto join = [&](int k) {
+      Piece& q = pc[(size_t)k];
+      const std::ptrdiff_t base = (std::ptrdiff_t)at[(size_t)k];
+      std::copy(q.us.begin(), q.us.end(), us.begin() + base);
+      std::copy(q.vs.begin(), q.vs.end(), vs.begin() + base);
+      std::copy(q.cs.begin(), q.cs.end(), cs.begin() + base);
+    };
+    try {
+      run_pieces(join);
+    } catch (const std::system_error&) {
+      return WBPR_ERR_IO;
+    }
+    std::vector<Piece>().swap(pc);
+    triples_to_csr((int32_t)n, us, vs, cs, c);
   }
-  triples_to_csr((int32_t)n, us, vs, cs, c);
   c->m_declared = mdecl;
   c->s = s;
   c->t = t;
@@ -364,8 +475,8 @@ wbpr_status read_dimacs(const char* path, Csr* c) {
 // n; other '#' lines are comments; every row is sorted by head; capacity 1.
 // Without the header, n = 1 + largest id seen.
 wbpr_status read_snap_txt(const char* path, Csr* c) {
-  std::string buf;
-  if (!slurp(path, &buf)) return WBPR_ERR_IO;
+  FileBytes buf;
+  if (!buf.open(path)) return WBPR_ERR_IO;
   Lines L{buf.data(), buf.data() + buf.size()};
   const char *b, *e;
   int64_t n = -1, mdecl = -1, maxid = -1;
@@ -413,8 +524,8 @@ wbpr_status read_snap_txt(const char* path, Csr* c) {
 // -v 1 : SNAP binary (reference graph.cpp:219-233 writer, 292-314 reader):
 // int32 n, m, m_processed, destinations[m_processed], offsets[n+1]; cap 1.
 wbpr_status read_snap_bin(const char* path, Csr* c) {
-  std::string buf;
-  if (!slurp(path, &buf)) return WBPR_ERR_IO;
+  FileBytes buf;
+  if (!buf.open(path)) return WBPR_ERR_IO;
   if (buf.size() < 12) return WBPR_ERR_IO;
   int32_t hdr[3];
   std::memcpy(hdr, buf.data(), 12);
@@ -450,8 +561,8 @@ struct CacheHeader {
 static_assert(sizeof(CacheHeader) == 48, "cache header layout");
 
 wbpr_status read_graph_cache(const char* path, Csr* c) {
-  std::string buf;
-  if (!slurp(path, &buf)) return WBPR_ERR_IO;
+  FileBytes buf;
+  if (!buf.open(path)) return WBPR_ERR_IO;
   CacheHeader h;
   if (buf.size() < sizeof(h)) return WBPR_ERR_IO;
   std::memcpy(&h, buf.data(), sizeof(h));
