@@ -368,3 +368,49 @@ def test_dimacs_reader_shuffled_and_grouped_arcs(tmp_path):
                 got = subprocess.run(["python3", "-c", code], env=dict(os.environ, WBPR_HOST_THREADS=threads),
                                      capture_output=True, text=True, check=True).stdout.strip()
                 assert got == want, (name, repr(eol), threads)
+
+
+def test_snap_reader_pieces_headers_and_page_sized_files(tmp_path):
+    """SNAP text in any line order, LF or CRLF, 1 or 7 threads: rows come out
+    sorted by head; the last "# Nodes: N Edges: M" header counts wherever it
+    stands, other '#' lines are comments; without a header n is the largest
+    id + 1.  A file of exactly 8192 bytes ending in a comment reads too (the
+    header search never leaves its own line)."""
+    import hashlib
+    rng = np.random.default_rng(5)
+    n, m = 400, 5000
+    tail = rng.integers(0, n - 30, m)
+    head = rng.integers(0, n - 30, m)
+    g = W.Graph.from_arcs(n, tail, head, np.ones(m, np.int32), 0, n - 1)
+    dst = g.dst.copy()
+    for u in range(n):
+        dst[g.off[u]:g.off[u + 1]].sort()
+
+    def digest(n_, off, d):
+        return "%d %d %s" % (n_, len(d), hashlib.sha256(off.tobytes() + d.tobytes()).hexdigest())
+
+    want = digest(n, g.off, dst)
+    code = ("import sys, hashlib; sys.path.insert(0, %r); import wbpr_gb300 as W; g = W.read_snap_txt(sys.argv[1]);"
+            "assert (g.cap == 1).all();"
+            "print(g.n, g.m, hashlib.sha256(g.off.tobytes() + g.dst.tobytes()).hexdigest())" % ROOT)
+    for name, order in (("shuffled", rng.permutation(m)), ("grouped", np.argsort(tail, kind="stable"))):
+        body = [f"{tail[i]}\t{head[i]}" for i in order]
+        body.insert(m // 2, "# FromNodeId\tToNodeId, a comment after the header")
+        lines = ["# Directed graph", f"# Nodes: {n + 7} Edges: 1"] + body[:m // 3] + \
+                [f"# Nodes: {n} Edges: {m}"] + body[m // 3:]  # the later header counts
+        for eol in ("\n", "\r\n"):
+            p = str(tmp_path / f"{name}{len(eol)}.txt")
+            with open(p, "wb") as f:
+                f.write((eol.join(lines) + eol).encode())
+            for threads in ("1", "7"):
+                got = subprocess.run(["python3", "-c", code, p], env=dict(os.environ, WBPR_HOST_THREADS=threads),
+                                     capture_output=True, text=True, check=True).stdout.strip()
+                assert got == want, (name, repr(eol), threads)
+    # no header: n = largest id + 1; padded to one page size exactly, ending in a comment
+    text = "\n".join(f"{tail[i]} {head[i]}" for i in range(50)) + "\n# trailing comment "
+    text += "x" * (8192 - len(text))
+    p = tmp_path / "page.txt"
+    p.write_bytes(text.encode())
+    assert os.path.getsize(p) == 8192
+    h = W.read_snap_txt(str(p))
+    assert h.n == int(max(tail[:50].max(), head[:50].max())) + 1 and h.m == 50

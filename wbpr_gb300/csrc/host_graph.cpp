@@ -268,6 +268,90 @@ wbpr_status triples_to_csr(int32_t n, const std::vector<int32_t>& us,
   }
   return WBPR_OK;
 }
+
+// Arcs parsed by one host thread from one piece of a file.
+struct ArcPiece {
+  std::vector<int32_t> us, vs, cs;  // cs left empty when every capacity is 1
+  bool sorted = true;               // tails non-decreasing inside the piece
+};
+
+// Run f(k) for every piece k, piece 0 on the calling thread.
+template <class F>
+bool run_pieces(int P, F&& f) {
+  try {
+    std::vector<std::thread> th;
+    for (int k = 1; k < P; ++k) th.emplace_back(f, k);
+    if (P > 0) f(0);
+    for (auto& x : th) x.join();
+  } catch (const std::system_error&) {
+    return false;
+  }
+  return true;
+}
+
+// Join pieces parsed in file order into c's CSR with n rows, keeping file
+// order inside each row.  When the tails run non-decreasing through the whole
+// file (the usual layout), every piece is copied straight into place by its
+// own thread, which also writes the row offsets of the tails it starts
+// (off[x] for previous tail < x <= tail); any other order goes through a
+// counting sort.
+wbpr_status pieces_to_csr(int64_t n, std::vector<ArcPiece>& pc, Csr* c) {
+  const int P = (int)pc.size();
+  size_t total = 0;
+  bool sorted = true;
+  int32_t prev_last = -1;
+  std::vector<size_t> at((size_t)P + 1, 0);
+  std::vector<int32_t> tail_before((size_t)P, -1);  // tail of the arc before each piece
+  for (int k = 0; k < P; ++k) {
+    const ArcPiece& q = pc[(size_t)k];
+    at[(size_t)k] = total;
+    tail_before[(size_t)k] = prev_last;
+    total += q.us.size();
+    if (!q.sorted || (!q.us.empty() && q.us.front() < prev_last)) sorted = false;
+    if (!q.us.empty()) prev_last = q.us.back();
+  }
+  at[(size_t)P] = total;
+  if (total > (size_t)std::numeric_limits<int32_t>::max()) return WBPR_ERR_OVERFLOW;
+  if (sorted) {
+    c->n = (int32_t)n;
+    c->m = (int64_t)total;
+    c->off.assign((size_t)n + 1, 0);
+    c->dst.resize(total);
+    c->cap.resize(total);
+    auto place = [&](int k) {
+      const ArcPiece& q = pc[(size_t)k];
+      const size_t base = at[(size_t)k];
+      std::copy(q.vs.begin(), q.vs.end(), c->dst.begin() + (std::ptrdiff_t)base);
+      if (q.cs.empty())
+        std::fill(c->cap.begin() + (std::ptrdiff_t)base, c->cap.begin() + (std::ptrdiff_t)(base + q.vs.size()), 1);
+      else
+        std::copy(q.cs.begin(), q.cs.end(), c->cap.begin() + (std::ptrdiff_t)base);
+      int32_t prev = tail_before[(size_t)k];
+      for (size_t j = 0; j < q.us.size(); ++j) {
+        const int32_t u = q.us[j];
+        for (int32_t x = prev + 1; x <= u; ++x) c->off[(size_t)x] = (int32_t)(base + j);
+        prev = u;
+      }
+    };
+    if (!run_pieces(P, place)) return WBPR_ERR_IO;
+    for (int64_t x = (int64_t)prev_last + 1; x <= n; ++x) c->off[(size_t)x] = (int32_t)total;
+    return WBPR_OK;
+  }
+  std::vector<int32_t> us(total), vs(total), cs(total);
+  auto join = [&](int k) {
+    ArcPiece& q = pc[(size_t)k];
+    const std::ptrdiff_t base = (std::ptrdiff_t)at[(size_t)k];
+    std::copy(q.us.begin(), q.us.end(), us.begin() + base);
+    std::copy(q.vs.begin(), q.vs.end(), vs.begin() + base);
+    if (q.cs.empty())
+      std::fill(cs.begin() + base, cs.begin() + base + (std::ptrdiff_t)q.us.size(), 1);
+    else
+      std::copy(q.cs.begin(), q.cs.end(), cs.begin() + base);
+  };
+  if (!run_pieces(P, join)) return WBPR_ERR_IO;
+  std::vector<ArcPiece>().swap(pc);
+  return triples_to_csr((int32_t)n, us, vs, cs, c);
+}
 }  // namespace
 
 // Split [b, e) into up to T pieces that start at line starts.
@@ -331,21 +415,21 @@ wbpr_status read_dimacs(const char* path, Csr* c) {
   const std::vector<const char*> cut = line_splits(arcs_from, buf.data() + buf.size(), host_threads());
   const int P = (int)cut.size() - 1;
   struct Piece {
-    std::vector<int32_t> us, vs, cs;
     int32_t s = -1, t = -1;
     bool bad = false;
-    bool sorted = true;  // tails non-decreasing inside the piece
   };
   std::vector<Piece> pc((size_t)std::max(P, 0));
+  std::vector<ArcPiece> arcs((size_t)std::max(P, 0));
   // One pass per line: "a u v c" lines are parsed where they stand (a newline
   // is neither blank nor a digit, so a short line fails its own parse);
   // comment lines are skipped to their newline.
   auto work = [&](int k) {
     Piece& q = pc[(size_t)k];
+    ArcPiece& a = arcs[(size_t)k];
     const size_t guess = (size_t)((cut[k + 1] - cut[k]) / 12 + 16);
-    q.us.reserve(guess);
-    q.vs.reserve(guess);
-    q.cs.reserve(guess);
+    a.us.reserve(guess);
+    a.vs.reserve(guess);
+    a.cs.reserve(guess);
     const char* p = cut[k];
     const char* const end = cut[k + 1];
     auto to_next_line = [&]() {
@@ -370,11 +454,11 @@ wbpr_status read_dimacs(const char* path, Csr* c) {
           return;
         }
         const int32_t tu = (int32_t)(u - 1);
-        if (tu < last) q.sorted = false;
+        if (tu < last) a.sorted = false;
         last = tu;
-        q.us.push_back(tu);
-        q.vs.push_back((int32_t)(v - 1));
-        q.cs.push_back((int32_t)cap);
+        a.us.push_back(tu);
+        a.vs.push_back((int32_t)(v - 1));
+        a.cs.push_back((int32_t)cap);
         to_next_line();  // the rest of the line is ignored
       } else if (kind == 'n') {
         const char* le = (const char*)std::memchr(p, '\n', (size_t)(end - p));
@@ -392,79 +476,14 @@ wbpr_status read_dimacs(const char* path, Csr* c) {
       }
     }
   };
-  auto run_pieces = [&](auto&& f) {
-    std::vector<std::thread> th;
-    for (int k = 1; k < P; ++k) th.emplace_back(f, k);
-    if (P > 0) f(0);
-    for (auto& x : th) x.join();
-  };
-  try {
-    run_pieces(work);
-  } catch (const std::system_error&) {
-    return WBPR_ERR_IO;
-  }
-  size_t total = 0;
-  bool sorted = true;
-  int32_t prev_last = -1;
-  std::vector<size_t> at((size_t)std::max(P, 0) + 1, 0);
-  std::vector<int32_t> tail_before((size_t)std::max(P, 0), -1);  // tail of the arc before each piece
-  for (int k = 0; k < P; ++k) {
-    const Piece& q = pc[(size_t)k];
+  if (!run_pieces(P, work)) return WBPR_ERR_IO;
+  for (const Piece& q : pc) {
     if (q.bad) return WBPR_ERR_IO;
-    at[(size_t)k] = total;
-    tail_before[(size_t)k] = prev_last;
-    total += q.us.size();
     if (q.s >= 0) s = q.s;
     if (q.t >= 0) t = q.t;
-    if (!q.sorted || (!q.us.empty() && q.us.front() < prev_last)) sorted = false;
-    if (!q.us.empty()) prev_last = q.us.back();
   }
-  at[(size_t)std::max(P, 0)] = total;
-  if (total > (size_t)std::numeric_limits<int32_t>::max()) return WBPR_ERR_OVERFLOW;
-  if (sorted) {
-    // Arcs already grouped by tail (the usual layout of DIMACS files): every
-    // piece goes straight into place, and writes the row offsets of the
-    // tails it starts (off[x] for prev tail < x <= first tail of a run).
-    c->n = (int32_t)n;
-    c->m = (int64_t)total;
-    c->off.assign((size_t)n + 1, 0);
-    c->dst.resize(total);
-    c->cap.resize(total);
-    auto place = [&](int k) {
-      Piece& q = pc[(size_t)k];
-      const size_t base = at[(size_t)k];
-      std::copy(q.vs.begin(), q.vs.end(), c->dst.begin() + (std::ptrdiff_t)base);
-      std::copy(q.cs.begin(), q.cs.end(), c->cap.begin() + (std::ptrdiff_t)base);
-      int32_t prev = tail_before[(size_t)k];
-      for (size_t j = 0; j < q.us.size(); ++j) {
-        const int32_t u = q.us[j];
-        for (int32_t x = prev + 1; x <= u; ++x) c->off[(size_t)x] = (int32_t)(base + j);
-        prev = u;
-      }
-    };
-    try {
-      run_pieces(place);
-    } catch (const std::system_error&) {
-      return WBPR_ERR_IO;
-    }
-    for (int64_t x = (int64_t)prev_last + 1; x <= n; ++x) c->off[(size_t)x] = (int32_t)total;
-  } else {
-    std::vector<int32_t> us(total), vs(total), cs(total);
-    auto join = [&](int k) {
-      Piece& q = pc[(size_t)k];
-      const std::ptrdiff_t base = (std::ptrdiff_t)at[(size_t)k];
-      std::copy(q.us.begin(), q.us.end(), us.begin() + base);
-      std::copy(q.vs.begin(), q.vs.end(), vs.begin() + base);
-      std::copy(q.cs.begin(), q.cs.end(), cs.begin() + base);
-    };
-    try {
-      run_pieces(join);
-    } catch (const std::system_error&) {
-      return WBPR_ERR_IO;
-    }
-    std::vector<Piece>().swap(pc);
-    triples_to_csr((int32_t)n, us, vs, cs, c);
-  }
+  const wbpr_status st = pieces_to_csr(n, arcs, c);
+  if (st) return st;
   c->m_declared = mdecl;
   c->s = s;
   c->t = t;
@@ -472,51 +491,110 @@ wbpr_status read_dimacs(const char* path, Csr* c) {
 }
 
 // -v 0 : SNAP text (reference graph.cpp:28-67).  "# Nodes: N Edges: M" gives
-// n; other '#' lines are comments; every row is sorted by head; capacity 1.
-// Without the header, n = 1 + largest id seen.
+// n (the last such header counts); other '#' lines are comments; every row is
+// sorted by head; capacity 1.  Without the header, n = 1 + largest id seen.
+// Parsed like DIMACS: one piece of the file per host thread, one pass per
+// line, headers searched within their own line only.
 wbpr_status read_snap_txt(const char* path, Csr* c) {
   FileBytes buf;
   if (!buf.open(path)) return WBPR_ERR_IO;
-  Lines L{buf.data(), buf.data() + buf.size()};
-  const char *b, *e;
-  int64_t n = -1, mdecl = -1, maxid = -1;
-  std::vector<int32_t> us, vs;
-  while (L.next(&b, &e)) {
-    const char* p = b;
-    while (p < e && (*p == ' ' || *p == '\t')) ++p;
-    if (p >= e) continue;
-    if (*p == '#') {
-      const char* k = std::strstr(p, "Nodes:");
-      if (k && k < e) {
-        const char* q = k + 6;
-        int64_t nn, mm;
-        if (!parse_int(&q, e, &nn)) return WBPR_ERR_IO;
-        const char* k2 = std::strstr(q, "Edges:");
-        if (!k2 || k2 >= e) return WBPR_ERR_IO;
-        q = k2 + 6;
-        if (!parse_int(&q, e, &mm)) return WBPR_ERR_IO;
-        if (nn <= 0 || nn > std::numeric_limits<int32_t>::max() - 2) return WBPR_ERR_IO;
-        n = nn;
-        mdecl = mm;
+  const char* const data = buf.data();
+  const std::vector<const char*> cut = line_splits(data, data + buf.size(), host_threads());
+  const int P = (int)cut.size() - 1;
+  struct Piece {
+    int64_t n = -1, mdecl = -1;  // the piece's last "# Nodes: N Edges: M" header
+    int64_t maxid = -1;
+    bool bad = false;
+  };
+  std::vector<Piece> pc((size_t)std::max(P, 0));
+  std::vector<ArcPiece> arcs((size_t)std::max(P, 0));
+  static const char kNodes[] = "Nodes:";
+  static const char kEdges[] = "Edges:";
+  constexpr int32_t kMaxId = std::numeric_limits<int32_t>::max() - 2;
+  auto work = [&](int k) {
+    Piece& q = pc[(size_t)k];
+    ArcPiece& a = arcs[(size_t)k];
+    const size_t guess = (size_t)((cut[k + 1] - cut[k]) / 10 + 16);
+    a.us.reserve(guess);
+    a.vs.reserve(guess);
+    const char* p = cut[k];
+    const char* const end = cut[k + 1];
+    auto to_next_line = [&]() {
+      const void* nl = std::memchr(p, '\n', (size_t)(end - p));
+      p = nl ? (const char*)nl + 1 : end;
+    };
+    int32_t last = -1;
+    while (p < end) {
+      while (p < end && (*p == ' ' || *p == '\t')) ++p;
+      if (p >= end) break;
+      const char ch = *p;
+      if (ch == '\n' || (ch == '\r' && (p + 1 == end || p[1] == '\n'))) {
+        to_next_line();
+        continue;
       }
-      continue;
+      if (ch == '#') {
+        const char* le = (const char*)std::memchr(p, '\n', (size_t)(end - p));
+        if (!le) le = end;
+        if (le > p && le[-1] == '\r') --le;
+        const char* kn = std::search(p, le, kNodes, kNodes + 6);
+        if (kn != le) {
+          const char* r = kn + 6;
+          int64_t nn, mm;
+          if (!parse_int(&r, le, &nn)) {
+            q.bad = true;
+            return;
+          }
+          const char* ke = std::search(r, le, kEdges, kEdges + 6);
+          if (ke == le) {
+            q.bad = true;
+            return;
+          }
+          r = ke + 6;
+          if (!parse_int(&r, le, &mm) || nn <= 0 || nn > kMaxId) {
+            q.bad = true;
+            return;
+          }
+          q.n = nn;
+          q.mdecl = mm;
+        }
+        p = le;
+        to_next_line();
+        continue;
+      }
+      int64_t u, v;
+      if (!parse_int(&p, end, &u) || !parse_int(&p, end, &v) || u < 0 || v < 0 || u > kMaxId || v > kMaxId) {
+        q.bad = true;
+        return;
+      }
+      q.maxid = std::max(q.maxid, std::max(u, v));
+      if ((int32_t)u < last) a.sorted = false;
+      last = (int32_t)u;
+      a.us.push_back((int32_t)u);
+      a.vs.push_back((int32_t)v);
+      to_next_line();  // the rest of the line is ignored
     }
-    int64_t u, v;
-    if (!parse_int(&p, e, &u) || !parse_int(&p, e, &v)) return WBPR_ERR_IO;
-    if (u < 0 || v < 0 || u > std::numeric_limits<int32_t>::max() - 2 ||
-        v > std::numeric_limits<int32_t>::max() - 2)
-      return WBPR_ERR_IO;
-    maxid = std::max(maxid, std::max(u, v));
-    us.push_back((int32_t)u);
-    vs.push_back((int32_t)v);
+  };
+  if (!run_pieces(P, work)) return WBPR_ERR_IO;
+  int64_t n = -1, mdecl = -1, maxid = -1;
+  for (const Piece& q : pc) {
+    if (q.bad) return WBPR_ERR_IO;
+    if (q.n >= 0) {
+      n = q.n;
+      mdecl = q.mdecl;
+    }
+    maxid = std::max(maxid, q.maxid);
   }
   if (n < 0) n = maxid + 1;
   if (n <= 0) return WBPR_ERR_IO;
   if (maxid >= n) return WBPR_ERR_IO;
-  std::vector<int32_t> cs(us.size(), 1);
-  triples_to_csr((int32_t)n, us, vs, cs, c);
-  for (int32_t u = 0; u < c->n; ++u)
-    std::sort(c->dst.begin() + c->off[u], c->dst.begin() + c->off[u + 1]);
+  const wbpr_status st = pieces_to_csr(n, arcs, c);
+  if (st) return st;
+  parallel_for(c->n, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t u = lo; u < hi; ++u) {
+      const auto b = c->dst.begin() + c->off[(size_t)u], e = c->dst.begin() + c->off[(size_t)u + 1];
+      if (!std::is_sorted(b, e)) std::sort(b, e);
+    }
+  });
   c->m_declared = mdecl < 0 ? c->m : mdecl;
   return WBPR_OK;
 }
