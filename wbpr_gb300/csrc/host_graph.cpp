@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cerrno>
+#include <charconv>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1087,6 +1088,55 @@ wbpr_status build_rcsr_dev(const wbpr_csr* g, Rcsr* out) {
   return WBPR_OK;
 }
 
+namespace {
+// "<kind> x y z\n" appended to s.
+void append_line(std::string& s, char kind, int64_t x, int64_t y, int64_t z) {
+  char b[80];
+  char* p = b;
+  *p++ = kind;
+  for (int64_t v : {x, y, z}) {
+    *p++ = ' ';
+    p = std::to_chars(p, b + sizeof(b), v).ptr;
+  }
+  *p++ = '\n';
+  s.append(b, (size_t)(p - b));
+}
+
+// The arc lines of a CSR, in arc order, formatted by every host thread into
+// its own buffer (2M arcs each per batch, so memory stays bounded) and
+// written in order.  fmt(s, u, i) appends the line of arc i (tail u), or
+// nothing.
+template <class Fmt>
+bool write_arc_lines(FILE* f, const wbpr_csr* g, Fmt&& fmt) {
+  const int64_t m = g->num_edges;
+  const int32_t n = g->num_nodes;
+  const int T = host_threads();
+  constexpr int64_t kPer = 1 << 21;
+  std::vector<std::string> out((size_t)T);
+  for (int64_t a0 = 0; a0 < m; a0 += kPer * T) {
+    auto work = [&](int k) {
+      std::string& s = out[(size_t)k];
+      s.clear();
+      const int64_t a = a0 + kPer * k, b = std::min(m, a + kPer);
+      if (a >= b) return;
+      s.reserve((size_t)(b - a) * 24);
+      int32_t u = (int32_t)(std::upper_bound(g->offsets, g->offsets + (size_t)n + 1, (int64_t)a,
+                                             [](int64_t x, int32_t o) { return x < (int64_t)o; }) -
+                            g->offsets) - 1;
+      for (int64_t i = a; i < b; ++i) {
+        while ((int64_t)g->offsets[u + 1] <= i) ++u;
+        fmt(s, u, i);
+      }
+    };
+    if (!run_pieces(T, work)) return false;
+    for (const std::string& s : out)
+      if (!s.empty() && std::fwrite(s.data(), 1, s.size(), f) != s.size()) return false;
+  }
+  return true;
+}
+
+}  // namespace
+
 }  // namespace wbpr
 
 // ===========================================================================
@@ -1188,10 +1238,10 @@ wbpr_status wbpr_write_dimacs_flow(const char* path, const wbpr_csr* g, int64_t 
   if (!f) return WBPR_ERR_IO;
   std::fprintf(f, "c maximum flow from %d to %d (1-based ids)\n", g->source + 1, g->sink + 1);
   std::fprintf(f, "s %lld\n", (long long)flow);
-  for (int32_t u = 0; u < g->num_nodes; ++u)
-    for (int32_t i = g->offsets[u]; i < g->offsets[u + 1]; ++i)
-      if (arc_flow[i] > 0) std::fprintf(f, "f %d %d %d\n", u + 1, g->destinations[i] + 1, arc_flow[i]);
-  return std::fclose(f) == 0 ? WBPR_OK : WBPR_ERR_IO;
+  const bool ok = write_arc_lines(f, g, [&](std::string& s, int32_t u, int64_t i) {
+    if (arc_flow[i] > 0) append_line(s, 'f', u + 1, (int64_t)g->destinations[i] + 1, arc_flow[i]);
+  });
+  return (std::fclose(f) == 0 && ok) ? WBPR_OK : WBPR_ERR_IO;
 }
 
 // Bipartite matching as maximum flow (the paper's super-source /
@@ -1258,11 +1308,10 @@ wbpr_status wbpr_write_dimacs(const char* path, const wbpr_csr* g) {
   std::fprintf(f, "p max %d %lld\n", g->num_nodes, (long long)g->num_edges);
   if (g->source >= 0) std::fprintf(f, "n %d s\n", g->source + 1);
   if (g->sink >= 0) std::fprintf(f, "n %d t\n", g->sink + 1);
-  for (int32_t u = 0; u < g->num_nodes; ++u)
-    for (int32_t i = g->offsets[u]; i < g->offsets[u + 1]; ++i)
-      std::fprintf(f, "a %d %d %d\n", u + 1, g->destinations[i] + 1,
-                   g->capacities ? g->capacities[i] : 1);
-  return std::fclose(f) == 0 ? WBPR_OK : WBPR_ERR_IO;
+  const bool ok = write_arc_lines(f, g, [&](std::string& s, int32_t u, int64_t i) {
+    append_line(s, 'a', u + 1, (int64_t)g->destinations[i] + 1, g->capacities ? g->capacities[i] : 1);
+  });
+  return (std::fclose(f) == 0 && ok) ? WBPR_OK : WBPR_ERR_IO;
 }
 
 #define WBPR_GEN(call)                            \
