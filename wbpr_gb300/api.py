@@ -241,15 +241,38 @@ class Graph:
                      np.asarray(cap, np.int32)[order], s, t)
 
 
+class _HostCsrMemory:
+    """A wbpr_host_csr the library returned: its arrays are viewed in place
+    (no copy) and released with the last numpy array that views them."""
+
+    def __init__(self, ptr):
+        self._ptr = ptr
+
+    def __del__(self):
+        if self._ptr is not None:
+            try:
+                lib().wbpr_host_csr_free(self._ptr)
+            except Exception:  # interpreter shutdown
+                pass
+            self._ptr = None
+
+
+def _viewed(owner, cptr, count: int) -> np.ndarray:
+    if count == 0:
+        return np.zeros(0, np.int32)
+    buf = (C.c_int32 * count).from_address(C.cast(cptr, C.c_void_p).value)
+    buf._owner = owner  # the ctypes array keeps the C memory, the numpy array keeps the ctypes array
+    return np.frombuffer(buf, dtype=np.int32)
+
+
 def _take(ptr) -> Graph:
     h = ptr.contents
     n, m = h.num_nodes, h.num_edges
-    off = np.ctypeslib.as_array(h.offsets, shape=(n + 1,)).copy()
-    dst = np.ctypeslib.as_array(h.destinations, shape=(max(m, 1),))[:m].copy()
-    cap = np.ctypeslib.as_array(h.capacities, shape=(max(m, 1),))[:m].copy()
-    g = Graph(n, off, dst, cap, h.source, h.sink, h.num_edges_declared)
-    lib().wbpr_host_csr_free(ptr)
-    return g
+    owner = _HostCsrMemory(ptr)
+    off = _viewed(owner, h.offsets, n + 1)
+    dst = _viewed(owner, h.destinations, m)
+    cap = _viewed(owner, h.capacities, m)
+    return Graph(n, off, dst, cap, h.source, h.sink, h.num_edges_declared)
 
 
 def _reader(fn: str, path: str) -> Graph:
