@@ -414,3 +414,30 @@ def test_snap_reader_pieces_headers_and_page_sized_files(tmp_path):
     assert os.path.getsize(p) == 8192
     h = W.read_snap_txt(str(p))
     assert h.n == int(max(tail[:50].max(), head[:50].max())) + 1 and h.m == 50
+
+
+@pytest.mark.parametrize("text,off,dst", [
+    ("p max 3 0\nn 1 s\nn 3 t\n", [0, 0, 0, 0], []),                      # no arcs
+    ("p max 3 0\r\nn 1 s\r\nn 3 t", [0, 0, 0, 0], []),                     # CRLF, no final newline
+    ("p max 3 1\nn 1 s\nn 3 t\na 1 3 5", [0, 1, 1, 1], [2]),               # last arc without newline
+    ("p max 3 1\nn 1 s\nn 3 t\n\n   \n\ta 1 3 5\n\n", [0, 1, 1, 1], [2]),  # blank lines, tab-indented arc
+])
+def test_dimacs_reader_edges(tmp_path, text, off, dst):
+    p = tmp_path / "e.dimacs"
+    p.write_bytes(text.encode())
+    g = W.read_dimacs(str(p))
+    assert list(g.off) == off and list(g.dst) == dst and (g.s, g.t) == (0, 2)
+
+
+def test_snap_reader_edges(tmp_path):
+    p = tmp_path / "a.txt"
+    p.write_text("# only a comment\n")
+    with pytest.raises(W.WbprError) as ei:  # no header and no arc: n would be 0
+        W.read_snap_txt(str(p))
+    assert ei.value.status == 6
+    p.write_text("# Nodes: 4 Edges: 0\n")
+    g = W.read_snap_txt(str(p))
+    assert g.n == 4 and g.m == 0 and list(g.off) == [0] * 5
+    p.write_text("0 1")
+    g = W.read_snap_txt(str(p))
+    assert g.n == 2 and list(g.off) == [0, 1, 1] and list(g.dst) == [1]
