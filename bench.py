@@ -155,14 +155,14 @@ def profile_traffic():
 
 
 # ---------------------------------------------------------------------------
-def _serial_sample(seed: int):
+def _serial_sample(seed: int, scale: int = SAMPLE_SCALE):
     """One bounded CPU sample: the reference's serial solver (oracle port) on a
-    scale-11 R-MAT with the workload's parameters."""
+    small R-MAT (scale 11 by default) with the workload's parameters."""
     import oracle
     import wbpr_gb300 as W
 
     w = WORKLOAD
-    g = W.gen_rmat(SAMPLE_SCALE, w["edge_factor"], w["a"], w["b"], w["c"], w["cap_lo"], w["cap_hi"], seed)
+    g = W.gen_rmat(scale, w["edge_factor"], w["a"], w["b"], w["c"], w["cap_lo"], w["cap_hi"], seed)
     t0 = time.perf_counter()
     v, st = oracle.serial_maxflow(g.n, g.off, g.dst, g.cap, g.s, g.t)
     dt = time.perf_counter() - t0
@@ -171,10 +171,10 @@ def _serial_sample(seed: int):
     return g.m, dt, v
 
 
-def cpu_baseline_once() -> dict:
-    m, dt, _ = _serial_sample(WORKLOAD["seed"])
+def cpu_baseline_once(scale: int = SAMPLE_SCALE) -> dict:
+    m, dt, _ = _serial_sample(WORKLOAD["seed"], scale)
     return {"value": m / dt / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"R-MAT scale {SAMPLE_SCALE} (n=2048, m={m}) of the workload's generator, "
+            "sample": f"R-MAT scale {scale} (n={1 << scale}, m={m}) of the workload's generator, "
                       f"seed {WORKLOAD['seed']}: oracle restatement of maxflow-serial, {dt:.2f} s on 1 core"}
 
 
@@ -187,7 +187,7 @@ def run_reference(args) -> None:
     with ctx.Pool(cores) as pool:
         def step(k):
             t0 = time.perf_counter()
-            outs = pool.map(_serial_sample, [1000 + k * cores + i for i in range(cores)])
+            outs = pool.starmap(_serial_sample, [(1000 + k * cores + i, args.sample_scale) for i in range(cores)])
             return sum(o[0] for o in outs), time.perf_counter() - t0
         for k in range(args.warmup):
             step(k)
@@ -205,7 +205,7 @@ def run_reference(args) -> None:
         "config": {"workload": "rmat22_ef16_cap1-100 (bounded samples: scale-11 instances of the same "
                                "generator, one per host core per step)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} parallel scale-{SAMPLE_SCALE} R-MAT instances per step; the "
+                         "sample": f"{cores} parallel scale-{args.sample_scale} R-MAT instances per step; the "
                                    "reference CPU solver maxflow-serial restated in oracle/oracle.c "
                                    "(reference sources are not on the GPU host)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -311,7 +311,7 @@ def run_ours(args) -> None:
                "path": "wbpr_graph_create (H2D of the input CSR from pinned host memory, residual graph "
                        "built on the device) + wbpr_solve + result read-back + wbpr_graph_destroy"}
     if rank == 0:
-        cpu = cpu_baseline_once() if world == 1 and not args.no_cpu_baseline else None
+        cpu = cpu_baseline_once(args.sample_scale) if world == 1 and not args.no_cpu_baseline else None
         workload = "rmat22_ef16_cap1-100" if args.scale == 22 else f"rmat{args.scale}_ef16_cap1-100 (profiling size)"
         last = res[-1]
         line = {
@@ -557,6 +557,8 @@ def main() -> None:
     ap.add_argument("--scale", type=int, default=22, help="R-MAT scale (22 is the benchmark; smaller "
                     "sizes are for profiling captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU sample (profiling)")
+    ap.add_argument("--sample-scale", type=int, default=SAMPLE_SCALE,
+                    help="R-MAT scale of the CPU samples (the baseline and the reference arm)")
     ap.add_argument("--config", type=int, choices=[0, 1, 2, 3, 4], default=1,
                     help="1: the R-MAT benchmark (default); 0: GENRMF 8x16; 2: bipartite matching; "
                     "3: batched instances; 4: grids with the adjoint")
