@@ -100,6 +100,11 @@ typedef struct wbpr_tuning {
                          /* n + arcs <= 16384: one block, block barriers only;    */
                          /* <= 2^21: SMs / 2; <= 2^22: SMs; <= 2^24: 2 x SMs;     */
                          /* larger: every SM x blocks_per_sm)                     */
+  int32_t gr_stall;      /* also relabel globally after this many rounds in a row */
+                         /* that moved no flow into t (0 = auto: 2 when n + arcs  */
+                         /* > 2^22, else never; -1 = never)                       */
+  int64_t barrier_timeout_ns; /* a grid-barrier wait gives up after this long and */
+                         /* the solve returns WBPR_ERR_TIMEOUT (0 = 10 s)         */
 } wbpr_tuning;
 
 typedef struct wbpr_result {
@@ -113,7 +118,9 @@ typedef struct wbpr_result {
   uint64_t vertex_visits;  /* active-vertex discharges                       */
   uint64_t bfs_arcs;       /* arcs inspected by global relabels              */
   uint64_t bfs_vertices;   /* vertex checks by global relabels               */
-  uint64_t alg_bytes;      /* algorithmic bytes from the counters above      */
+  uint64_t alg_bytes;      /* algorithmic bytes of the persistent solver     */
+                           /* launch (bytes_push + bytes_relabel + bytes_gr  */
+                           /* + 12 n of initialisation)                      */
   int32_t rounds;          /* push/relabel supersteps                        */
   int32_t global_relabels; /* BFS passes                                     */
   int32_t stranded;        /* vertices left with excess unable to reach t    */
@@ -122,6 +129,16 @@ typedef struct wbpr_result {
   int32_t bfs_levels;      /* BFS levels over all global relabels            */
   int32_t bfs_bottom_up_levels; /* of which bottom-up                        */
   uint64_t heavy_visits;   /* discharges of rows handled by a whole block    */
+  uint64_t bytes_push;     /* algorithmic bytes of the push phases: 12 per   */
+                           /* arc scanned, 16 per visit, 24 per push (28     */
+                           /* with the undo-log entry)                       */
+  uint64_t bytes_deep;     /* of which the deep passes: 12 per arc           */
+  uint64_t bytes_relabel;  /* relabel phases: 12 per relabel                 */
+  uint64_t bytes_gr;       /* global relabels: 12 per arc inspected, 8 per   */
+                           /* vertex check, 4 n per relabel                  */
+  float deep_ms;           /* deep passes of the push phases (in push_ms)    */
+  int32_t pad0;
+  uint64_t deep_arcs_scanned; /* arcs read by the deep passes (in arcs_scanned) */
 } wbpr_result;
 
 typedef struct wbpr_verify_report {
@@ -347,18 +364,23 @@ wbpr_status wbpr_batch_autotune(wbpr_batch* b, wbpr_tuning* best, float* best_ms
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory (code running inside a caller-owned memory pool or arena, or a
  * framework that forbids cudaMalloc on its hot path): the caller passes the
- * BCSR residual graph in device buffers it owns -- d_row[n+1], d_arc (2 ints
- * per residual arc: head, residual; the residual is reset to the capacity and
- * holds the final residual on return), d_arx (2 ints per residual arc: twin
- * arc, capacity), as produced by wbpr_build_bcsr -- and receives the maximum
- * flow in *flow (host).  All solver scratch lives in one fixed file-scope
- * device array (about 5.6 MB per device, held until exit), so no allocation
- * happens.  Limits: n <= 65536 vertices and num_residual_arcs <= 1048576;
- * larger inputs return WBPR_ERR_INVALID_ARG (see wbpr_last_error).  The first
- * call on a device looks up the array's address; make it before any stream
- * capture.  Calls share the array: calls that overlap on the GPU race and
- * must be serialised by the caller.  `stream` is a cudaStream_t or NULL; the
- * call synchronises it before returning. */
+ * BCSR residual graph in device buffers it owns and receives the maximum flow
+ * in *flow (host).  The buffers interleave the arrays wbpr_build_bcsr writes:
+ *   d_row[n+1]  = offsets;
+ *   d_arc[2a]   = destinations[a], d_arc[2a+1] = residual of arc a (reset
+ *                 to the capacity at the start, the final residual on return);
+ *   d_arx[2a]   = backward_idx[a], d_arx[2a+1] = capacities[a].
+ * They are checked on the device before the solve: d_row must start at 0, end
+ * at num_residual_arcs and never decrease; heads must lie in [0, n), twins be
+ * paired, capacities be >= 0 (WBPR_ERR_INVALID_ARG otherwise); and no vertex's
+ * incoming capacities may sum past int32 (WBPR_ERR_OVERFLOW).  All solver
+ * scratch lives in one fixed file-scope device array (about 5.6 MB per device,
+ * held until exit), so no allocation happens.  Limits: n <= 65536 vertices and
+ * num_residual_arcs <= 1048576; larger inputs return WBPR_ERR_INVALID_ARG (see
+ * wbpr_last_error).  The first call on a device looks up the array's address;
+ * make it before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller.  `stream` is
+ * a cudaStream_t or NULL; the call synchronises it before returning. */
 wbpr_status wbpr_solve_bcsr_noalloc(int32_t n, int64_t num_residual_arcs, const int32_t* d_row,
                                     int32_t* d_arc, const int32_t* d_arx, int32_t s, int32_t t,
                                     int32_t algo, void* stream, int64_t* flow);

@@ -48,7 +48,8 @@ class Tuning(C.Structure):
     _fields_ = [("tile", C.c_int32), ("block", C.c_int32), ("heavy_degree", C.c_int32),
                 ("blocks_per_sm", C.c_int32), ("gr_alpha", C.c_double), ("max_rounds", C.c_int64),
                 ("max_ms", C.c_double), ("verify", C.c_int32), ("trace", C.c_int32),
-                ("gr_rounds", C.c_int32), ("grid_blocks", C.c_int32)]
+                ("gr_rounds", C.c_int32), ("grid_blocks", C.c_int32), ("gr_stall", C.c_int32),
+                ("barrier_timeout_ns", C.c_int64)]
 
 
 class Result(C.Structure):
@@ -58,7 +59,9 @@ class Result(C.Structure):
                 ("bfs_vertices", C.c_uint64), ("alg_bytes", C.c_uint64), ("rounds", C.c_int32),
                 ("global_relabels", C.c_int32), ("stranded", C.c_int32), ("launch_ms", C.c_float),
                 ("push_ms", C.c_float), ("bfs_levels", C.c_int32), ("bfs_bottom_up_levels", C.c_int32),
-                ("heavy_visits", C.c_uint64)]
+                ("heavy_visits", C.c_uint64), ("bytes_push", C.c_uint64), ("bytes_deep", C.c_uint64),
+                ("bytes_relabel", C.c_uint64), ("bytes_gr", C.c_uint64), ("deep_ms", C.c_float),
+                ("pad0", C.c_int32), ("deep_arcs_scanned", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -182,6 +182,7 @@ __global__ void __launch_bounds__(512, 2) pr_batch(BatchParams bp) {
     const int abeg = __ldg(bp.row + in.vbase), aend = __ldg(bp.row + in.vbase + in.n);
     if (threadIdx.x == 0) {
       acc.scanned = acc.pushes = acc.relabels = acc.visits = acc.bfs_arcs = acc.bfs_vertices = acc.wmark = 0;
+      acc.deep = 0;
       acc.fdeg = 0;
       acc.sink = 0;
       bc.lcount[0] = bc.lcount[1] = 0;

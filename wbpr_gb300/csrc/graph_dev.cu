@@ -125,6 +125,12 @@ struct wbpr_graph {
   int2* rarc = nullptr;
   // input row offsets (maps input arc i of u to its residual slot)
   int* ioff = nullptr;
+  // BCSR16 undo log (pr_kernel.cuh): arcs pushed since the residuals were
+  // last restored; `full_reset` asks the next fresh solve to rewrite them all
+  int* ulog = nullptr;
+  int* ulog_n = nullptr;
+  int ulog_cap = 0;
+  bool full_reset = false;
   // per-vertex state and scratch
   int* h = nullptr;
   int* e = nullptr;
@@ -203,6 +209,34 @@ __global__ void reset_bcsr(int2* arc, const int2* arx, long long na) {
   for (long long a = blockIdx.x * (long long)blockDim.x + threadIdx.x; a < na;
        a += (long long)gridDim.x * blockDim.x)
     arc[a].y = __ldg(&arx[a].y);
+}
+// Restore the residuals a BCSR16 solve changed: every logged arc and its twin
+// get their capacity back.  A slot that overflowed (or `full`) makes it a
+// rewrite of all `na` arcs, as reset_bcsr.
+__global__ void reset_logged(int2* arc, const int2* arx, long long na, const int* ulog, const int* ulog_n,
+                             int cap, int full) {
+  __shared__ int s_full;
+  if (threadIdx.x == 0) {
+    int f = full;
+    for (int k = 0; k < kLogSlots; ++k) f |= ulog_n[k * kLogStride + 1];
+    s_full = f;
+  }
+  __syncthreads();
+  const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x, gs = (long long)gridDim.x * blockDim.x;
+  if (s_full) {
+    for (long long a = gt; a < na; a += gs) arc[a].y = __ldg(&arx[a].y);
+    return;
+  }
+  for (int k = 0; k < kLogSlots; ++k) {
+    const int cnt = min(ulog_n[k * kLogStride], cap);
+    const int* lg = ulog + (long long)k * cap;
+    for (long long i = gt; i < cnt; i += gs) {
+      const int a = lg[i];
+      const int2 x = __ldg(arx + a);
+      arc[a].y = x.y;
+      arc[x.x].y = __ldg(&arx[x.x].y);
+    }
+  }
 }
 __global__ void reset_rcsr(int2* farc, int* fcb, const int* fcap, long long m) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m;
@@ -1140,6 +1174,15 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   }
   TRY(dalloc(g, &g->ctl, 1));
   TRY(dalloc(g, &g->st, 1));
+  if (g->layout == WBPR_LAYOUT_BCSR && g->m > 0) {
+    // undo log: an eighth of the residual arcs (at least 2^20 entries), over
+    // kLogSlots slots; the built residuals are the capacities, so it starts empty
+    const int64_t want = std::max<int64_t>((2 * g->m) / 8, (int64_t)1 << 20);
+    g->ulog_cap = (int)((want + kLogSlots - 1) / kLogSlots);
+    TRY(dalloc(g, &g->ulog, (size_t)g->ulog_cap * kLogSlots));
+    TRY(dalloc(g, &g->ulog_n, (size_t)kLogSlots * kLogStride));
+    TRYC(cudaMemset(g->ulog_n, 0, sizeof(int) * (size_t)kLogSlots * kLogStride));
+  }
   TRYC(cudaMemset(g->h, 0, 4 * (size_t)n));
   TRYC(cudaMemset(g->e, 0, 4 * (size_t)n));
 #undef TRY
@@ -1147,6 +1190,9 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   *out = g;
   return WBPR_OK;
 }
+
+// a grid-barrier wait gives up after this long unless the tuning says otherwise
+constexpr unsigned long long kBarrierTimeoutNs = 10ull * 1000 * 1000 * 1000;
 
 template <class Topo>
 void fill_common(wbpr_graph* g, Params<Topo>& p) {
@@ -1178,7 +1224,7 @@ void fill_common(wbpr_graph* g, Params<Topo>& p) {
   p.ctl = g->ctl;
   p.st = g->st;
   p.total_deg = g->total_deg;
-  p.bar_timeout_ns = 10ull * 1000 * 1000 * 1000;
+  p.bar_timeout_ns = kBarrierTimeoutNs;
   p.bfs_dir = 0;
   p.bfs_root = 0;
   p.bfs_excl = -1;
@@ -1191,6 +1237,9 @@ void topo_of(wbpr_graph* g, TopoB& b) {
   b.bd.viol = &g->ctl->viol;
   b.bd.na = 2 * g->m;
   b.bd.n = g->n;
+  b.ulog = g->ulog;
+  b.ulog_n = g->ulog_n;
+  b.ulog_cap = g->ulog_cap;
 }
 void topo_of(wbpr_graph* g, TopoR& r) {
   r.frow = g->frow;
@@ -1203,9 +1252,6 @@ void topo_of(wbpr_graph* g, TopoR& r) {
   r.bd.n = g->n;
 }
 
-// graphs with n + residual arcs up to this run on one block: its phases are
-// then separated by block barriers instead of grid barriers
-constexpr int64_t kOneBlockUnits = 16384;
 
 struct RunCfg {
   int mode;
@@ -1217,8 +1263,10 @@ struct RunCfg {
   int heavy_deg;
   unsigned long long gr_threshold;
   int gr_rounds;
+  int gr_stall;
   long long max_rounds;
   unsigned long long budget_ns;
+  unsigned long long bar_timeout_ns;
   int bfs_dir, bfs_root, bfs_excl;
   int* lab;
   bool trace;
@@ -1241,6 +1289,8 @@ wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch
   p.heavy_deg = rc.heavy_deg;
   p.gr_threshold = rc.gr_threshold;
   p.gr_rounds = rc.gr_rounds;
+  p.gr_stall = rc.gr_stall;
+  if (rc.bar_timeout_ns) p.bar_timeout_ns = rc.bar_timeout_ns;
   p.max_rounds = rc.max_rounds;
   p.budget_ns = rc.budget_ns;
   p.bfs_dir = rc.bfs_dir;
@@ -1281,18 +1331,8 @@ wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch
   }
   const int bps = rc.blocks_per_sm > 0 ? std::min(occ, rc.blocks_per_sm) : occ;
   int blocks = g->sms * bps;
-  if (rc.grid_blocks > 0) {
-    blocks = std::min(blocks, rc.grid_blocks);
-  } else {
-    // Smaller graphs run on fewer blocks: their rounds and BFS levels are
-    // latency-bound, and fewer blocks make every phase's barrier and idle
-    // block cheaper.  Bands measured on GB300 (GENRMF, layered, grids, R-MAT).
-    const int64_t units = (int64_t)g->n + g->total_deg;
-    if (units <= kOneBlockUnits) blocks = 1;
-    else if (units <= (int64_t)1 << 21) blocks = std::min(blocks, std::max(1, g->sms / 2));
-    else if (units <= (int64_t)1 << 22) blocks = std::min(blocks, g->sms);
-    else if (units <= (int64_t)1 << 24) blocks = std::min(blocks, 2 * g->sms);
-  }
+  if (rc.grid_blocks > 0) blocks = std::min(blocks, rc.grid_blocks);
+  else blocks = grid_blocks_for((long long)g->n + g->total_deg, g->sms, blocks);
   CK(cudaMemsetAsync(g->ctl, 0, sizeof(Ctl), g->stream));
   CK(cudaMemsetAsync(g->st, 0, sizeof(Stats), g->stream));
   CK(cudaEventRecord(g->ev2, g->stream));
@@ -1347,6 +1387,10 @@ wbpr_status make_cfg(wbpr_graph* g, int s, int t, wbpr_algo algo, const wbpr_tun
   const double alpha = tu->gr_alpha > 0 ? tu->gr_alpha : 0.75;
   rc->gr_threshold = (unsigned long long)(alpha * ((double)g->n + (double)g->total_deg)) + 1;
   rc->gr_rounds = tu->gr_rounds > 0 ? tu->gr_rounds : 48;
+  if (tu->gr_stall < -1 || tu->barrier_timeout_ns < 0) return WBPR_ERR_INVALID_ARG;
+  rc->gr_stall = tu->gr_stall == 0 ? default_gr_stall((long long)g->n + g->total_deg)
+                                   : (tu->gr_stall < 0 ? 0 : tu->gr_stall);
+  rc->bar_timeout_ns = tu->barrier_timeout_ns > 0 ? (unsigned long long)tu->barrier_timeout_ns : kBarrierTimeoutNs;
   rc->max_rounds = tu->max_rounds;
   rc->trace = tu->trace != 0;
   const double ms = tu->max_ms > 0 ? tu->max_ms : 120000.0;
@@ -1355,19 +1399,40 @@ wbpr_status make_cfg(wbpr_graph* g, int s, int t, wbpr_algo algo, const wbpr_tun
   return WBPR_OK;
 }
 
-uint64_t alg_bytes(const wbpr_graph* g, const Stats& s) {
-  // bytes each counted unit must move (residual layout of this handle)
+// Residuals back to the capacities before a fresh BCSR16 solve: only the arcs
+// the undo log holds, or all of them after a change of capacities.
+void restore_bcsr(wbpr_graph* g) {
+  if (!g->m) return;
+  if (g->ulog) {
+    reset_logged<<<g->sms * 8, 256, 0, g->stream>>>(g->arc, g->arx, 2 * g->m, g->ulog, g->ulog_n, g->ulog_cap,
+                                                    g->full_reset ? 1 : 0);
+  } else {
+    reset_bcsr<<<g->sms * 8, 256, 0, g->stream>>>(g->arc, g->arx, 2 * g->m);
+  }
+  g->full_reset = false;
+}
+
+// Algorithmic bytes of one persistent-kernel launch, by phase, from its
+// counters (the residual restore before the launch is not included).
+struct PhaseBytes {
+  uint64_t push, deep, relabel, gr, init;
+  uint64_t total() const { return push + relabel + gr + init; }  // deep is part of push
+};
+PhaseBytes phase_bytes(const wbpr_graph* g, const Stats& s) {
   const uint64_t arc_b = 12;   // {dst, cf} record + label of the head
   const uint64_t visit_b = 16; // row bounds, excess, label
-  const uint64_t push_b = 24;  // twin index, residual store, twin RMW, excess RMW
+  // twin index, residual store, twin residual read-modify-write, excess
+  // atomic; plus the undo-log entry where the handle keeps one
+  const uint64_t push_b = 24 + (g->ulog ? 4 : 0);
   const uint64_t rel_b = 12;   // relabel record + label store
   const uint64_t bfs_arc_b = 12, bfs_v_b = 8;
-  // reset: BCSR reads cap and writes cf of 2m residual arcs; RCSR writes
-  // cf_f and cf_b and reads cap of m forward arcs
-  const uint64_t reset_b = g->layout == WBPR_LAYOUT_RCSR ? 12ull * g->m : 16ull * g->m;
-  return s.arcs_scanned * arc_b + s.vertex_visits * visit_b + s.pushes * push_b +
-         s.relabels * rel_b + s.bfs_arcs * bfs_arc_b + s.bfs_vertices * bfs_v_b + reset_b +
-         (uint64_t)g->n * 12 + (uint64_t)s.grs * g->n * 4;
+  PhaseBytes b;
+  b.push = s.arcs_scanned * arc_b + s.vertex_visits * visit_b + s.pushes * push_b;
+  b.deep = s.deep_scanned * arc_b;
+  b.relabel = s.relabels * rel_b;
+  b.gr = s.bfs_arcs * bfs_arc_b + s.bfs_vertices * bfs_v_b + (uint64_t)s.grs * g->n * 4;
+  b.init = (uint64_t)g->n * 12;  // labels, excess, relabel records
+  return b;
 }
 
 }  // namespace
@@ -1497,6 +1562,7 @@ wbpr_status wbpr_graph_set_capacities(wbpr_graph* g, const int32_t* capacities) 
   if (h[1] > 0x7fffffffull) return WBPR_ERR_OVERFLOW;
   caps_kernel<<<g->sms * 8, 256, 0, g->stream>>>(g->ioff, bcsr ? g->row : nullptr, g->arc, g->arx, g->farc, g->fcap,
                                                 dcap, g->n, g->m, 1, incap, chk);
+  g->full_reset = true;  // every residual goes back to its new capacity at the next solve
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(g->stream));
   return WBPR_OK;
@@ -1564,7 +1630,7 @@ wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, cons
   if (g->layout == WBPR_LAYOUT_RCSR) {
     if (g->m) reset_rcsr<<<g->sms * 8, 256, 0, g->stream>>>(g->farc, g->fcb, g->fcap, g->m);
   } else {
-    if (g->m) reset_bcsr<<<g->sms * 8, 256, 0, g->stream>>>(g->arc, g->arx, 2 * g->m);
+    restore_bcsr(g);
   }
   CK(cudaGetLastError());
   Stats hs;
@@ -1590,7 +1656,14 @@ wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, cons
     out->rounds = hs.rounds;
     out->global_relabels = hs.grs;
     out->stranded = hs.stranded;
-    out->alg_bytes = alg_bytes(g, hs);
+    const PhaseBytes pb = phase_bytes(g, hs);
+    out->alg_bytes = pb.total();
+    out->bytes_push = pb.push;
+    out->bytes_deep = pb.deep;
+    out->bytes_relabel = pb.relabel;
+    out->bytes_gr = pb.gr;
+    out->deep_ms = (float)(hs.deep_ns * 1e-6);
+    out->deep_arcs_scanned = hs.deep_scanned;
     out->launch_ms = launch_ms;
     out->push_ms = (float)(hs.push_ns * 1e-6);
     out->bfs_levels = hs.bfs_levels;
@@ -1650,7 +1723,7 @@ wbpr_status wbpr_solve_pairs(wbpr_graph* g, int32_t k, const int32_t* sources, c
   if (g->layout == WBPR_LAYOUT_RCSR) {
     if (g->m) reset_rcsr<<<g->sms * 8, 256, 0, g->stream>>>(g->farc, g->fcb, g->fcap, g->m);
   } else {
-    if (g->m) reset_bcsr<<<g->sms * 8, 256, 0, g->stream>>>(g->arc, g->arx, 2 * g->m);
+    restore_bcsr(g);
   }
   CK(cudaGetLastError());
   Stats hs;
@@ -1681,7 +1754,14 @@ wbpr_status wbpr_solve_pairs(wbpr_graph* g, int32_t k, const int32_t* sources, c
     out->rounds = hs.rounds;
     out->global_relabels = hs.grs;
     out->stranded = hs.stranded;
-    out->alg_bytes = alg_bytes(g, hs);
+    const PhaseBytes pb = phase_bytes(g, hs);
+    out->alg_bytes = pb.total();
+    out->bytes_push = pb.push;
+    out->bytes_deep = pb.deep;
+    out->bytes_relabel = pb.relabel;
+    out->bytes_gr = pb.gr;
+    out->deep_ms = (float)(hs.deep_ns * 1e-6);
+    out->deep_arcs_scanned = hs.deep_scanned;
     out->launch_ms = launch_ms;
     out->push_ms = (float)(hs.push_ns * 1e-6);
     out->bfs_levels = hs.bfs_levels;

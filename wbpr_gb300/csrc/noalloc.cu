@@ -78,11 +78,14 @@ __global__ void na_reset(int2* arc, const int2* arx, long long na) {
 }
 
 // counts: [0] light, [1] medium, [2] heavy, [3] long-row chunks,
-//         [4..7] fill cursors of the second pass
-__global__ void na_count(const int* row, int n, int* counts) {
+//         [4..7] fill cursors of the second pass, [8] malformed rows,
+//         [9] malformed arcs, [10] vertices whose incoming capacity passes int32
+__global__ void na_count(const int* row, int n, long long na, int* counts) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (row[0] != 0 || (long long)row[n] != na)) atomicAdd(counts + 8, 1);
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
     const int d = row[v + 1] - row[v];
-    if (d == 0) continue;
+    if (d < 0) atomicAdd(counts + 8, 1);
+    if (d <= 0) continue;
     if (d <= kLightDeg) atomicAdd(counts + 0, 1);
     else if (d <= kHeavyDeg) atomicAdd(counts + 1, 1);
     else {
@@ -110,6 +113,58 @@ __global__ void na_fill(const int* row, int n, int* counts, int* cls, int4* bch)
   }
 }
 
+// The caller's arcs, read before any solver kernel indexes with them: heads
+// in [0, n), twins in [0, na) and paired (twin of twin is the arc itself),
+// capacities >= 0; and each vertex's incoming capacity (the capacities of the
+// twins of its row's arcs, which bound its excess) summed in 64 bits and
+// compared with int32.  Rows of up to kHeavyDeg arcs are summed by a warp
+// each, longer rows by a block per kChunk-arc chunk (the bch items).
+__global__ void na_check(const int* row, const int2* arc, const int2* arx, int n, long long na, const int* cls,
+                         int n_short, const int4* bch, int n_bch, unsigned long long* insum, int* counts) {
+  const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x, gs = (long long)gridDim.x * blockDim.x;
+  int bad = 0;
+  for (long long a = gt; a < na; a += gs) {
+    const int2 r = arc[a], x = arx[a];
+    bool ok = r.x >= 0 && r.x < n && x.x >= 0 && (long long)x.x < na && x.y >= 0;
+    if (ok) ok = arx[x.x].x == (int)a;
+    bad += !ok;
+  }
+  if (bad) atomicAdd(counts + 9, bad);
+  const int lane = threadIdx.x & 31;
+  for (long long w = gt >> 5; w < n_short; w += gs >> 5) {
+    const int v = cls[w];
+    const int b = row[v], e = row[v + 1];
+    unsigned long long sum = 0;
+    for (int a = b + lane; a < e; a += 32) {
+      const int tw = arx[a].x;
+      if (tw >= 0 && (long long)tw < na) sum += (unsigned long long)max(arx[tw].y, 0);
+    }
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if (lane == 0 && sum > 0x7fffffffull) atomicAdd(counts + 10, 1);
+  }
+  __shared__ unsigned long long s_sum;
+  for (int it = blockIdx.x; it < n_bch; it += gridDim.x) {
+    const int4 ch = bch[it];  // {vertex, 0, begin, end}
+    if (threadIdx.x == 0) s_sum = 0;
+    __syncthreads();
+    unsigned long long sum = 0;
+    for (int a = ch.z + threadIdx.x; a < ch.w; a += blockDim.x) {
+      const int tw = arx[a].x;
+      if (tw >= 0 && (long long)tw < na) sum += (unsigned long long)max(arx[tw].y, 0);
+    }
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if (lane == 0 && sum) atomicAdd(&s_sum, sum);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_sum) atomicAdd(insum + ch.x, s_sum);
+    __syncthreads();
+  }
+}
+
+__global__ void na_check_heavy(const int* cls, int first, int nh, const unsigned long long* insum, int* counts) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nh; i += gridDim.x * blockDim.x)
+    if (insum[cls[first + i]] > 0x7fffffffull) atomicAdd(counts + 10, 1);
+}
+
 #define NA_CK(call)                                                          \
   do {                                                                       \
     cudaError_t e_ = (call);                                                 \
@@ -133,8 +188,10 @@ extern "C" wbpr_status wbpr_solve_bcsr_noalloc(int32_t n, int64_t num_residual_a
     return WBPR_ERR_INVALID_ARG;
   }
   if (!d_row || !flow || (num_residual_arcs > 0 && (!d_arc || !d_arx)) || s < 0 || t < 0 || s >= n ||
-      t >= n || s == t || (algo != WBPR_ALGO_TC && algo != WBPR_ALGO_VC))
+      t >= n || s == t || (algo != WBPR_ALGO_TC && algo != WBPR_ALGO_VC)) {
+    wbpr::set_last_error("wbpr_solve_bcsr_noalloc: null buffer, terminal out of range or bad algo");
     return WBPR_ERR_INVALID_ARG;
+  }
   cudaStream_t st = (cudaStream_t)stream;
   int dev = 0, sms = 0;
   NA_CK(cudaGetDevice(&dev));
@@ -147,22 +204,52 @@ extern "C" wbpr_status wbpr_solve_bcsr_noalloc(int32_t n, int64_t num_residual_a
   NA_CK(cudaMemsetAsync(base, 0, sizeof(int) * (size_t)kOffVert, st));
   int2* arc = (int2*)d_arc;
   const int2* arx = (const int2*)d_arx;
-  if (num_residual_arcs > 0) na_reset<<<sms * 4, 256, 0, st>>>(arc, arx, num_residual_arcs);
   int* vert = base + kOffVert;
   auto va = [&](int i) { return vert + (long long)i * kNoAllocMaxVertices; };
   int* cls = va(14);
   int4* bch = (int4*)(base + kOffBch);
-  na_count<<<sms * 2, 256, 0, st>>>(d_row, n, counts);
-  na_fill<<<sms * 2, 256, 0, st>>>(d_row, n, counts, cls, bch);
+  // The rows are checked before anything sizes work by them: the class list
+  // and the chunk items are bounded by the declared arc count only when
+  // row[0] == 0, row[n] == num_residual_arcs and no row is negative.
+  na_count<<<sms * 2, 256, 0, st>>>(d_row, n, num_residual_arcs, counts);
   NA_CK(cudaGetLastError());
-  int hc[4];
+  int hc[11];
   NA_CK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st));
   NA_CK(cudaStreamSynchronize(st));
+  if (hc[8]) {
+    wbpr::set_last_error("wbpr_solve_bcsr_noalloc: d_row must start at 0, end at num_residual_arcs and never "
+                         "decrease");
+    return WBPR_ERR_INVALID_ARG;
+  }
+  na_fill<<<sms * 2, 256, 0, st>>>(d_row, n, counts, cls, bch);
+  // the per-vertex incoming-capacity sums borrow two vertex arrays (active
+  // lists the solver fills before it reads them)
+  unsigned long long* insum = (unsigned long long*)va(4);
+  NA_CK(cudaMemsetAsync(insum, 0, sizeof(unsigned long long) * (size_t)n, st));
+  na_check<<<sms * 2, 256, 0, st>>>(d_row, arc, arx, n, num_residual_arcs, cls, hc[0] + hc[1], bch, hc[3], insum,
+                                    counts);
+  na_check_heavy<<<sms, 256, 0, st>>>(cls, hc[0] + hc[1], hc[2], insum, counts);
+  NA_CK(cudaGetLastError());
+  NA_CK(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, st));
+  NA_CK(cudaStreamSynchronize(st));
+  if (hc[9]) {
+    wbpr::set_last_error("wbpr_solve_bcsr_noalloc: " + std::to_string(hc[9]) +
+                         " residual arcs with a head outside [0, n), an unpaired twin or a negative capacity");
+    return WBPR_ERR_INVALID_ARG;
+  }
+  if (hc[10]) {
+    wbpr::set_last_error("wbpr_solve_bcsr_noalloc: a vertex's incoming capacities sum past int32");
+    return WBPR_ERR_OVERFLOW;
+  }
+  if (num_residual_arcs > 0) na_reset<<<sms * 4, 256, 0, st>>>(arc, arx, num_residual_arcs);
 
   Params<TopoB> p{};  // every field zero unless it has its own initializer
   p.g.row = d_row;
   p.g.arc = arc;
   p.g.arx = arx;
+  p.g.bd.viol = &ctl->viol;  // bounds counted in the checked build only
+  p.g.bd.na = num_residual_arcs;
+  p.g.bd.n = n;
   p.n = n;
   p.s = s;
   p.t = t;
@@ -195,6 +282,7 @@ extern "C" wbpr_status wbpr_solve_bcsr_noalloc(int32_t n, int64_t num_residual_a
   p.total_deg = num_residual_arcs;
   p.gr_threshold = (unsigned long long)(0.75 * ((double)n + (double)num_residual_arcs)) + 1;
   p.gr_rounds = 48;
+  p.gr_stall = default_gr_stall((long long)n + num_residual_arcs);
   p.budget_ns = 120ull * 1000 * 1000 * 1000;
   p.bar_timeout_ns = 10ull * 1000 * 1000 * 1000;
   p.heavy_deg = 32;
@@ -206,12 +294,22 @@ extern "C" wbpr_status wbpr_solve_bcsr_noalloc(int32_t n, int64_t num_residual_a
     wbpr::set_last_error("wbpr_solve_bcsr_noalloc: solver kernel does not fit on an SM");
     return WBPR_ERR_CUDA;
   }
-  NA_CK(launch_pr(p, tile, sms * occ, 256, st));
-  int err = 0, et = 0;
-  NA_CK(cudaMemcpyAsync(&err, &ctl->err, sizeof(int), cudaMemcpyDeviceToHost, st));
-  NA_CK(cudaMemcpyAsync(&et, p.e + t, sizeof(int), cudaMemcpyDeviceToHost, st));
+  NA_CK(launch_pr(p, tile, grid_blocks_for((long long)n + num_residual_arcs, sms, sms * occ), 256, st));
+  int res[3] = {0, 0, 0};  // err, viol, excess(t)
+  NA_CK(cudaMemcpyAsync(res, &ctl->err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  NA_CK(cudaMemcpyAsync(res + 1, &ctl->viol, sizeof(int), cudaMemcpyDeviceToHost, st));
+  NA_CK(cudaMemcpyAsync(res + 2, p.e + t, sizeof(int), cudaMemcpyDeviceToHost, st));
   NA_CK(cudaStreamSynchronize(st));
-  if (err) return (wbpr_status)err;
-  *flow = et;
+  if (res[0]) {
+    wbpr::set_last_error(res[0] == WBPR_ERR_TIMEOUT ? "wbpr_solve_bcsr_noalloc: a grid-barrier wait timed out"
+                                                    : "wbpr_solve_bcsr_noalloc: round or time budget exhausted");
+    return (wbpr_status)res[0];
+  }
+  if (res[1]) {
+    wbpr::set_last_error("wbpr_solve_bcsr_noalloc: bounds check: " + std::to_string(res[1]) +
+                         " out-of-range arc or vertex indices");
+    return WBPR_ERR_VERIFY;
+  }
+  *flow = res[2];
   return WBPR_OK;
 }

@@ -77,6 +77,7 @@ struct Ctl {
   int mcount;       // materialised frontier: short rows
   int mhcount;      //   long-row chunk items
   alignas(128) int gr_ok;  // the rounds since the last global relabel took at least half as long as it
+  int stalled;             // excess(t) has not changed for gr_stall rounds
   int viol;                // out-of-range indices seen by the checked build
   long long dead_deg;      // arcs of the vertices global relabels marked unable to reach the sink
   // work done in rounds of even / odd parity; block b adds to slot b % 32
@@ -94,6 +95,8 @@ struct Stats {
   unsigned long long round_ns;
   unsigned long long push_ns;
   unsigned long long heavy_visits;
+  unsigned long long deep_ns;       // deep passes A and B of the push phases
+  unsigned long long deep_scanned;  // arcs those passes read (part of arcs_scanned)
   int rounds;
   int grs;
   int stranded;
@@ -173,11 +176,22 @@ __device__ __forceinline__ long long chk(const Bounds& b, long long i, long long
   return i;
 }
 
+// Undo log of a BCSR16 graph: every push records its arc, so the next fresh
+// solve restores only the arcs (and their twins) that changed instead of
+// rewriting all 2m residuals.  kLogSlots counters, one per 128-byte line,
+// picked by block, each owning `ulog_cap` entries; a slot that fills up sets
+// its overflow word and the next restore rewrites every arc.
+constexpr int kLogSlots = 32;
+constexpr int kLogStride = 32;  // ints between two slot counters: [0] count, [1] overflow
+
 struct TopoB {  // BCSR16: row[n+1], arc {dst, cf}, arx {rev, cap}
   const int* row;
   int2* arc;
   const int2* arx;
   Bounds bd;
+  int* ulog = nullptr;    // undo log (nullptr: not recorded)
+  int* ulog_n = nullptr;  // kLogSlots x kLogStride counter words
+  int ulog_cap = 0;       // entries per slot
   static constexpr int kSeg = 1;
   __device__ __forceinline__ void seg(int u, int, int& b, int& e) const {
     u = (int)chk(bd, u, bd.n);
@@ -204,6 +218,12 @@ struct TopoB {  // BCSR16: row[n+1], arc {dst, cf}, arx {rev, cap}
     int r = (int)chk(bd, __ldg(&arx[a].x), bd.na);
     int* tc = &arc[r].y;
     *tc = __ldcg(tc) + p;
+    if (ulog) {
+      int* c = ulog_n + (blockIdx.x & (kLogSlots - 1)) * kLogStride;
+      const int i = atomicAdd(c, 1);
+      if (i < ulog_cap) ulog[(long long)(blockIdx.x & (kLogSlots - 1)) * ulog_cap + i] = a;
+      else c[1] = 1;
+    }
   }
   __device__ __forceinline__ int twin_cf(int, int a) const {
     a = (int)chk(bd, a, bd.na);
@@ -306,6 +326,7 @@ struct Params {
   long long total_deg;
   unsigned long long gr_threshold;
   int gr_rounds;  // global relabel at the latest after this many rounds
+  int gr_stall;   // also after this many rounds in a row that moved no flow into t (0: off)
   long long max_rounds;
   unsigned long long budget_ns;
   unsigned long long bar_timeout_ns;
@@ -344,7 +365,8 @@ __device__ __forceinline__ bool bfs_skip(const Params<Topo>& p, int v) {
 
 // Optional event trace (written by global thread 0 only; count in Stats).
 enum TraceKind : int {
-  kTrLevel = 1, kTrRound = 2, kTrPassA = 3, kTrPassB = 4, kTrRelabel = 5, kTrGrEnd = 6, kTrSplit = 7
+  kTrLevel = 1, kTrRound = 2, kTrPassA = 3, kTrPassB = 4, kTrRelabel = 5, kTrGrEnd = 6, kTrSplit = 7,
+  kTrBuSplit = 8
 };
 
 // Per-block counters, flushed to Stats once per phase.
@@ -357,6 +379,7 @@ struct BlockAcc {
   unsigned long long bfs_vertices;
   long long fdeg;
   unsigned long long wmark;  // scanned + visits + relabels at the last work flush
+  unsigned long long deep;   // arcs scanned by the deep passes (also in `scanned`)
   int sink;
   int pad;
 };
@@ -386,25 +409,31 @@ __device__ __forceinline__ unsigned atom_add_release(unsigned* p, unsigned x) {
 // per barrier at 456 blocks, against 2.4 us with full fences around a
 // relaxed atomic.
 __device__ __forceinline__ bool grid_sync(Ctl* c, unsigned long long timeout_ns) {
+  // Thread 0 reads the error word once and the block takes its answer: a
+  // word another block may set at any moment (a timed-out wait) must not send
+  // the threads of one block different ways.
+  __shared__ int s_ok;
   __syncthreads();
-  if (gridDim.x == 1) return ldv(&c->err) == 0;  // a one-block grid: the block barrier is enough
   if (threadIdx.x == 0) {
-    const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
-    const unsigned old = atom_add_release(&c->bar, add);
-    if (((old + add) ^ old) & 0x80000000u) {
-      ld_acquire(&c->bar);  // last arrival
-    } else {
-      const unsigned long long t0 = gtime();
-      while (!((ld_acquire(&c->bar) ^ old) & 0x80000000u)) {
-        if (gtime() - t0 > timeout_ns) {
-          atomicCAS(&c->err, 0, (int)WBPR_ERR_TIMEOUT);
-          break;
+    if (gridDim.x > 1) {  // a one-block grid: the block barriers are enough
+      const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
+      const unsigned old = atom_add_release(&c->bar, add);
+      if (((old + add) ^ old) & 0x80000000u) {
+        ld_acquire(&c->bar);  // last arrival
+      } else {
+        const unsigned long long t0 = gtime();
+        while (!((ld_acquire(&c->bar) ^ old) & 0x80000000u)) {
+          if (gtime() - t0 > timeout_ns) {
+            atomicCAS(&c->err, 0, (int)WBPR_ERR_TIMEOUT);
+            break;
+          }
         }
       }
     }
+    s_ok = ldv(&c->err) == 0;
   }
   __syncthreads();
-  return ldv(&c->err) == 0;
+  return s_ok != 0;
 }
 
 // Warp-aggregated append of v to q[*cnt] (one atomic per converged group).
@@ -445,7 +474,8 @@ __device__ __forceinline__ void flush_acc(BlockAcc& a, Stats* st) {
     if (a.visits) atomicAdd(&st->vertex_visits, a.visits);
     if (a.bfs_arcs) atomicAdd(&st->bfs_arcs, a.bfs_arcs);
     if (a.bfs_vertices) atomicAdd(&st->bfs_vertices, a.bfs_vertices);
-    a.scanned = a.pushes = a.relabels = a.visits = a.bfs_arcs = a.bfs_vertices = a.wmark = 0;
+    if (a.deep) atomicAdd(&st->deep_scanned, a.deep);
+    a.scanned = a.pushes = a.relabels = a.visits = a.bfs_arcs = a.bfs_vertices = a.wmark = a.deep = 0;
   }
   __syncthreads();
 }
@@ -741,7 +771,10 @@ __device__ __forceinline__ unsigned ordered_push(const Params<Topo>& p, const VR
     }
   }
   if (npush) atomicAdd(&acc.pushes, (unsigned long long)npush);
-  if (threadIdx.x == 0) atomicAdd(&acc.scanned, scanned);
+  if (threadIdx.x == 0) {
+    atomicAdd(&acc.scanned, scanned);
+    atomicAdd(&acc.deep, scanned);
+  }
   *mn = mloc;
   return erem;
 }
@@ -836,6 +869,7 @@ __device__ void deep_pass_a(const Params<Topo>& p, int k, BlockAcc& acc) {
     p.hsum[k] = (int)(t > (unsigned long long)m.Er ? (unsigned long long)m.Er : t);
     p.hmin[k] = mm;
     atomicAdd(&acc.scanned, (unsigned long long)(hi - lo));
+    atomicAdd(&acc.deep, (unsigned long long)(hi - lo));
   }
   __syncthreads();
 }
@@ -1266,6 +1300,7 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
       }
     }
   }
+  if (p.trace && threadIdx.x == 0) p.bt2[blockIdx.x] = gtime();  // light rows done
   // medium rows: the warp checks a batch of rows' labels at once (32 rows, or
   // 8 when there are too few rows to give every warp several batches); 8-lane
   // tiles scan the open rows four at a time over their first kBuTile arcs
@@ -1363,6 +1398,10 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
         }
       }
     }
+  }
+  if (p.trace) {
+    __syncwarp();
+    if (threadIdx.x == 0) p.bt2[gridDim.x + blockIdx.x] = gtime();  // medium rows done (warp 0's view)
   }
   // long rows: blocks over static 2048-arc chunks; first chunk to hit wins
   __shared__ int s_item;
@@ -1534,6 +1573,7 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
     if (threadIdx.x == 0) acc.fdeg = 0;
     __syncthreads();
     const unsigned long long tb = gtime();
+    if (p.trace && threadIdx.x == 0) p.bt2[2 * gridDim.x + blockIdx.x] = tb;
     if (bu) bfs_bottom_up<Topo, DIR>(p, level, acc);
     else bfs_top_down<Topo, DIR>(p, level, nl, nlh, fc, fn, acc);
     TRACE_BLOCK(p, tb);
@@ -1541,6 +1581,17 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
     if (threadIdx.x == 0 && acc.fdeg)
       atomicAdd((unsigned long long*)&c->fdeg[fn], (unsigned long long)acc.fdeg);
     if (!grid_sync(c, p.bar_timeout_ns)) return false;
+    if (p.trace && bu && gt == 0) {
+      // longest light-row part and longest medium-row part of any block
+      unsigned long long ml = 0, mm = 0;
+      for (int b2 = 0; b2 < (int)gridDim.x; ++b2) {
+        const unsigned long long t1 = p.bt2[b2], t2 = p.bt2[gridDim.x + b2];
+        const unsigned long long t0b = p.bt2[2 * gridDim.x + b2];
+        ml = max(ml, t1 - t0b);
+        mm = max(mm, t2 - t1);
+      }
+      TRACE(p, kTrBuSplit, level, (long long)ml, (long long)mm);
+    }
     prev_bu = bu;
   }
   if (queues) {
@@ -1580,6 +1631,14 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
   return true;
 }
 
+__device__ __forceinline__ void clear_log(const TopoB& g, int gt) {
+  if (g.ulog && gt < kLogSlots) {
+    g.ulog_n[gt * kLogStride] = 0;
+    g.ulog_n[gt * kLogStride + 1] = 0;
+  }
+}
+__device__ __forceinline__ void clear_log(const TopoR&, int) {}
+
 // ---------------------------------------------------------------------------
 template <class Topo, int W>
 __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ Params<Topo> p) {
@@ -1587,6 +1646,7 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
   Ctl* c = p.ctl;
   if (threadIdx.x == 0) {
     acc.scanned = acc.pushes = acc.relabels = acc.visits = acc.bfs_arcs = acc.bfs_vertices = acc.wmark = 0;
+    acc.deep = 0;
     acc.fdeg = 0;
     acc.sink = 0;
   }
@@ -1610,6 +1670,8 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
       p.e[v] = 0;
       p.rl_min[v] = kNone;
     }
+    // the residuals were restored before this launch: the undo log starts empty
+    clear_log(p.g, gt);
     if (!grid_sync(c, p.bar_timeout_ns)) return;
     // preflow: saturate every residual arc out of s (reference preflow.cu:3-31,
     // with excess accumulated so parallel source arcs are kept)
@@ -1654,14 +1716,20 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
   // counter of the finished round (final at the barrier), so all agree
   unsigned long long work = 0;
   int since_gr = 0;
-  unsigned long long gr_ns = 0, round_ns = 0, push_ns = 0;
+  unsigned long long gr_ns = 0, round_ns = 0, push_ns = 0, deep_ns = 0;
   unsigned long long gr_end = 0, gr_last = 0;  // global thread 0 only
   bool marked = false;  // a global relabel has marked dead vertices (label n + 1)
+  // global thread 0: rounds in a row after which excess(t) had not changed
+  int stall = 0, et_prev = 0;
   for (;;) {
     if (need_gr) {
       const unsigned long long t0 = gtime();
       if (!bfs<Topo, 0>(p, p.term ? -1 : p.t, true, cur, acc, marked)) break;
       marked = true;
+      if (gt == 0) {
+        stall = 0;
+        if (p.t >= 0) et_prev = ldv(p.e + p.t);
+      }
       if (threadIdx.x == 0 && blockIdx.x == 0) {
         gr_end = gtime();
         gr_last = gr_end - t0;
@@ -1682,7 +1750,7 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
     }
     const unsigned long long t0 = gtime();
     if (gt == 0) TRACE(p, kTrRound, rounds, nL, nH);
-    unsigned long long tb = gtime();
+    unsigned long long tb = gtime(), tdeep = 0;
     if (p.trace && threadIdx.x == 0) p.bt2[gridDim.x + blockIdx.x] = tb;
     push_first<Topo, W>(p, cur, raw, acc);
     if (nH > 0) {
@@ -1708,6 +1776,7 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
         push_deep<Topo>(p, 0, nD, raw, acc);
         if (!grid_sync(c, p.bar_timeout_ns)) break;
         push_deep<Topo>(p, 1, nD, raw, acc);
+        tdeep = tb;
       }
     }
     TRACE_BLOCK(p, tb);
@@ -1715,7 +1784,9 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
     flush_work(acc, c, raw);
     if (!grid_sync(c, p.bar_timeout_ns)) break;
     if (gt == 0) {
-      push_ns += gtime() - t0;
+      const unsigned long long now = gtime();
+      push_ns += now - t0;
+      if (tdeep) deep_ns += now - tdeep;  // pass A start to the push phase's closing barrier
       TRACE(p, kTrPassB, rounds, 0, 0);
     }
     tb = gtime();
@@ -1727,9 +1798,17 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
       if ((p.max_rounds > 0 && rounds + 1 >= p.max_rounds) || gtime() - t_start > p.budget_ns)
         c->stop = 1;
       c->gr_ok = 2 * (gtime() - gr_end) >= gr_last;
+      // excess(t) is final once the push phase's barrier has passed: every
+      // block flushed its pushes into t before it
+      if (p.gr_stall > 0 && p.t >= 0) {
+        const int et = ldv(p.e + p.t);
+        stall = et == et_prev ? stall + 1 : 0;
+        et_prev = et;
+        c->stalled = stall >= p.gr_stall;
+      }
     }
     if (!grid_sync(c, p.bar_timeout_ns)) break;
-    if (gt == 0) TRACE(p, kTrRelabel, rounds, ldv(&c->qraw_count[raw]), 0);
+    if (gt == 0) TRACE(p, kTrRelabel, rounds, ldv(&c->qraw_count[raw]), p.t >= 0 ? ldv(p.e + p.t) : 0);
     work += work_total(c, raw);
     ++rounds;
     ++since_gr;
@@ -1743,7 +1822,12 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
     // most about two thirds of the time on graphs whose BFS is deep (512 x
     // 512 grids: 38 -> 27 ms; a 20,000-vertex path whose one unit of excess
     // walks 20,000 rounds: 60 s of relabels every 48 rounds without it).
-    if ((work > p.gr_threshold || since_gr >= p.gr_rounds) && ldv(&c->gr_ok)) need_gr = true;
+    // A run of rounds that moved no flow into t suggests the remaining
+    // excess is cut off from t; a global relabel then retires it at once
+    // instead of letting it climb towards n over many rounds.
+    // (published by global thread 0 before the barrier, read by all after it)
+    const bool stalled = ldv(&c->stalled) != 0;
+    if ((work > p.gr_threshold || since_gr >= p.gr_rounds || stalled) && ldv(&c->gr_ok)) need_gr = true;
   }
   // callers see label n for every vertex that cannot reach the sink (every
   // block has left the loop after the same barrier and reads no label now)
@@ -1756,6 +1840,7 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
     p.st->gr_ns = gr_ns;
     p.st->round_ns = round_ns;
     p.st->push_ns = push_ns;
+    p.st->deep_ns = deep_ns;
   }
 }
 

@@ -15,4 +15,25 @@ int occupancy_pr(const Params<TopoR>*, int tile, int threads);
 cudaError_t launch_stranded(const Params<TopoB>& p, int blocks, int threads, cudaStream_t st);
 cudaError_t launch_stranded(const Params<TopoR>& p, int blocks, int threads, cudaStream_t st);
 
+// Blocks of the persistent grid for a graph of `units` = n + residual arcs,
+// with `full` = SMs x resident blocks per SM.  Smaller graphs run on fewer
+// blocks: their rounds and BFS levels are latency-bound, and fewer blocks make
+// every phase's barrier and idle block cheaper.  Bands measured on GB300
+// (GENRMF, layered, grids, R-MAT); at most 16,384 units one block, whose
+// phases are then separated by block barriers only.
+constexpr long long kOneBlockUnits = 16384;
+inline int grid_blocks_for(long long units, int sms, int full) {
+  if (units <= kOneBlockUnits) return 1;
+  if (units <= (1LL << 21)) return full < sms / 2 ? full : (sms / 2 > 1 ? sms / 2 : 1);
+  if (units <= (1LL << 22)) return full < sms ? full : sms;
+  if (units <= (1LL << 24)) return full < 2 * sms ? full : 2 * sms;
+  return full;
+}
+
+// Default of the no-flow-into-t global-relabel trigger (rounds in a row, 0:
+// off).  On R-MAT scale 20/22 and the 2M x 2M bipartite graph it cut 5-18%
+// of the solve; on graphs of at most 2^22 units (GENRMF, layered networks,
+// 512 x 512 grids) it ran extra global relabels and cost 0-25%.
+inline int default_gr_stall(long long units) { return units > (1LL << 22) ? 2 : 0; }
+
 }  // namespace wbpr_dev
