@@ -753,7 +753,8 @@ __global__ void db_fill_twin(const int* off, const int* skey, const int* sval, c
 __device__ __forceinline__ int seg_len(const int* o, int u) { return o ? __ldg(o + u + 1) - __ldg(o + u) : 0; }
 
 // length classes (flags for three stable compactions) and the chunk counts
-// cnt: [0] rows > kTdHeavy [1] their top-down chunk items [2] push-phase chunk bound
+// cnt: [0] rows > kTdHeavy [1] their top-down chunk items [2] bound on the deep
+// parts of a push phase (every vertex is filed at most once a round)
 __global__ void db_classify(const int* o1, const int* o2, int n, int* f0, int* f1, int* f2,
                             unsigned long long* cnt) {
   unsigned long long a = 0, b = 0, c = 0;
@@ -762,7 +763,7 @@ __global__ void db_classify(const int* o1, const int* o2, int n, int* f0, int* f
     f0[u] = d > 0 && d <= kLightDeg;
     f1[u] = d > kLightDeg && d <= kHeavyDeg;
     f2[u] = d > kHeavyDeg;
-    c += (d + kChunk - 1) / kChunk;
+    if (d > kFirst) c += (d - kFirst + kPart - 1) / kPart;  // deep parts of the row
     if (d > kTdHeavy) {
       a += 1;
       b += (d + kTdChunk - 1) / kTdChunk;

@@ -41,8 +41,9 @@ constexpr long long kStatWords = align_ints((sizeof(Stats) + 3) / 4);
 constexpr long long kCountWords = 64;  // classification counters
 constexpr int kVertexArrays = 15;      // per-vertex int arrays, indexed as in wbpr_solve_bcsr_noalloc
 constexpr long long kTdItems = kNoAllocMaxArcs / kTdChunk + kNoAllocMaxVertices;
-// deep entries are rows longer than kFirst, each filed at most once a round
-constexpr long long kChunkItems = kNoAllocMaxArcs / kChunk + kNoAllocMaxArcs / (kFirst + 1) + 1;
+// deep parts: rows longer than kFirst, each filed at most once a round, cut
+// into kPart-arc parts beyond their first kFirst arcs
+constexpr long long kChunkItems = kNoAllocMaxArcs / kPart + kNoAllocMaxArcs / (kFirst + 1) + 1;
 constexpr long long kBchItems = kNoAllocMaxArcs / kChunk + kNoAllocMaxArcs / (kHeavyDeg + 1) + 1;
 constexpr long long kOffStat = kCtlWords;
 constexpr long long kOffCount = kOffStat + kStatWords;

@@ -46,6 +46,7 @@ constexpr int kBfsAlpha = 14;  // top-down -> bottom-up when frontier arcs * alp
 constexpr int kBfsBeta = 24;   // bottom-up -> top-down when frontier * beta < n
 constexpr int kLightDeg = 32;  // BFS: rows up to this length scanned by one thread
 constexpr int kHeavyDeg = 2048;  // BFS: rows longer than this scanned by a whole block
+constexpr int kChunk = 2048;     // BFS: heavy rows are cut into static chunks of this many arcs
 
 enum Mode : int {
   kModeFresh = 0,   // reset residuals, preflow, solve
@@ -66,14 +67,11 @@ struct Ctl {
   alignas(128) int qraw_count[2];
   alignas(128) int light_next;
   alignas(128) int heavy_next;
-  alignas(128) int deep_next_a;
-  int deep_next_b;
   alignas(128) int fcount[3];
   int fhcount[3];
   long long fdeg[3];
   alignas(128) unsigned long long dpack;  // deep list of the round: (entries << 32) | chunk items
-  alignas(128) int bfs_heavy_next[3];
-  int bu_found[3];  // vertices labelled by a bottom-up level, by level % 3
+  alignas(128) int bu_found[3];  // vertices labelled by a bottom-up level, by level % 3
   int mcount;       // materialised frontier: short rows
   int mhcount;      //   long-row chunk items
   alignas(128) int gr_ok;  // the rounds since the last global relabel took at least half as long as it
@@ -152,6 +150,9 @@ __device__ __forceinline__ void trace_rec(long long* tr, int cap, int* n, unsign
     }                                                                 \
   } while (0)
 __device__ __forceinline__ long long ldv64(const long long* p) { return *(const volatile long long*)p; }
+__device__ __forceinline__ unsigned long long ldv64u(const unsigned long long* p) {
+  return *(const volatile unsigned long long*)p;
+}
 
 // ---------------------------------------------------------------------------
 // Residual topologies.  load() returns (head, residual of u->head); push()
@@ -506,36 +507,32 @@ __device__ __forceinline__ void vidx(const VRow& r, int vi, int& k, int& a) {
   }
 }
 
-// Push phase for one vertex: a tile of W lanes (W = 1 is the thread-centric
-// form) with Q arcs per lane in flight walks the row in order from its start,
-// with early exit, over at most `limit` arcs.  A vertex whose row is longer
-// than `limit` and that keeps excess becomes a deep entry: its remaining
-// chunks are processed by whole blocks (deep passes A and B).
+// Long rows are walked by one warp over their first kFirst arcs; a vertex
+// that still has excess after them becomes a deep entry, and the rest of its
+// row is cut into kPart-arc parts that warps of the whole grid process in two
+// passes (deep passes A and B below).
+#ifndef WBPR_FIRST_ARCS
+#define WBPR_FIRST_ARCS 2048
+#endif
+constexpr int kFirst = WBPR_FIRST_ARCS;  // arcs of a long row walked by one warp before it goes deep
+constexpr int kPart = 256;               // arcs of a deep part: one warp, 8 arcs a lane in flight
+
 template <class Topo>
 __device__ __forceinline__ void make_deep(const Params<Topo>& p, int u, int E, int erem, int mn, int from, int hu,
-                                          const VRow& r);
+                                          const VRow& r, int lane, int nl);
 
+// The ordered walk of a tile of W lanes (W = 1: one thread) with Q arcs per
+// lane in flight over the virtual arcs [lo, hi) of row r: pushes at most erem
+// units along admissible arcs (label = th + 1 ... th = label(u) - 1) in arc
+// order, apportioned by a saturating prefix sum across the tile, with early
+// exit once erem is placed.  minh gets the minimum label over the arcs left
+// residual; npush and scanned count for the caller.
 template <class Topo, int W, int Q>
-__device__ __forceinline__ void tile_discharge(const Params<Topo>& p, int u, int limit, int* rawcnt,
-                                               BlockAcc& acc) {
-  const unsigned lw = threadIdx.x & 31u;
-  const int lane = (W == 1) ? 0 : (int)(lw & (W - 1));
-  const unsigned mask =
-      (W == 32) ? 0xffffffffu : (W == 1 ? (1u << lw) : (((1u << W) - 1u) << (lw & ~(unsigned)(W - 1))));
-  const int hu = __ldcg(p.lab + u);
-  int eu = 0;
-  if (lane == 0) eu = ldv(p.e + u);
-  if (W > 1) eu = __shfl_sync(mask, eu, 0, W);
-  if (eu <= 0 || hu >= p.n) return;
-  const VRow r = vrow(p.g, u);
-  const int hi = min(r.deg, limit);
-  unsigned erem = (unsigned)eu;
-  const int th = hu - 1;
-  int minh = kBig;
-  int npush = 0;
-  unsigned long long scanned = 0;
+__device__ __forceinline__ void tile_walk(const Params<Topo>& p, const VRow& r, int lo, int hi, int th, unsigned mask,
+                                          int lane, unsigned& erem, int& minh, int& npush,
+                                          unsigned long long& scanned, int* rawcnt, BlockAcc& acc) {
 #pragma unroll 1
-  for (int base = 0; base < hi; base += W * Q) {
+  for (int base = lo; base < hi; base += W * Q) {
     int dst[Q], cf[Q], hv[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -594,98 +591,77 @@ __device__ __forceinline__ void tile_discharge(const Params<Topo>& p, int u, int
     }
     if (erem == 0) break;
   }
+}
+
+// Push phase for one vertex: a tile walks its row from the start with early
+// exit, over at most `limit` arcs; a longer row that keeps excess becomes a
+// deep entry, anything else settles here.
+template <class Topo, int W, int Q>
+__device__ __forceinline__ void tile_discharge(const Params<Topo>& p, int u, int limit, int* rawcnt,
+                                               BlockAcc& acc) {
+  const unsigned lw = threadIdx.x & 31u;
+  const int lane = (W == 1) ? 0 : (int)(lw & (W - 1));
+  const unsigned mask =
+      (W == 32) ? 0xffffffffu : (W == 1 ? (1u << lw) : (((1u << W) - 1u) << (lw & ~(unsigned)(W - 1))));
+  const int hu = __ldcg(p.lab + u);
+  int eu = 0;
+  if (lane == 0) eu = ldv(p.e + u);
+  if (W > 1) eu = __shfl_sync(mask, eu, 0, W);
+  if (eu <= 0 || hu >= p.n) return;
+  const VRow r = vrow(p.g, u);
+  const int hi = min(r.deg, limit);
+  unsigned erem = (unsigned)eu;
+  int minh = kBig;
+  int npush = 0;
+  unsigned long long scanned = 0;
+  tile_walk<Topo, W, Q>(p, r, 0, hi, hu - 1, mask, lane, erem, minh, npush, scanned, rawcnt, acc);
   if (W > 1) minh = __reduce_min_sync(mask, minh);
   if (npush) atomicAdd(&acc.pushes, (unsigned long long)npush);
+  if (lane == 0) atomicAdd(&acc.scanned, scanned);
+  if (erem > 0 && r.deg > hi) {  // uniform over the tile
+    make_deep(p, u, eu, (int)erem, minh, hi, hu, r, lane, W);
+    return;
+  }
   if (lane == 0) {
-    atomicAdd(&acc.scanned, scanned);
-    if (erem > 0 && r.deg > hi) {
-      make_deep(p, u, eu, (int)erem, minh, hi, hu, r);
-    } else {
-      const int D = eu - (int)erem;
-      bool self = true;
-      if (D > 0) self = (atomicSub(p.e + u, D) - D) > 0;
-      if (erem > 0) {
-        // Pushes into u during this phase open arcs u->w with label(w) =
-        // label(u) + 1 that the scan may not have seen; the relabel phase
-        // detects them by comparing excess with (filing snapshot - pushed).
-        p.rl_min[u] = minh;
-        p.rl_left[u] = __ldcg(p.esnap + u) - D;
-      }
-      if (self) append(p.qraw, rawcnt, u);
-      atomicAdd(&acc.visits, 1ull);
+    const int D = eu - (int)erem;
+    bool self = true;
+    if (D > 0) self = (atomicSub(p.e + u, D) - D) > 0;
+    if (erem > 0) {
+      // Pushes into u during this phase open arcs u->w with label(w) =
+      // label(u) + 1 that the scan may not have seen; the relabel phase
+      // detects them by comparing excess with (filing snapshot - pushed).
+      p.rl_min[u] = minh;
+      p.rl_left[u] = __ldcg(p.esnap + u) - D;
     }
+    if (self) append(p.qraw, rawcnt, u);
+    atomicAdd(&acc.visits, 1ull);
   }
 }
 
 // ---------------------------------------------------------------------------
-// Heavy rows (longer than heavy_deg) are cut into chunks of kChunk arcs that
-// different blocks process in two passes of the push phase:
-//   pass A  every chunk sums the residual capacity of its admissible arcs
-//           (saturated at the vertex's excess) and takes the min label over
-//           its other residual arcs;
+// Deep entries: the part of a long row beyond its first kFirst arcs, cut into
+// kPart-arc parts, each processed by one warp in two passes of the push phase:
+//   pass A  every part sums the residual capacity of its admissible arcs
+//           (saturated at the vertex's excess left) and takes the minimum
+//           label over its other residual arcs;
 //   -- grid barrier --
-//   pass B  chunk c of u receives allot = min(sum_c, E - sum of earlier
-//           chunks) and pushes it along its admissible arcs in arc order;
-//           the last chunk settles excess(u) and the relabel record.
-// Total pushed = min(E, sum of all chunks), in arc order: the same pushes a
-// single thread walking the row would make.  Labels are frozen across both
-// passes, and admissible residuals of u change only by u's own pushes, so the
-// two passes see the same admissible set.
-constexpr int kItems = 8;
-constexpr int kChunk = 2048;
-constexpr int kFirst = 2048;  // arcs of a long row walked by one warp before it goes deep
+//   pass B  part j of u receives allot = min(sum_j, E left - sum of earlier
+//           parts) and pushes it along its admissible arcs in arc order; the
+//           last part settles excess(u) and the relabel record.
+// Total pushed = min(E left, sum of all parts), in arc order: the same pushes
+// a single tile walking the whole row would make.  Labels are frozen across
+// both passes, and admissible residuals of u change only by u's own pushes,
+// so the two passes see the same admissible set.  Warps need no block
+// barrier, and every part is the same size, so parts are dealt to warps
+// statically (part k to warp k mod warps) without a claim counter.
+//
+// Part record (3 x int4, 48 bytes: all a warp needs, in one load):
+//   {u, first part of the entry, E (excess at filing), E left after the first
+//    kFirst arcs}, {label, parts, entry, first arc of part 0}, the row
+//   {b0, d0, b1, deg}.
 
-// Block-wide inclusive scan of x (saturated at cap); returns the inclusive
-// value of this thread and writes the exclusive one to *excl, the total to
-// *total.  All threads of the block must call it.
-__device__ __forceinline__ unsigned block_scan_sat(unsigned x, unsigned cap, unsigned* excl,
-                                                   unsigned* total) {
-  __shared__ unsigned s_w[32];
-  __shared__ unsigned s_t;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  unsigned incl = x > cap ? cap : x;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    unsigned y = __shfl_up_sync(0xffffffffu, incl, d);
-    if (lane >= d) {
-      incl += y;
-      if (incl > cap) incl = cap;
-    }
-  }
-  unsigned prevw = __shfl_up_sync(0xffffffffu, incl, 1);
-  if (lane == 0) prevw = 0;
-  if (lane == 31) s_w[wid] = incl;
-  __syncthreads();
-  if (wid == 0) {
-    unsigned v = lane < nw ? s_w[lane] : 0u;
-    unsigned inc2 = v;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      unsigned y = __shfl_up_sync(0xffffffffu, inc2, d);
-      if (lane >= d) {
-        inc2 += y;
-        if (inc2 > cap) inc2 = cap;
-      }
-    }
-    unsigned exc2 = __shfl_up_sync(0xffffffffu, inc2, 1);
-    if (lane == 0) exc2 = 0;
-    if (lane < nw) s_w[lane] = exc2;
-    if (lane == nw - 1) s_t = inc2;
-  }
-  __syncthreads();
-  const unsigned wpre = s_w[wid];
-  unsigned ib = wpre + incl, pb = wpre + prevw;
-  if (ib > cap) ib = cap;
-  if (pb > cap) pb = cap;
-  *excl = pb;
-  *total = s_t;
-  __syncthreads();
-  return ib;
-}
-
-// Settle a heavy vertex: subtract what it pushed, re-file it when it still
-// has excess, record the relabel candidate when some of its own excess was
-// left over.
+// Settle a vertex: subtract what it pushed, re-file it when it still has
+// excess, record the relabel candidate when some of its own excess was left.
 template <class Topo>
 __device__ __forceinline__ void settle(const Params<Topo>& p, int u, int E, int erem, int mn, int* rawcnt,
                                        BlockAcc& acc) {
@@ -701,96 +677,23 @@ __device__ __forceinline__ void settle(const Params<Topo>& p, int u, int E, int 
   atomicAdd(&p.st->heavy_visits, 1ull);
 }
 
-__device__ __forceinline__ int block_min(int v) {
-  __shared__ int s_mn[32];
-  v = __reduce_min_sync(0xffffffffu, v);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) s_mn[wid] = v;
-  __syncthreads();
-  int m = kBig;
-  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = min(m, s_mn[w]);
-  __syncthreads();
-  return m;
-}
-
-// Ordered discharge of the arcs [lo, hi) of the virtual row r by the whole
-// block: pushes at most erem units along admissible arcs in arc order.
-// Returns the units left; *mn gets this thread's min label over arcs still
-// residual after the pushes.
-template <class Topo>
-__device__ __forceinline__ unsigned ordered_push(const Params<Topo>& p, const VRow& r, int lo, int hi, int hu,
-                                                 unsigned erem, int* mn, int* rawcnt, BlockAcc& acc) {
-  const int th = hu - 1;
-  int npush = 0, mloc = kBig;
-  unsigned long long scanned = 0;
-  // slabs of blockDim x ni arcs with ni = 1, 2, 4, 8, 8, ...: a vertex that
-  // places its excess early reads only the first few hundred arcs
-  int ni = 1;
-  for (int vb = lo; vb < hi && erem > 0; vb += blockDim.x * ni, ni = ni < kItems ? 2 * ni : kItems) {
-    int dst[kItems], cf[kItems], hv[kItems];
-#pragma unroll
-    for (int it = 0; it < kItems; ++it) {
-      const int vi = vb + it * blockDim.x + threadIdx.x;
-      dst[it] = 0;
-      cf[it] = 0;
-      if (it < ni && vi < hi) {
-        int kk, aa;
-        vidx(r, vi, kk, aa);
-        p.g.load(kk, aa, dst[it], cf[it]);
-      }
-    }
-#pragma unroll
-    for (int it = 0; it < kItems; ++it) hv[it] = cf[it] > 0 ? __ldcg(p.lab + dst[it]) : kBig;
-    scanned += (unsigned long long)min((int)blockDim.x * ni, hi - vb);
-#pragma unroll
-    for (int it = 0; it < kItems; ++it) {
-      if (it >= ni) break;  // uniform: ni is the same in every thread
-      const bool adm = cf[it] > 0 && hv[it] == th;
-      int pushed = 0;
-      if (erem > 0 && __syncthreads_or(adm)) {
-        unsigned ex, total;
-        const unsigned inc = block_scan_sat(adm ? (unsigned)cf[it] : 0u, erem, &ex, &total);
-        pushed = (int)(inc - ex);
-        erem -= total;
-        if (pushed > 0) {
-          int kk, aa;
-          vidx(r, vb + it * blockDim.x + threadIdx.x, kk, aa);
-          p.g.push(kk, aa, cf[it], pushed);
-          ++npush;
-          if (dst[it] == p.t) {
-            atomicAdd(&acc.sink, pushed);
-          } else if (p.term && p.term[dst[it]] == 2) {
-            atomicAdd(p.e + dst[it], pushed);
-          } else {
-            int old = atomicAdd(p.e + dst[it], pushed);
-            if (old == 0) append(p.qraw, rawcnt, dst[it]);
-          }
-        }
-      }
-      if (cf[it] - pushed > 0 && hv[it] < mloc) mloc = hv[it];
-    }
-  }
-  if (npush) atomicAdd(&acc.pushes, (unsigned long long)npush);
-  if (threadIdx.x == 0) {
-    atomicAdd(&acc.scanned, scanned);
-    atomicAdd(&acc.deep, scanned);
-  }
-  *mn = mloc;
-  return erem;
-}
-
-// A vertex that kept excess after the first `from` arcs of its row: its
-// remaining arcs are cut into kChunk chunks for the deep passes.
+// File the deep entry of u: the nl lanes of the tile that walked its first
+// `from` arcs write the part records together.
 template <class Topo>
 __device__ __forceinline__ void make_deep(const Params<Topo>& p, int u, int E, int erem, int mn, int from, int hu,
-                                          const VRow& r) {
-  Ctl* c = p.ctl;
-  const int nch = (r.deg - from + kChunk - 1) / kChunk;
-  const unsigned long long old = atomicAdd(&c->dpack, (1ull << 32) | (unsigned long long)nch);
+                                          const VRow& r, int lane, int nl) {
+  const int np = (r.deg - from + kPart - 1) / kPart;
+  unsigned long long old = 0;
+  if (lane == 0) old = atomicAdd(&p.ctl->dpack, (1ull << 32) | (unsigned long long)np);
+  if (nl > 1) {
+    const unsigned mask = nl == 32 ? 0xffffffffu : (((1u << nl) - 1u) << ((threadIdx.x & 31u) & ~(unsigned)(nl - 1)));
+    old = __shfl_sync(mask, old, 0, nl);
+  }
   const int di = (int)(old >> 32), base = (int)(old & 0xffffffffu);
-  p.dmin0[di] = mn;
-  const int4 a = make_int4(u, base, E, erem), b = make_int4(hu, nch, di, 0), rr = make_int4(r.b0, r.d0, r.b1, r.deg);
-  for (int j = 0; j < nch; ++j) {
+  if (lane == 0) p.dmin0[di] = mn;
+  const int4 a = make_int4(u, base, E, erem), b = make_int4(hu, np, di, from),
+             rr = make_int4(r.b0, r.d0, r.b1, r.deg);
+  for (int j = lane; j < np; j += nl) {
     int4* q = p.hrec + 3LL * (base + j);
     q[0] = a;
     q[1] = b;
@@ -798,116 +701,106 @@ __device__ __forceinline__ void make_deep(const Params<Topo>& p, int u, int E, i
   }
 }
 
-struct DeepMeta {
-  int u, di, base, E, Er, hu, j, nch;
+struct DeepPart {
+  int u, first, E, Er, hu, np, di, lo, hi, j;
   VRow r;
 };
 
-template <class Topo>
-__device__ __forceinline__ void deep_meta(const Params<Topo>& p, int k, DeepMeta* m) {
-  __shared__ DeepMeta s_m;
-  if (threadIdx.x == 0) {
-    const int4* q = p.hrec + 3LL * k;
-    const int4 a = __ldcg(q), b = __ldcg(q + 1), rr = __ldcg(q + 2);
-    s_m.u = a.x;
-    s_m.base = a.y;
-    s_m.E = a.z;
-    s_m.Er = a.w;
-    s_m.hu = b.x;
-    s_m.nch = b.y;
-    s_m.di = b.z;
-    s_m.j = k - s_m.base;
-    s_m.r.b0 = rr.x;
-    s_m.r.d0 = rr.y;
-    s_m.r.b1 = rr.z;
-    s_m.r.deg = rr.w;
-  }
-  __syncthreads();
-  *m = s_m;
-  __syncthreads();
+__device__ __forceinline__ DeepPart deep_part(const int4* hrec, int k) {
+  const int4* q = hrec + 3LL * k;
+  const int4 a = __ldcg(q), b = __ldcg(q + 1), rr = __ldcg(q + 2);
+  DeepPart d;
+  d.u = a.x;
+  d.first = a.y;
+  d.E = a.z;
+  d.Er = a.w;
+  d.hu = b.x;
+  d.np = b.y;
+  d.di = b.z;
+  d.j = k - a.y;
+  d.r.b0 = rr.x;
+  d.r.d0 = rr.y;
+  d.r.b1 = rr.z;
+  d.r.deg = rr.w;
+  d.lo = b.w + d.j * kPart;
+  d.hi = min(d.r.deg, d.lo + kPart);
+  return d;
 }
 
-// Deep entry, pass A: admissible capacity (saturated at the excess left) and
-// min label over the other residual arcs of chunk j + 1.
+// Pass A of part k (all 32 lanes of a warp).
 template <class Topo>
-__device__ void deep_pass_a(const Params<Topo>& p, int k, BlockAcc& acc) {
-  DeepMeta m;
-  deep_meta(p, k, &m);
-  const int lo = kFirst + m.j * kChunk, hi = min(m.r.deg, lo + kChunk);
-  const int th = m.hu - 1;
+__device__ void deep_part_a(const Params<Topo>& p, int k, BlockAcc& acc) {
+  const int lane = threadIdx.x & 31;
+  const DeepPart d = deep_part(p.hrec, k);
+  const int th = d.hu - 1;
+  constexpr int kIt = kPart / 32;
+  int dst[kIt], cf[kIt];
+#pragma unroll
+  for (int it = 0; it < kIt; ++it) {
+    const int vi = d.lo + it * 32 + lane;
+    dst[it] = 0;
+    cf[it] = 0;
+    if (vi < d.hi) {
+      int kk, a;
+      vidx(d.r, vi, kk, a);
+      p.g.load(kk, a, dst[it], cf[it]);
+    }
+  }
   unsigned long long sum = 0;
   int mn = kBig;
-  for (int vb = lo; vb < hi; vb += blockDim.x * kItems) {
-    int dst[kItems], cf[kItems];
 #pragma unroll
-    for (int it = 0; it < kItems; ++it) {
-      const int vi = vb + it * blockDim.x + threadIdx.x;
-      dst[it] = 0;
-      cf[it] = 0;
-      if (vi < hi) {
-        int kk, a;
-        vidx(m.r, vi, kk, a);
-        p.g.load(kk, a, dst[it], cf[it]);
-      }
-    }
-#pragma unroll
-    for (int it = 0; it < kItems; ++it) {
-      if (cf[it] > 0) {
-        const int hv = __ldcg(p.lab + dst[it]);
-        if (hv == th) sum += (unsigned)cf[it];
-        else if (hv < mn) mn = hv;
-      }
+  for (int it = 0; it < kIt; ++it) {
+    if (cf[it] > 0) {
+      const int hv = __ldcg(p.lab + dst[it]);
+      if (hv == th) sum += (unsigned)cf[it];
+      else if (hv < mn) mn = hv;
     }
   }
-  __shared__ unsigned long long s_sum[32];
-  for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-  if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = sum;
-  const int mm = block_min(mn);
-  if (threadIdx.x == 0) {
-    unsigned long long t = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_sum[w];
-    p.hsum[k] = (int)(t > (unsigned long long)m.Er ? (unsigned long long)m.Er : t);
-    p.hmin[k] = mm;
-    atomicAdd(&acc.scanned, (unsigned long long)(hi - lo));
-    atomicAdd(&acc.deep, (unsigned long long)(hi - lo));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  mn = __reduce_min_sync(0xffffffffu, mn);
+  if (lane == 0) {
+    p.hsum[k] = (int)(sum > (unsigned long long)d.Er ? (unsigned long long)d.Er : sum);
+    p.hmin[k] = mn;
+    atomicAdd(&acc.scanned, (unsigned long long)(d.hi - d.lo));
+    atomicAdd(&acc.deep, (unsigned long long)(d.hi - d.lo));
   }
-  __syncthreads();
 }
 
-// Deep entry, pass B: chunk takes min(sum, Er - earlier chunks) and pushes it
-// in order; the last chunk settles the vertex.
+// Pass B of part k (all 32 lanes of a warp): the sums of the earlier parts
+// and, for the last part, the minima of all parts are read by the lanes in
+// parallel.
 template <class Topo>
-__device__ void deep_pass_b(const Params<Topo>& p, int k, int* rawcnt, BlockAcc& acc) {
-  DeepMeta m;
-  deep_meta(p, k, &m);
-  __shared__ int s_allot;
-  __shared__ long long s_prev;
-  if (threadIdx.x == 0) {
-    long long prev = 0;
-    for (int i = m.base; i < k && prev < m.Er; ++i) prev += __ldcg(p.hsum + i);
-    const int S = __ldcg(p.hsum + k);
-    s_prev = prev;
-    s_allot = prev >= m.Er ? 0 : (int)min((long long)S, (long long)m.Er - prev);
-  }
-  __syncthreads();
-  const unsigned allot = (unsigned)s_allot;
-  const long long prev = s_prev;
-  __syncthreads();
+__device__ void deep_part_b(const Params<Topo>& p, int k, int* rawcnt, BlockAcc& acc) {
+  const int lane = threadIdx.x & 31;
+  const DeepPart d = deep_part(p.hrec, k);
+  long long prev = 0;
+  for (int i = d.first + lane; i < k; i += 32) prev += __ldcg(p.hsum + i);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) prev += __shfl_xor_sync(0xffffffffu, prev, o);
+  const int S = __ldcg(p.hsum + k);
+  unsigned allot = prev >= d.Er ? 0u : (unsigned)min((long long)S, (long long)d.Er - prev);
   if (allot > 0) {
-    const int lo = kFirst + m.j * kChunk, hi = min(m.r.deg, lo + kChunk);
-    int unused;
-    ordered_push(p, m.r, lo, hi, m.hu, allot, &unused, rawcnt, acc);
+    int minh = kBig, npush = 0;
+    unsigned long long scanned = 0;
+    tile_walk<Topo, 32, 4>(p, d.r, d.lo, d.hi, d.hu - 1, 0xffffffffu, lane, allot, minh, npush, scanned, rawcnt,
+                           acc);
+    if (npush) atomicAdd(&acc.pushes, (unsigned long long)npush);
+    if (lane == 0) {
+      atomicAdd(&acc.scanned, scanned);
+      atomicAdd(&acc.deep, scanned);
+    }
   }
-  if (threadIdx.x == 0 && m.j == m.nch - 1) {
-    const long long all = prev + __ldcg(p.hsum + k);
-    const int Dd = (int)min((long long)m.Er, all);
-    const int erest = m.Er - Dd;
-    int mn = __ldcg(p.dmin0 + m.di);
-    if (erest > 0)
-      for (int i = m.base; i < m.base + m.nch; ++i) mn = min(mn, __ldcg(p.hmin + i));
-    settle(p, m.u, m.E, erest, mn, rawcnt, acc);
+  if (d.j == d.np - 1) {
+    int mn = kBig;
+    for (int i = d.first + lane; i < d.first + d.np; i += 32) mn = min(mn, __ldcg(p.hmin + i));
+    mn = __reduce_min_sync(0xffffffffu, mn);
+    if (lane == 0) {
+      const long long all = prev + S;
+      const int erest = d.Er - (int)min((long long)d.Er, all);
+      settle(p, d.u, d.E, erest, min(mn, __ldcg(p.dmin0 + d.di)), rawcnt, acc);
+    }
   }
-  __syncthreads();
 }
 
 // Push phase, stage 1: rows longer than heavy_deg by a warp each (128 arcs in
@@ -945,22 +838,15 @@ __device__ void push_first(const Params<Topo>& p, int cur, int raw, BlockAcc& ac
   }
 }
 
+// Deep pass A or B over the round's nD parts: part k to warp k mod warps.
 template <class Topo>
 __device__ void push_deep(const Params<Topo>& p, int pass, int nD, int raw, BlockAcc& acc) {
-  Ctl* c = p.ctl;
-  int* rawcnt = &c->qraw_count[raw];
-  int* ctr = pass == 0 ? &c->deep_next_a : &c->deep_next_b;
-  __shared__ int s_item;
-  for (int it = blockIdx.x; it < nD;) {
-    // claim the next item now, so the atomic's latency hides behind this one
-    int nx = 0;
-    if (threadIdx.x == 0) nx = (int)gridDim.x + atomicAdd(ctr, 1);
-    if (pass == 0) deep_pass_a<Topo>(p, it, acc);
-    else deep_pass_b<Topo>(p, it, rawcnt, acc);
-    if (threadIdx.x == 0) s_item = nx;
-    __syncthreads();
-    it = s_item;
-    __syncthreads();
+  int* rawcnt = &p.ctl->qraw_count[raw];
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int k = gw; k < nD; k += nwarps) {
+    if (pass == 0) deep_part_a<Topo>(p, k, acc);
+    else deep_part_b<Topo>(p, k, rawcnt, acc);
   }
 }
 
@@ -1040,8 +926,6 @@ __device__ void relabel_phase(const Params<Topo>& p, int cur, int nxt, int raw, 
     c->qraw_count[raw ^ 1] = 0;
     c->light_next = 0;
     c->heavy_next = 0;
-    c->deep_next_a = 0;
-    c->deep_next_b = 0;
   }
   if (blockIdx.x == 0 && threadIdx.x < kWorkSlots) c->work[raw ^ 1][threadIdx.x * 16] = 0;
 }
@@ -1404,40 +1288,49 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
     if (threadIdx.x == 0) p.bt2[gridDim.x + blockIdx.x] = gtime();  // medium rows done (warp 0's view)
   }
   // long rows: blocks over static 2048-arc chunks; first chunk to hit wins
-  __shared__ int s_item;
-  __shared__ int s_skip;
-  const int cur3 = level % 3;
   unsigned long long ha = 0;
-  for (int it = blockIdx.x; it < p.n_bch;) {
-    const int4 ch = __ldg(p.bch + it);  // {vertex, segment, begin, end}
-    if (threadIdx.x == 0) {
-      s_skip = (bfs_skip(p, ch.x) || __ldcg(p.lab + ch.x) != p.n);
-      s_item = (int)gridDim.x + atomicAdd(&c->bfs_heavy_next[cur3], 1);
+  // chunk k of the list goes to block k % blocks; warp 0 checks 32 of the
+  // block's chunks at once (their vertex still unlabelled), one block
+  // barrier per 32 chunks, and only those chunks are scanned
+  __shared__ unsigned s_live;
+  for (int k0 = 0; (long long)blockIdx.x + (long long)k0 * gridDim.x < p.n_bch; k0 += 32) {
+    if (threadIdx.x < 32) {
+      const long long it = blockIdx.x + (long long)(k0 + (int)threadIdx.x) * gridDim.x;
+      bool live = false;
+      if (it < p.n_bch) {
+        const int v = __ldg(&p.bch[it].x);
+        live = !bfs_skip(p, v) && __ldcg(p.lab + v) == p.n;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, live);
+      if (threadIdx.x == 0) s_live = m;
     }
     __syncthreads();
-    const bool skip = s_skip;
-    it = s_item;
+    unsigned live = s_live;
     __syncthreads();
-    if (skip) continue;
-    bool hit = false;
-    for (int base = ch.z; base < ch.w; base += blockDim.x * 4) {
-      bool h = false;
+    while (live) {
+      const int j = __ffs(live) - 1;
+      live &= live - 1;
+      const int4 ch = __ldg(p.bch + blockIdx.x + (long long)(k0 + j) * gridDim.x);  // {vertex, segment, begin, end}
+      bool hit = false;
+      for (int base = ch.z; base < ch.w; base += blockDim.x * 4) {
+        bool h = false;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int a = base + q * blockDim.x + threadIdx.x;
-        if (a < ch.w) {
-          ++ha;
-          h |= bu_arc<Topo, DIR>(p, ch.y, a, level);
+        for (int q = 0; q < 4; ++q) {
+          const int a = base + q * blockDim.x + threadIdx.x;
+          if (a < ch.w) {
+            ++ha;
+            h |= bu_arc<Topo, DIR>(p, ch.y, a, level);
+          }
+        }
+        if (__syncthreads_or(h)) {
+          hit = true;
+          break;
         }
       }
-      if (__syncthreads_or(h)) {
-        hit = true;
-        break;
+      if (hit && threadIdx.x == 0 && atomicCAS(p.lab + ch.x, p.n, level + 1) == p.n) {
+        ++found;
+        fdeg += (unsigned long long)p.g.deg(ch.x);
       }
-    }
-    if (hit && threadIdx.x == 0 && atomicCAS(p.lab + ch.x, p.n, level + 1) == p.n) {
-      ++found;
-      fdeg += (unsigned long long)p.g.deg(ch.x);
     }
   }
   arcs += ha;
@@ -1505,15 +1398,12 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
     c->fdeg[1] = c->fdeg[2] = 0;
     c->bu_found[0] = c->bu_found[1] = c->bu_found[2] = 0;
     c->mcount = c->mhcount = 0;
-    c->bfs_heavy_next[0] = c->bfs_heavy_next[1] = c->bfs_heavy_next[2] = 0;
     if (queues) {
       c->lcount[cur] = 0;
       c->hcount[cur] = 0;
       c->dpack = 0;
       c->light_next = 0;
       c->heavy_next = 0;
-      c->deep_next_a = 0;
-      c->deep_next_b = 0;
     }
   }
   if (!grid_sync(c, p.bar_timeout_ns)) return false;
@@ -1563,7 +1453,6 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
       c->fcount[fr] = 0;
       c->fhcount[fr] = 0;
       c->fdeg[fr] = 0;
-      c->bfs_heavy_next[fn] = 0;
       c->bu_found[fn] = 0;
       if (!mat) c->mcount = c->mhcount = 0;
       atomicAdd(&p.st->bfs_levels, 1);
@@ -1585,10 +1474,10 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
       // longest light-row part and longest medium-row part of any block
       unsigned long long ml = 0, mm = 0;
       for (int b2 = 0; b2 < (int)gridDim.x; ++b2) {
-        const unsigned long long t1 = p.bt2[b2], t2 = p.bt2[gridDim.x + b2];
-        const unsigned long long t0b = p.bt2[2 * gridDim.x + b2];
-        ml = max(ml, t1 - t0b);
-        mm = max(mm, t2 - t1);
+        const unsigned long long t1 = ldv64u(p.bt2 + b2), t2 = ldv64u(p.bt2 + gridDim.x + b2);
+        const unsigned long long t0b = ldv64u(p.bt2 + 2 * gridDim.x + b2);
+        ml = max(ml, t1 > t0b ? t1 - t0b : 0ull);
+        mm = max(mm, t2 > t1 ? t2 - t1 : 0ull);
       }
       TRACE(p, kTrBuSplit, level, (long long)ml, (long long)mm);
     }
@@ -1640,8 +1529,14 @@ __device__ __forceinline__ void clear_log(const TopoB& g, int gt) {
 __device__ __forceinline__ void clear_log(const TopoR&, int) {}
 
 // ---------------------------------------------------------------------------
+// Resident blocks per SM the register allocation is sized for (80 registers
+// a thread at 3 blocks of 256 threads).
+#ifndef WBPR_PR_MIN_BLOCKS
+#define WBPR_PR_MIN_BLOCKS 3
+#endif
+
 template <class Topo, int W>
-__global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ Params<Topo> p) {
+__global__ void __launch_bounds__(256, WBPR_PR_MIN_BLOCKS) pr_persistent(const __grid_constant__ Params<Topo> p) {
   __shared__ BlockAcc acc;
   Ctl* c = p.ctl;
   if (threadIdx.x == 0) {
@@ -1763,7 +1658,7 @@ __global__ void __launch_bounds__(256, 3) pr_persistent(const __grid_constant__ 
         if (p.trace) {  // longest heavy part and longest light part of any block
           unsigned long long mh = 0, ml = 0;
           for (int b = 0; b < (int)gridDim.x; ++b) {
-            const unsigned long long t0b = p.bt2[gridDim.x + b], th = p.bt2[b];
+            const unsigned long long t0b = ldv64u(p.bt2 + gridDim.x + b), th = ldv64u(p.bt2 + b);
             const unsigned long long tot = p.bt[b];
             mh = max(mh, th - t0b);
             ml = max(ml, tot > th - t0b ? tot - (th - t0b) : 0ull);
