@@ -156,6 +156,7 @@ def build_ref_cuda(force: bool = False) -> str | None:
 
 
 def build_all(force: bool = False) -> None:
+    stage_reference()  # keeps the staged copy current for machines without the tree
     build_oracle(force)
     build_ref(force)
 

@@ -1265,6 +1265,7 @@ struct RunCfg {
   unsigned long long gr_threshold;
   int gr_rounds;
   int gr_stall;
+  int greedy;
   long long max_rounds;
   unsigned long long budget_ns;
   unsigned long long bar_timeout_ns;
@@ -1291,6 +1292,7 @@ wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch
   p.gr_threshold = rc.gr_threshold;
   p.gr_rounds = rc.gr_rounds;
   p.gr_stall = rc.gr_stall;
+  p.greedy = rc.greedy;
   if (rc.bar_timeout_ns) p.bar_timeout_ns = rc.bar_timeout_ns;
   p.max_rounds = rc.max_rounds;
   p.budget_ns = rc.budget_ns;
@@ -1388,7 +1390,9 @@ wbpr_status make_cfg(wbpr_graph* g, int s, int t, wbpr_algo algo, const wbpr_tun
   const double alpha = tu->gr_alpha > 0 ? tu->gr_alpha : 0.75;
   rc->gr_threshold = (unsigned long long)(alpha * ((double)g->n + (double)g->total_deg)) + 1;
   rc->gr_rounds = tu->gr_rounds > 0 ? tu->gr_rounds : 48;
-  if (tu->gr_stall < -1 || tu->barrier_timeout_ns < 0) return WBPR_ERR_INVALID_ARG;
+  if (tu->gr_stall < -1 || tu->barrier_timeout_ns < 0 || tu->greedy < -1 || tu->greedy > 0)
+    return WBPR_ERR_INVALID_ARG;
+  rc->greedy = tu->greedy == 0 ? 1 : 0;
   rc->gr_stall = tu->gr_stall == 0 ? default_gr_stall((long long)g->n + g->total_deg)
                                    : (tu->gr_stall < 0 ? 0 : tu->gr_stall);
   rc->bar_timeout_ns = tu->barrier_timeout_ns > 0 ? (unsigned long long)tu->barrier_timeout_ns : kBarrierTimeoutNs;

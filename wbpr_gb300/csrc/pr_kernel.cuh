@@ -42,8 +42,14 @@ namespace cg = cooperative_groups;
 
 constexpr int kNone = -1;
 constexpr int kBig = 0x7fffffff;
-constexpr int kBfsAlpha = 14;  // top-down -> bottom-up when frontier arcs * alpha > unvisited arcs
-constexpr int kBfsBeta = 24;   // bottom-up -> top-down when frontier * beta < n
+#ifndef WBPR_BFS_ALPHA
+#define WBPR_BFS_ALPHA 14
+#endif
+#ifndef WBPR_BFS_BETA
+#define WBPR_BFS_BETA 24
+#endif
+constexpr int kBfsAlpha = WBPR_BFS_ALPHA;  // top-down -> bottom-up when frontier arcs * alpha > unvisited arcs
+constexpr int kBfsBeta = WBPR_BFS_BETA;    // bottom-up -> top-down when frontier * beta < n
 constexpr int kLightDeg = 32;  // BFS: rows up to this length scanned by one thread
 constexpr int kHeavyDeg = 2048;  // BFS: rows longer than this scanned by a whole block
 constexpr int kChunk = 2048;     // BFS: heavy rows are cut into static chunks of this many arcs
@@ -73,6 +79,7 @@ struct Ctl {
   alignas(128) unsigned long long dpack;  // deep list of the round: (entries << 32) | chunk items
   alignas(128) int bu_found[3];  // vertices labelled by a bottom-up level, by level % 3
   int mcount;       // materialised frontier: short rows
+  int glong;        // greedy routing: walkers left for the warp stage
   int mhcount;      //   long-row chunk items
   alignas(128) int gr_ok;  // the rounds since the last global relabel took at least half as long as it
   int stalled;             // excess(t) has not changed for gr_stall rounds
@@ -219,12 +226,15 @@ struct TopoB {  // BCSR16: row[n+1], arc {dst, cf}, arx {rev, cap}
     int r = (int)chk(bd, __ldg(&arx[a].x), bd.na);
     int* tc = &arc[r].y;
     *tc = __ldcg(tc) + p;
-    if (ulog) {
-      int* c = ulog_n + (blockIdx.x & (kLogSlots - 1)) * kLogStride;
-      const int i = atomicAdd(c, 1);
-      if (i < ulog_cap) ulog[(long long)(blockIdx.x & (kLogSlots - 1)) * ulog_cap + i] = a;
-      else c[1] = 1;
-    }
+    log_push(a);
+  }
+  // record arc a (and so its twin) in the undo log
+  __device__ __forceinline__ void log_push(int a) const {
+    if (!ulog) return;
+    int* c = ulog_n + (blockIdx.x & (kLogSlots - 1)) * kLogStride;
+    const int i = atomicAdd(c, 1);
+    if (i < ulog_cap) ulog[(long long)(blockIdx.x & (kLogSlots - 1)) * ulog_cap + i] = a;
+    else c[1] = 1;
   }
   __device__ __forceinline__ int twin_cf(int, int a) const {
     a = (int)chk(bd, a, bd.na);
@@ -293,6 +303,7 @@ struct TopoR {  // RCSR: forward {dst, cf_f} + cf_b, reverse {tail, forward id}
     a = (int)chk(bd, a, bd.na);
     return k == 0 ? fcb + a : &farc[chk(bd, __ldg(&rarc[a].y), bd.na)].y;
   }
+  __device__ __forceinline__ void log_push(int) const {}
 };
 
 template <class Topo>
@@ -328,6 +339,7 @@ struct Params {
   unsigned long long gr_threshold;
   int gr_rounds;  // global relabel at the latest after this many rounds
   int gr_stall;   // also after this many rounds in a row that moved no flow into t (0: off)
+  int greedy;     // fresh one-sink BCSR solves: route along x->t and x->y->t before the first round
   long long max_rounds;
   unsigned long long budget_ns;
   unsigned long long bar_timeout_ns;
@@ -367,7 +379,7 @@ __device__ __forceinline__ bool bfs_skip(const Params<Topo>& p, int v) {
 // Optional event trace (written by global thread 0 only; count in Stats).
 enum TraceKind : int {
   kTrLevel = 1, kTrRound = 2, kTrPassA = 3, kTrPassB = 4, kTrRelabel = 5, kTrGrEnd = 6, kTrSplit = 7,
-  kTrBuSplit = 8
+  kTrBuSplit = 8, kTrGreedy = 9
 };
 
 // Per-block counters, flushed to Stats once per phase.
@@ -1520,6 +1532,223 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// Greedy two-hop routing, right after the preflow of a fresh solve with one
+// sink on the BCSR layout: every vertex x that the preflow gave excess sends
+// what it can straight on to t, along x->t and along x->y->t, taking the
+// residual of each arc by compare-and-swap so that concurrent walkers never
+// take more than an arc holds.  Every such move is a valid push of a preflow
+// (a path of residual arcs whose middle vertex y keeps its excess), and labels
+// are not consulted: the global relabel that opens the first round computes
+// valid labels for whatever state this leaves.  So the maximum flow found is
+// the same.  In a CPU model of this pass (vertices in order, arcs in row
+// order) these moves carry 93% of the maximum flow of R-MAT scale 20 and 90%
+// of the 2M x 2M matching before the first round.
+// The y->t arc of each vertex y comes from the twins in t's row (an arc of
+// capacity 0 whose twin has positive capacity), kept in `esnap` until the
+// first global relabel files the active vertices (which overwrites it).
+#ifndef WBPR_GREEDY_ARCS
+#define WBPR_GREEDY_ARCS 1024
+#endif
+constexpr int kGreedyArcs = WBPR_GREEDY_ARCS;  // arcs of x's row a walker tries
+constexpr int kGreedyShort = 32;               // of them by the walker's own thread,
+constexpr int kGreedyBatch = 8;                //   eight in flight; the rest by a warp
+
+template <class Topo>
+__device__ __forceinline__ bool greedy_applies(const Params<Topo>& p) {
+  return Topo::kSeg == 1 && p.greedy && !p.term && p.t >= 0;
+}
+
+// Take up to `want` from the residual word *r (0 if it holds none).
+__device__ __forceinline__ int claim_residual(int* r, int want) {
+  int cur = ldv(r);
+  while (cur > 0 && want > 0) {
+    const int take = min(cur, want);
+    const int prev = atomicCAS(r, cur, cur - take);
+    if (prev == cur) return take;
+    cur = prev;
+  }
+  return 0;
+}
+
+template <class Topo>
+__device__ __forceinline__ void two_hop_arcs(const Params<Topo>&) {}
+__device__ __forceinline__ void two_hop_arcs(const Params<TopoB>& p) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+  int b, e;
+  p.g.seg(p.t, 0, b, e);
+  for (int a = b + gt; a < e; a += gs) {
+    const int2 x = __ldg(p.g.arx + a);  // {twin, capacity}
+    if (x.y != 0) continue;             // t's own arc, not the twin of an arc into t
+    if (__ldg(&p.g.arx[x.x].y) <= 0) continue;
+    const int y = p.g.head(0, a);
+    if (y != p.s) p.esnap[y] = x.x;
+  }
+}
+
+// Move up to `want` units out of x along arc a (x->y) and on along arc yt
+// (y->t), or straight along a when y is t (yt < 0).  Each residual is taken
+// by compare-and-swap; what y->t cannot take goes back to x->y.  Returns
+// the amount that reached t.
+__device__ __forceinline__ int route_to_sink(const Params<TopoB>& p, int a, int yt, int want) {
+  int* ra = &p.g.arc[a].y;
+  const int got1 = claim_residual(ra, want);
+  if (got1 <= 0) return 0;
+  int got = got1;
+  if (yt >= 0) {
+    got = claim_residual(&p.g.arc[yt].y, got1);
+    if (got < got1) atomicAdd(ra, got1 - got);  // hand back what y->t could not take
+    if (got <= 0) return 0;
+    atomicAdd(&p.g.arc[__ldg(&p.g.arx[yt].x)].y, got);
+    p.g.log_push(yt);
+  }
+  atomicAdd(&p.g.arc[__ldg(&p.g.arx[a].x)].y, got);
+  p.g.log_push(a);
+  return got;
+}
+
+// The walker of arc sa of s: its vertex x and the excess that arc delivered
+// (only s's own arcs carried preflow; a twin in s's row is the reverse of an
+// arc into s, its residual 0 at the preflow; what an arc carried is its
+// twin's residual now).  Returns the budget, 0 if the arc is no walker.
+__device__ __forceinline__ int walker_of(const Params<TopoB>& p, int sa, int& x) {
+  x = -1;
+  if (__ldg(&p.g.arx[sa].y) <= 0) return 0;
+  x = p.g.head(0, sa);
+  if (x == p.t || x == p.s) return 0;
+  return p.g.twin_cf(0, sa);
+}
+
+template <class Topo>
+__device__ __forceinline__ void two_hop_short(const Params<Topo>&, BlockAcc&) {}
+template <class Topo>
+__device__ __forceinline__ void two_hop_long(const Params<Topo>&, BlockAcc&) {}
+
+// Stage 1: a thread per walker over the first kGreedyShort arcs of x's row,
+// eight in flight.  A walker with excess and arcs left joins the list of long
+// walkers (fr[1]: its arc of s, fr[2]: its excess left).
+__device__ __forceinline__ void two_hop_short(const Params<TopoB>& p, BlockAcc& acc) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  int sb, se;
+  p.g.seg(p.s, 0, sb, se);
+  unsigned long long pushes = 0, scanned = 0;
+  int sink = 0;
+  for (int base = sb + gt - lane; base < se; base += gs) {  // whole warps, for the aggregated append
+    const int sa = base + lane;
+    int x = -1, budget = 0;
+    if (sa < se) budget = walker_of(p, sa, x);
+    const int budget0 = budget;
+    int xb = 0, xe = 0;
+    if (budget > 0) p.g.seg(x, 0, xb, xe);
+    const int xend = min(xe, xb + kGreedyShort);
+    for (int a0 = xb; a0 < xend && budget > 0; a0 += kGreedyBatch) {
+      int y[kGreedyBatch], cf[kGreedyBatch], yt[kGreedyBatch];
+#pragma unroll
+      for (int q = 0; q < kGreedyBatch; ++q) {
+        y[q] = -1;
+        cf[q] = 0;
+        if (a0 + q < xend) {
+          p.g.load(0, a0 + q, y[q], cf[q]);
+          ++scanned;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < kGreedyBatch; ++q)
+        yt[q] = (cf[q] > 0 && y[q] >= 0 && y[q] != p.s && y[q] != p.t) ? __ldcg(p.esnap + y[q]) : -1;
+#pragma unroll
+      for (int q = 0; q < kGreedyBatch; ++q) {
+        if (budget <= 0 || cf[q] <= 0 || y[q] < 0 || y[q] == p.s) continue;
+        if (y[q] != p.t && yt[q] < 0) continue;
+        const int got = route_to_sink(p, a0 + q, y[q] == p.t ? -1 : yt[q], min(budget, cf[q]));
+        if (got > 0) {
+          budget -= got;
+          sink += got;
+          pushes += y[q] == p.t ? 1 : 2;
+        }
+      }
+    }
+    if (budget < budget0) atomicSub(p.e + x, budget0 - budget);
+    const bool more = budget > 0 && xe > xend && kGreedyArcs > kGreedyShort;
+    const unsigned m = __ballot_sync(0xffffffffu, more);
+    if (m) {
+      int at = 0;
+      const int leader = __ffs(m) - 1;
+      if (lane == leader) at = atomicAdd(&p.ctl->glong, __popc(m));
+      at = __shfl_sync(0xffffffffu, at, leader) + __popc(m & ((1u << lane) - 1u));
+      if (more && at < p.n) {  // the lists hold n entries (parallel arcs of s could make more walkers)
+        p.fr[1][at] = sa;
+        p.fr[2][at] = budget;
+      }
+    }
+  }
+  if (sink) atomicAdd(&acc.sink, sink);
+  if (pushes) atomicAdd(&acc.pushes, pushes);
+  if (scanned) atomicAdd(&acc.scanned, scanned);
+}
+
+// Stage 2: a warp per long walker over arcs kGreedyShort .. kGreedyArcs of
+// x's row, 32 at a time.  The lanes' shares of the excess left follow arc
+// order by a saturating prefix sum (each capped at what the arc and its
+// y->t arc hold when read), and all lanes route their shares together.
+__device__ __forceinline__ void two_hop_long(const Params<TopoB>& p, BlockAcc& acc) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int nl = min(ldv(&p.ctl->glong), p.n);
+  unsigned long long pushes = 0, scanned = 0;
+  int sink = 0;
+  for (int w = gw; w < nl; w += nwarps) {
+    const int sa = __ldcg(p.fr[1] + w);
+    int budget = __ldcg(p.fr[2] + w);
+    const int budget0 = budget;
+    const int x = p.g.head(0, sa);
+    int xb, xe;
+    p.g.seg(x, 0, xb, xe);
+    const int xend = min(xe, xb + kGreedyArcs);
+    for (int a0 = xb + kGreedyShort; a0 < xend && budget > 0; a0 += 32) {
+      const int a = a0 + lane;
+      int y = -1, cf = 0, yt = -1, room = 0;
+      if (a < xend) {
+        p.g.load(0, a, y, cf);
+        if (lane == 0) scanned += (unsigned long long)min(32, xend - a0);
+      }
+      if (cf > 0 && y != p.s) {
+        if (y == p.t) {
+          room = cf;
+        } else {
+          yt = __ldcg(p.esnap + y);
+          if (yt >= 0) room = min(cf, ldv(&p.g.arc[yt].y));
+        }
+      }
+      unsigned incl = room > 0 ? (unsigned)room : 0u;
+      if (incl > (unsigned)budget) incl = (unsigned)budget;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const unsigned v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) {
+          incl += v;
+          if (incl > (unsigned)budget) incl = (unsigned)budget;
+        }
+      }
+      unsigned prev = __shfl_up_sync(0xffffffffu, incl, 1);
+      if (lane == 0) prev = 0;
+      const int share = (int)(incl - prev);
+      int got = 0;
+      if (share > 0) got = route_to_sink(p, a, y == p.t ? -1 : yt, share);
+      if (got > 0) pushes += y == p.t ? 1 : 2;
+      int tot = got;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+      budget -= tot;
+      sink += got;
+    }
+    if (lane == 0 && budget < budget0) atomicSub(p.e + x, budget0 - budget);
+  }
+  if (sink) atomicAdd(&acc.sink, sink);
+  if (pushes) atomicAdd(&acc.pushes, pushes);
+  if (scanned) atomicAdd(&acc.scanned, scanned);
+}
+
 __device__ __forceinline__ void clear_log(const TopoB& g, int gt) {
   if (g.ulog && gt < kLogSlots) {
     g.ulog_n[gt * kLogStride] = 0;
@@ -1560,10 +1789,12 @@ __global__ void __launch_bounds__(256, WBPR_PR_MIN_BLOCKS) pr_persistent(const _
   if (p.mode == kModeFresh) {
     // heights 0, excess 0, no pending relabel; residuals are reset by the
     // host-side reset kernel before this launch
+    const bool greedy = greedy_applies(p);
     for (int v = gt; v < p.n; v += gs) {
       p.lab[v] = 0;
       p.e[v] = 0;
       p.rl_min[v] = kNone;
+      if (greedy) p.esnap[v] = -1;  // the y->t arc of every vertex, filled below
     }
     // the residuals were restored before this launch: the undo log starts empty
     clear_log(p.g, gt);
@@ -1599,11 +1830,22 @@ __global__ void __launch_bounds__(256, WBPR_PR_MIN_BLOCKS) pr_persistent(const _
           }
         }
       }
+      if (greedy) two_hop_arcs(p);
+    }
+    if (greedy) {
+      if (!grid_sync(c, p.bar_timeout_ns)) return;
+      const unsigned long long tb = gtime();
+      two_hop_short(p, acc);
+      if (!grid_sync(c, p.bar_timeout_ns)) return;
+      two_hop_long(p, acc);
+      TRACE_BLOCK(p, tb);
+      flush_sink(p.e + p.t, acc);
     }
   } else {
     for (int v = gt; v < p.n; v += gs) p.rl_min[v] = kNone;
   }
   if (!grid_sync(c, p.bar_timeout_ns)) return;
+  if (p.mode == kModeFresh && greedy_applies(p) && gt == 0) TRACE(p, kTrGreedy, 0, ldv(p.e + p.t), 0);
 
   int cur = 0, raw = 0, rounds = 0;
   bool need_gr = true;
