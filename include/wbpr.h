@@ -90,7 +90,7 @@ typedef struct wbpr_tuning {
                          /* (128 arcs in flight) instead of a tile (0 = 32)       */
   int32_t blocks_per_sm; /* resident blocks per SM for the persistent grid (0=max) */
   double gr_alpha;       /* global relabel after alpha*(n + arcs) units of work   */
-                         /* (0 = 0.75)                                            */
+                         /* (0 = 1.0)                                             */
   int64_t max_rounds;    /* push/relabel round budget (0 = unlimited)             */
   double max_ms;         /* wall-clock budget of one solve in ms (0 = 120000)     */
   int32_t verify;        /* 1: run the device certificate check after the solve  */
@@ -101,7 +101,7 @@ typedef struct wbpr_tuning {
                          /* <= 2^21: SMs / 2; <= 2^22: SMs; <= 2^24: 2 x SMs;     */
                          /* larger: every SM x blocks_per_sm)                     */
   int32_t gr_stall;      /* also relabel globally after this many rounds in a row */
-                         /* that moved no flow into t (0 = auto: 2 when n + arcs  */
+                         /* that moved no flow into t (0 = auto: 1 when n + arcs  */
                          /* > 2^22, else never; -1 = never)                       */
   int64_t barrier_timeout_ns; /* a grid-barrier wait gives up after this long and */
                          /* the solve returns WBPR_ERR_TIMEOUT (0 = 10 s)         */
@@ -300,7 +300,7 @@ wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo,
 wbpr_status wbpr_solve_pairs(wbpr_graph* g, int32_t k, const int32_t* sources, const int32_t* sinks,
                              wbpr_algo algo, const wbpr_tuning* tuning, int64_t* flows, wbpr_result* out);
 /* Try tile widths {8, 16, 32} (VC; TC has one), global-relabel work factors
- * {0.5, 0.75, 1.5, 3} and long-row thresholds {32, 64} on this graph and
+ * {0.5, 1, 1.5, 3} and long-row thresholds {32, 64} on this graph and
  * these terminals (the faster of two solves each); return the fastest tuning
  * and its solve time.  Every tuning must give the same flow (WBPR_ERR_VERIFY
  * otherwise).  The graph's state afterwards is that of the last solve. */

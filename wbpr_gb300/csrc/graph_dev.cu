@@ -211,26 +211,24 @@ __global__ void reset_bcsr(int2* arc, const int2* arx, long long na) {
     arc[a].y = __ldg(&arx[a].y);
 }
 // Restore the residuals a BCSR16 solve changed: every logged arc and its twin
-// get their capacity back.  A slot that overflowed (or `full`) makes it a
-// rewrite of all `na` arcs, as reset_bcsr.
+// get their capacity back, a block per log slot (slot k to block k mod
+// blocks).  A slot that overflowed (or `full`) makes it a rewrite of all
+// `na` arcs, as reset_bcsr.  The overflow words are read by the block's
+// threads together.
 __global__ void reset_logged(int2* arc, const int2* arx, long long na, const int* ulog, const int* ulog_n,
                              int cap, int full) {
-  __shared__ int s_full;
-  if (threadIdx.x == 0) {
-    int f = full;
-    for (int k = 0; k < kLogSlots; ++k) f |= ulog_n[k * kLogStride + 1];
-    s_full = f;
-  }
-  __syncthreads();
-  const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x, gs = (long long)gridDim.x * blockDim.x;
-  if (s_full) {
+  int f = full;
+  for (int k = threadIdx.x; k < kLogSlots; k += blockDim.x) f |= ulog_n[k * kLogStride + 1];
+  if (__syncthreads_or(f)) {
+    const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long gs = (long long)gridDim.x * blockDim.x;
     for (long long a = gt; a < na; a += gs) arc[a].y = __ldg(&arx[a].y);
     return;
   }
-  for (int k = 0; k < kLogSlots; ++k) {
+  for (int k = blockIdx.x; k < kLogSlots; k += gridDim.x) {
     const int cnt = min(ulog_n[k * kLogStride], cap);
     const int* lg = ulog + (long long)k * cap;
-    for (long long i = gt; i < cnt; i += gs) {
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
       const int a = lg[i];
       const int2 x = __ldg(arx + a);
       arc[a].y = x.y;
@@ -1176,9 +1174,9 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   TRY(dalloc(g, &g->ctl, 1));
   TRY(dalloc(g, &g->st, 1));
   if (g->layout == WBPR_LAYOUT_BCSR && g->m > 0) {
-    // undo log: an eighth of the residual arcs (at least 2^20 entries), over
+    // undo log: a quarter of the residual arcs (at least 2^20 entries), over
     // kLogSlots slots; the built residuals are the capacities, so it starts empty
-    const int64_t want = std::max<int64_t>((2 * g->m) / 8, (int64_t)1 << 20);
+    const int64_t want = std::max<int64_t>((2 * g->m) / 4, (int64_t)1 << 20);
     g->ulog_cap = (int)((want + kLogSlots - 1) / kLogSlots);
     TRY(dalloc(g, &g->ulog, (size_t)g->ulog_cap * kLogSlots));
     TRY(dalloc(g, &g->ulog_n, (size_t)kLogSlots * kLogStride));
@@ -1192,6 +1190,11 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   return WBPR_OK;
 }
 
+// global relabel after this many times (n + residual arcs) units of scan work
+// (measured on GB300 with the greedy routing on: R-MAT scale 20 and 22 and
+// layered networks gain 4-18% over 0.75, R-MAT scale 16 and the 2M x 2M
+// matching lose 5-13%; the matching's best is 0.5, which wbpr_autotune finds)
+constexpr double kDefaultGrAlpha = 1.0;
 // a grid-barrier wait gives up after this long unless the tuning says otherwise
 constexpr unsigned long long kBarrierTimeoutNs = 10ull * 1000 * 1000 * 1000;
 
@@ -1363,7 +1366,7 @@ wbpr_status run(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch_ms = n
 
 void tuning_defaults(wbpr_tuning* t) {
   std::memset(t, 0, sizeof(*t));
-  t->gr_alpha = 0.75;
+  t->gr_alpha = kDefaultGrAlpha;
   t->max_ms = 120000.0;
 }
 
@@ -1387,7 +1390,7 @@ wbpr_status make_cfg(wbpr_graph* g, int s, int t, wbpr_algo algo, const wbpr_tun
   if (tu->grid_blocks < 0) return WBPR_ERR_INVALID_ARG;
   rc->grid_blocks = tu->grid_blocks;
   rc->heavy_deg = tu->heavy_degree > 0 ? tu->heavy_degree : 32;
-  const double alpha = tu->gr_alpha > 0 ? tu->gr_alpha : 0.75;
+  const double alpha = tu->gr_alpha > 0 ? tu->gr_alpha : kDefaultGrAlpha;
   rc->gr_threshold = (unsigned long long)(alpha * ((double)g->n + (double)g->total_deg)) + 1;
   rc->gr_rounds = tu->gr_rounds > 0 ? tu->gr_rounds : 48;
   if (tu->gr_stall < -1 || tu->barrier_timeout_ns < 0 || tu->greedy < -1 || tu->greedy > 0)
@@ -1501,7 +1504,7 @@ wbpr_status wbpr_autotune(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, w
   if (!g || !best) return WBPR_ERR_INVALID_ARG;
   const int tiles_vc[] = {8, 16, 32};
   const int tiles_tc[] = {0};
-  const double alphas[] = {0.5, 0.75, 1.5, 3.0};
+  const double alphas[] = {0.5, 1.0, 1.5, 3.0};
   const int heavies[] = {32, 64};
   const int* tiles = algo == WBPR_ALGO_TC ? tiles_tc : tiles_vc;
   const int ntiles = algo == WBPR_ALGO_TC ? 1 : 3;

@@ -80,6 +80,7 @@ struct Ctl {
   alignas(128) int bu_found[3];  // vertices labelled by a bottom-up level, by level % 3
   int mcount;       // materialised frontier: short rows
   int glong;        // greedy routing: walkers left for the warp stage
+  alignas(128) int glong_next;  //   and the claim counter of that stage
   int mhcount;      //   long-row chunk items
   alignas(128) int gr_ok;  // the rounds since the last global relabel took at least half as long as it
   int stalled;             // excess(t) has not changed for gr_stall rounds
@@ -187,9 +188,11 @@ __device__ __forceinline__ long long chk(const Bounds& b, long long i, long long
 // Undo log of a BCSR16 graph: every push records its arc, so the next fresh
 // solve restores only the arcs (and their twins) that changed instead of
 // rewriting all 2m residuals.  kLogSlots counters, one per 128-byte line,
-// picked by block, each owning `ulog_cap` entries; a slot that fills up sets
-// its overflow word and the next restore rewrites every arc.
-constexpr int kLogSlots = 32;
+// picked by warp (a burst of pushes, as in the greedy routing after the
+// preflow, would otherwise queue on a few counters), each owning `ulog_cap`
+// entries; a slot that fills up sets its overflow word and the next restore
+// rewrites every arc.
+constexpr int kLogSlots = 256;
 constexpr int kLogStride = 32;  // ints between two slot counters: [0] count, [1] overflow
 
 struct TopoB {  // BCSR16: row[n+1], arc {dst, cf}, arx {rev, cap}
@@ -231,9 +234,10 @@ struct TopoB {  // BCSR16: row[n+1], arc {dst, cf}, arx {rev, cap}
   // record arc a (and so its twin) in the undo log
   __device__ __forceinline__ void log_push(int a) const {
     if (!ulog) return;
-    int* c = ulog_n + (blockIdx.x & (kLogSlots - 1)) * kLogStride;
+    const int slot = ((blockIdx.x << 3) + (threadIdx.x >> 5)) & (kLogSlots - 1);  // by warp
+    int* c = ulog_n + slot * kLogStride;
     const int i = atomicAdd(c, 1);
-    if (i < ulog_cap) ulog[(long long)(blockIdx.x & (kLogSlots - 1)) * ulog_cap + i] = a;
+    if (i < ulog_cap) ulog[(long long)slot * ulog_cap + i] = a;
     else c[1] = 1;
   }
   __device__ __forceinline__ int twin_cf(int, int a) const {
@@ -1559,9 +1563,11 @@ __device__ __forceinline__ bool greedy_applies(const Params<Topo>& p) {
   return Topo::kSeg == 1 && p.greedy && !p.term && p.t >= 0;
 }
 
-// Take up to `want` from the residual word *r (0 if it holds none).
-__device__ __forceinline__ int claim_residual(int* r, int want) {
-  int cur = ldv(r);
+// Take up to `want` from the residual word *r (0 if it holds none); `hint`
+// is the value last read there (a guess for the first compare-and-swap), or
+// -1 to read it first.
+__device__ __forceinline__ int claim_residual(int* r, int want, int hint = -1) {
+  int cur = hint >= 0 ? hint : ldv(r);
   while (cur > 0 && want > 0) {
     const int take = min(cur, want);
     const int prev = atomicCAS(r, cur, cur - take);
@@ -1590,9 +1596,9 @@ __device__ __forceinline__ void two_hop_arcs(const Params<TopoB>& p) {
 // (y->t), or straight along a when y is t (yt < 0).  Each residual is taken
 // by compare-and-swap; what y->t cannot take goes back to x->y.  Returns
 // the amount that reached t.
-__device__ __forceinline__ int route_to_sink(const Params<TopoB>& p, int a, int yt, int want) {
+__device__ __forceinline__ int route_to_sink(const Params<TopoB>& p, int a, int yt, int want, int cf_hint) {
   int* ra = &p.g.arc[a].y;
-  const int got1 = claim_residual(ra, want);
+  const int got1 = claim_residual(ra, want, cf_hint);
   if (got1 <= 0) return 0;
   int got = got1;
   if (yt >= 0) {
@@ -1607,16 +1613,15 @@ __device__ __forceinline__ int route_to_sink(const Params<TopoB>& p, int a, int 
   return got;
 }
 
-// The walker of arc sa of s: its vertex x and the excess that arc delivered
-// (only s's own arcs carried preflow; a twin in s's row is the reverse of an
-// arc into s, its residual 0 at the preflow; what an arc carried is its
-// twin's residual now).  Returns the budget, 0 if the arc is no walker.
+// The walker of arc sa of s: its vertex x and the excess that arc delivered.
+// Only s's own arcs carried preflow (a twin in s's row is the reverse of an
+// arc into s, with capacity 0), and a fresh solve's preflow pushed each one's
+// whole capacity.  Returns the budget, 0 if the arc is no walker.
 __device__ __forceinline__ int walker_of(const Params<TopoB>& p, int sa, int& x) {
-  x = -1;
-  if (__ldg(&p.g.arx[sa].y) <= 0) return 0;
+  const int cap = __ldg(&p.g.arx[sa].y);
   x = p.g.head(0, sa);
-  if (x == p.t || x == p.s) return 0;
-  return p.g.twin_cf(0, sa);
+  if (cap <= 0 || x == p.t || x == p.s) return 0;
+  return cap;
 }
 
 template <class Topo>
@@ -1660,7 +1665,7 @@ __device__ __forceinline__ void two_hop_short(const Params<TopoB>& p, BlockAcc& 
       for (int q = 0; q < kGreedyBatch; ++q) {
         if (budget <= 0 || cf[q] <= 0 || y[q] < 0 || y[q] == p.s) continue;
         if (y[q] != p.t && yt[q] < 0) continue;
-        const int got = route_to_sink(p, a0 + q, y[q] == p.t ? -1 : yt[q], min(budget, cf[q]));
+        const int got = route_to_sink(p, a0 + q, y[q] == p.t ? -1 : yt[q], min(budget, cf[q]), cf[q]);
         if (got > 0) {
           budget -= got;
           sink += got;
@@ -1697,7 +1702,11 @@ __device__ __forceinline__ void two_hop_long(const Params<TopoB>& p, BlockAcc& a
   const int nl = min(ldv(&p.ctl->glong), p.n);
   unsigned long long pushes = 0, scanned = 0;
   int sink = 0;
-  for (int w = gw; w < nl; w += nwarps) {
+  // first walker by warp index, the rest claimed (walks differ in length)
+  for (int w = gw; w < nl;) {
+    int nx = 0;
+    if (lane == 0) nx = nwarps + atomicAdd(&p.ctl->glong_next, 1);
+    nx = __shfl_sync(0xffffffffu, nx, 0);
     const int sa = __ldcg(p.fr[1] + w);
     int budget = __ldcg(p.fr[2] + w);
     const int budget0 = budget;
@@ -1734,7 +1743,7 @@ __device__ __forceinline__ void two_hop_long(const Params<TopoB>& p, BlockAcc& a
       if (lane == 0) prev = 0;
       const int share = (int)(incl - prev);
       int got = 0;
-      if (share > 0) got = route_to_sink(p, a, y == p.t ? -1 : yt, share);
+      if (share > 0) got = route_to_sink(p, a, y == p.t ? -1 : yt, share, cf);
       if (got > 0) pushes += y == p.t ? 1 : 2;
       int tot = got;
 #pragma unroll
@@ -1743,6 +1752,7 @@ __device__ __forceinline__ void two_hop_long(const Params<TopoB>& p, BlockAcc& a
       sink += got;
     }
     if (lane == 0 && budget < budget0) atomicSub(p.e + x, budget0 - budget);
+    w = nx;
   }
   if (sink) atomicAdd(&acc.sink, sink);
   if (pushes) atomicAdd(&acc.pushes, pushes);
@@ -1834,9 +1844,12 @@ __global__ void __launch_bounds__(256, WBPR_PR_MIN_BLOCKS) pr_persistent(const _
     }
     if (greedy) {
       if (!grid_sync(c, p.bar_timeout_ns)) return;
-      const unsigned long long tb = gtime();
+      unsigned long long tb = gtime();
       two_hop_short(p, acc);
+      TRACE_BLOCK(p, tb);
       if (!grid_sync(c, p.bar_timeout_ns)) return;
+      if (gt == 0) TRACE(p, kTrGreedy, 1, ldv(&c->glong), 0);
+      tb = gtime();
       two_hop_long(p, acc);
       TRACE_BLOCK(p, tb);
       flush_sink(p.e + p.t, acc);
@@ -1845,10 +1858,11 @@ __global__ void __launch_bounds__(256, WBPR_PR_MIN_BLOCKS) pr_persistent(const _
     for (int v = gt; v < p.n; v += gs) p.rl_min[v] = kNone;
   }
   if (!grid_sync(c, p.bar_timeout_ns)) return;
-  if (p.mode == kModeFresh && greedy_applies(p) && gt == 0) TRACE(p, kTrGreedy, 0, ldv(p.e + p.t), 0);
+  if (p.mode == kModeFresh && greedy_applies(p) && gt == 0) TRACE(p, kTrGreedy, 2, ldv(p.e + p.t), 0);
 
   int cur = 0, raw = 0, rounds = 0;
   bool need_gr = true;
+  int gr_why = 0;  // trace only: what started the coming global relabel (bit 0 work, 1 rounds, 2 no flow)
   // work since the last global relabel: every block adds the per-round
   // counter of the finished round (final at the barrier), so all agree
   unsigned long long work = 0;
@@ -1872,7 +1886,7 @@ __global__ void __launch_bounds__(256, WBPR_PR_MIN_BLOCKS) pr_persistent(const _
         gr_last = gr_end - t0;
         gr_ns += gr_last;
         atomicAdd(&p.st->grs, 1);
-        TRACE(p, kTrGrEnd, 0, 0, 0);
+        TRACE(p, kTrGrEnd, gr_why, (long long)work, since_gr);
       }
       need_gr = false;
       work = 0;
@@ -1964,7 +1978,10 @@ __global__ void __launch_bounds__(256, WBPR_PR_MIN_BLOCKS) pr_persistent(const _
     // instead of letting it climb towards n over many rounds.
     // (published by global thread 0 before the barrier, read by all after it)
     const bool stalled = ldv(&c->stalled) != 0;
-    if ((work > p.gr_threshold || since_gr >= p.gr_rounds || stalled) && ldv(&c->gr_ok)) need_gr = true;
+    if ((work > p.gr_threshold || since_gr >= p.gr_rounds || stalled) && ldv(&c->gr_ok)) {
+      need_gr = true;
+      if (p.trace) gr_why = (work > p.gr_threshold) | (since_gr >= p.gr_rounds) << 1 | (int)stalled << 2;
+    }
   }
   // callers see label n for every vertex that cannot reach the sink (every
   // block has left the loop after the same barrier and reads no label now)

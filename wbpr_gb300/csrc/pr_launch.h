@@ -32,8 +32,9 @@ inline int grid_blocks_for(long long units, int sms, int full) {
 
 // Default of the no-flow-into-t global-relabel trigger (rounds in a row, 0:
 // off).  On R-MAT scale 20/22 and the 2M x 2M bipartite graph it cut 5-18%
-// of the solve; on graphs of at most 2^22 units (GENRMF, layered networks,
-// 512 x 512 grids) it ran extra global relabels and cost 0-25%.
-inline int default_gr_stall(long long units) { return units > (1LL << 22) ? 2 : 0; }
+// of the solve, one round a little more than two after the greedy routing;
+// on graphs of at most 2^22 units (GENRMF, layered networks, 512 x 512 grids)
+// it ran extra global relabels and cost 0-25%.
+inline int default_gr_stall(long long units) { return units > (1LL << 22) ? 1 : 0; }
 
 }  // namespace wbpr_dev
