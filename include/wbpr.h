@@ -108,7 +108,9 @@ typedef struct wbpr_tuning {
   int32_t greedy;        /* BCSR solves with one sink: 0 = route excess along      */
                          /* x->t and x->y->t paths right after the preflow (the   */
                          /* same maximum flow, fewer rounds); -1 = off            */
-  int32_t pad0;
+  int32_t bfs_alpha;     /* a global relabel's BFS turns bottom-up when the        */
+                         /* frontier's arcs x this exceed the unvisited arcs      */
+                         /* (0 = 14)                                              */
 } wbpr_tuning;
 
 typedef struct wbpr_result {

@@ -1269,6 +1269,7 @@ struct RunCfg {
   int gr_rounds;
   int gr_stall;
   int greedy;
+  int bfs_alpha;
   long long max_rounds;
   unsigned long long budget_ns;
   unsigned long long bar_timeout_ns;
@@ -1296,6 +1297,7 @@ wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch
   p.gr_rounds = rc.gr_rounds;
   p.gr_stall = rc.gr_stall;
   p.greedy = rc.greedy;
+  if (rc.bfs_alpha > 0) p.bfs_alpha = rc.bfs_alpha;
   if (rc.bar_timeout_ns) p.bar_timeout_ns = rc.bar_timeout_ns;
   p.max_rounds = rc.max_rounds;
   p.budget_ns = rc.budget_ns;
@@ -1396,6 +1398,8 @@ wbpr_status make_cfg(wbpr_graph* g, int s, int t, wbpr_algo algo, const wbpr_tun
   if (tu->gr_stall < -1 || tu->barrier_timeout_ns < 0 || tu->greedy < -1 || tu->greedy > 0)
     return WBPR_ERR_INVALID_ARG;
   rc->greedy = tu->greedy == 0 ? 1 : 0;
+  if (tu->bfs_alpha < 0) return WBPR_ERR_INVALID_ARG;
+  rc->bfs_alpha = tu->bfs_alpha;
   rc->gr_stall = tu->gr_stall == 0 ? default_gr_stall((long long)g->n + g->total_deg)
                                    : (tu->gr_stall < 0 ? 0 : tu->gr_stall);
   rc->bar_timeout_ns = tu->barrier_timeout_ns > 0 ? (unsigned long long)tu->barrier_timeout_ns : kBarrierTimeoutNs;

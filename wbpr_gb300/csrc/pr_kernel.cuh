@@ -42,14 +42,8 @@ namespace cg = cooperative_groups;
 
 constexpr int kNone = -1;
 constexpr int kBig = 0x7fffffff;
-#ifndef WBPR_BFS_ALPHA
-#define WBPR_BFS_ALPHA 14
-#endif
-#ifndef WBPR_BFS_BETA
-#define WBPR_BFS_BETA 24
-#endif
-constexpr int kBfsAlpha = WBPR_BFS_ALPHA;  // top-down -> bottom-up when frontier arcs * alpha > unvisited arcs
-constexpr int kBfsBeta = WBPR_BFS_BETA;    // bottom-up -> top-down when frontier * beta < n
+constexpr int kBfsAlpha = 14;  // default: top-down -> bottom-up when frontier arcs * alpha > unvisited arcs
+constexpr int kBfsBeta = 24;   // bottom-up -> top-down when frontier * beta < n
 constexpr int kLightDeg = 32;  // BFS: rows up to this length scanned by one thread
 constexpr int kHeavyDeg = 2048;  // BFS: rows longer than this scanned by a whole block
 constexpr int kChunk = 2048;     // BFS: heavy rows are cut into static chunks of this many arcs
@@ -344,6 +338,7 @@ struct Params {
   int gr_rounds;  // global relabel at the latest after this many rounds
   int gr_stall;   // also after this many rounds in a row that moved no flow into t (0: off)
   int greedy;     // fresh one-sink BCSR solves: route along x->t and x->y->t before the first round
+  int bfs_alpha = kBfsAlpha;  // the BFS goes bottom-up when frontier arcs * this > unvisited arcs
   long long max_rounds;
   unsigned long long budget_ns;
   unsigned long long bar_timeout_ns;
@@ -1449,7 +1444,7 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
     const long long fdeg = ldv64(&c->fdeg[fc]);
     visited += fdeg;
     const long long rem = p.total_deg - dead - visited;
-    if (!bu && fdeg * kBfsAlpha > rem) bu = true;
+    if (!bu && fdeg * p.bfs_alpha > rem) bu = true;
     else if (bu && (long long)nf * kBfsBeta < (long long)p.n) bu = false;
     const bool mat = !bu && prev_bu;
     int nl = 0, nlh = 0;
