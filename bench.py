@@ -591,7 +591,8 @@ def config2(args):
         # the library's own tuning search (wbpr_autotune), outside the timing;
         # unit-capacity matching gains from more frequent global relabels
         tu, _ = d.autotune("vc", g.s, g.t)
-        kw = {"tile": tu.tile, "gr_alpha": tu.gr_alpha, "heavy_degree": tu.heavy_degree}
+        kw = {"tile": tu.tile, "gr_alpha": tu.gr_alpha, "heavy_degree": tu.heavy_degree,
+              "bfs_alpha": tu.bfs_alpha, "gr_plateau": tu.gr_plateau}
         for _ in range(args.warmup):
             d.solve("vc", g.s, g.t, **kw)
         r = [d.solve("vc", g.s, g.t, **kw) for _ in range(args.steps)]

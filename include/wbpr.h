@@ -111,6 +111,10 @@ typedef struct wbpr_tuning {
   int32_t bfs_alpha;     /* a global relabel's BFS turns bottom-up when the        */
                          /* frontier's arcs x this exceed the unvisited arcs      */
                          /* (0 = 14)                                              */
+  int32_t gr_plateau;    /* also relabel globally when the active set shrank by   */
+                         /* less than 10% over this many rounds, 1..8 (0 or -1 =  */
+                         /* never, the default)                                   */
+  int32_t pad1;
 } wbpr_tuning;
 
 typedef struct wbpr_result {
@@ -303,8 +307,9 @@ wbpr_status wbpr_solve_pairs(wbpr_graph* g, int32_t k, const int32_t* sources, c
                              wbpr_algo algo, const wbpr_tuning* tuning, int64_t* flows, wbpr_result* out);
 /* Try tile widths {8, 16, 32} (VC; TC has one), global-relabel work factors
  * {0.5, 1, 1.5, 3} and long-row thresholds {32, 64} on this graph and
- * these terminals (the faster of two solves each); return the fastest tuning
- * and its solve time.  Every tuning must give the same flow (WBPR_ERR_VERIFY
+ * these terminals (the faster of two solves each), then the best of those
+ * with bfs_alpha 4, gr_plateau 4 and both; return the fastest tuning and its
+ * solve time.  Every tuning must give the same flow (WBPR_ERR_VERIFY
  * otherwise).  The graph's state afterwards is that of the last solve. */
 wbpr_status wbpr_autotune(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, wbpr_tuning* best,
                           float* best_ms);

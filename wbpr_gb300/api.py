@@ -49,7 +49,8 @@ class Tuning(C.Structure):
                 ("blocks_per_sm", C.c_int32), ("gr_alpha", C.c_double), ("max_rounds", C.c_int64),
                 ("max_ms", C.c_double), ("verify", C.c_int32), ("trace", C.c_int32),
                 ("gr_rounds", C.c_int32), ("grid_blocks", C.c_int32), ("gr_stall", C.c_int32),
-                ("barrier_timeout_ns", C.c_int64), ("greedy", C.c_int32), ("bfs_alpha", C.c_int32)]
+                ("barrier_timeout_ns", C.c_int64), ("greedy", C.c_int32), ("bfs_alpha", C.c_int32),
+                ("gr_plateau", C.c_int32), ("pad1", C.c_int32)]
 
 
 class Result(C.Structure):

@@ -1180,21 +1180,18 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
     g->ulog_cap = (int)((want + kLogSlots - 1) / kLogSlots);
     TRY(dalloc(g, &g->ulog, (size_t)g->ulog_cap * kLogSlots));
     TRY(dalloc(g, &g->ulog_n, (size_t)kLogSlots * kLogStride));
-    TRYC(cudaMemset(g->ulog_n, 0, sizeof(int) * (size_t)kLogSlots * kLogStride));
+    TRYC(cudaMemsetAsync(g->ulog_n, 0, sizeof(int) * (size_t)kLogSlots * kLogStride, g->stream));
   }
-  TRYC(cudaMemset(g->h, 0, 4 * (size_t)n));
-  TRYC(cudaMemset(g->e, 0, 4 * (size_t)n));
+  // in the stream the pool allocations were made on (stream-ordered memory)
+  TRYC(cudaMemsetAsync(g->h, 0, 4 * (size_t)n, g->stream));
+  TRYC(cudaMemsetAsync(g->e, 0, 4 * (size_t)n, g->stream));
+  TRYC(cudaStreamSynchronize(g->stream));
 #undef TRY
 #undef TRYC
   *out = g;
   return WBPR_OK;
 }
 
-// global relabel after this many times (n + residual arcs) units of scan work
-// (measured on GB300 with the greedy routing on: R-MAT scale 20 and 22 and
-// layered networks gain 4-18% over 0.75, R-MAT scale 16 and the 2M x 2M
-// matching lose 5-13%; the matching's best is 0.5, which wbpr_autotune finds)
-constexpr double kDefaultGrAlpha = 1.0;
 // a grid-barrier wait gives up after this long unless the tuning says otherwise
 constexpr unsigned long long kBarrierTimeoutNs = 10ull * 1000 * 1000 * 1000;
 
@@ -1270,6 +1267,7 @@ struct RunCfg {
   int gr_stall;
   int greedy;
   int bfs_alpha;
+  int gr_plateau;
   long long max_rounds;
   unsigned long long budget_ns;
   unsigned long long bar_timeout_ns;
@@ -1298,6 +1296,7 @@ wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch
   p.gr_stall = rc.gr_stall;
   p.greedy = rc.greedy;
   if (rc.bfs_alpha > 0) p.bfs_alpha = rc.bfs_alpha;
+  p.gr_plateau = rc.gr_plateau;
   if (rc.bar_timeout_ns) p.bar_timeout_ns = rc.bar_timeout_ns;
   p.max_rounds = rc.max_rounds;
   p.budget_ns = rc.budget_ns;
@@ -1400,6 +1399,8 @@ wbpr_status make_cfg(wbpr_graph* g, int s, int t, wbpr_algo algo, const wbpr_tun
   rc->greedy = tu->greedy == 0 ? 1 : 0;
   if (tu->bfs_alpha < 0) return WBPR_ERR_INVALID_ARG;
   rc->bfs_alpha = tu->bfs_alpha;
+  if (tu->gr_plateau < -1 || tu->gr_plateau > kMaxPlateau) return WBPR_ERR_INVALID_ARG;
+  rc->gr_plateau = tu->gr_plateau == 0 ? kDefaultPlateau : (tu->gr_plateau < 0 ? 0 : tu->gr_plateau);
   rc->gr_stall = tu->gr_stall == 0 ? default_gr_stall((long long)g->n + g->total_deg)
                                    : (tu->gr_stall < 0 ? 0 : tu->gr_stall);
   rc->bar_timeout_ns = tu->barrier_timeout_ns > 0 ? (unsigned long long)tu->barrier_timeout_ns : kBarrierTimeoutNs;
@@ -1538,6 +1539,27 @@ wbpr_status wbpr_autotune(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, w
           *best = tu;
         }
       }
+  // then, on the best of those, the global relabel's BFS turning bottom-up
+  // earlier and the plateau trigger (both pay on unit-capacity matching
+  // networks and lose on GENRMF, layered networks and large R-MAT graphs)
+  const wbpr_tuning base = *best;
+  for (int k = 0; k < 3; ++k) {
+    wbpr_tuning tu = base;
+    if (k != 1) tu.bfs_alpha = 4;
+    if (k != 0) tu.gr_plateau = 4;
+    float ms = 0;
+    for (int rep = 0; rep < 2; ++rep) {
+      wbpr_result r;
+      const wbpr_status st = wbpr_solve(g, s, t, algo, &tu, &r);
+      if (st) return st;
+      if (r.flow != flow) return WBPR_ERR_VERIFY;
+      ms = rep ? std::min(ms, r.solve_ms) : r.solve_ms;
+    }
+    if (ms < bms) {
+      bms = ms;
+      *best = tu;
+    }
+  }
   if (best_ms) *best_ms = bms;
   return WBPR_OK;
 }

@@ -281,10 +281,11 @@ extern "C" wbpr_status wbpr_solve_bcsr_noalloc(int32_t n, int64_t num_residual_a
   p.ctl = ctl;
   p.st = stats;
   p.total_deg = num_residual_arcs;
-  p.gr_threshold = (unsigned long long)(0.75 * ((double)n + (double)num_residual_arcs)) + 1;
+  p.gr_threshold = (unsigned long long)(kDefaultGrAlpha * ((double)n + (double)num_residual_arcs)) + 1;
   p.gr_rounds = 48;
   p.gr_stall = default_gr_stall((long long)n + num_residual_arcs);
   p.greedy = 1;
+  p.gr_plateau = kDefaultPlateau;
   p.budget_ns = 120ull * 1000 * 1000 * 1000;
   p.bar_timeout_ns = 10ull * 1000 * 1000 * 1000;
   p.heavy_deg = 32;

@@ -42,6 +42,7 @@ namespace cg = cooperative_groups;
 
 constexpr int kNone = -1;
 constexpr int kBig = 0x7fffffff;
+constexpr int kMaxPlateau = 8;
 constexpr int kBfsAlpha = 14;  // default: top-down -> bottom-up when frontier arcs * alpha > unvisited arcs
 constexpr int kBfsBeta = 24;   // bottom-up -> top-down when frontier * beta < n
 constexpr int kLightDeg = 32;  // BFS: rows up to this length scanned by one thread
@@ -339,6 +340,8 @@ struct Params {
   int gr_stall;   // also after this many rounds in a row that moved no flow into t (0: off)
   int greedy;     // fresh one-sink BCSR solves: route along x->t and x->y->t before the first round
   int bfs_alpha = kBfsAlpha;  // the BFS goes bottom-up when frontier arcs * this > unvisited arcs
+  int gr_plateau = 0;         // also relabel globally when the active set shrank by less than 10% over
+                              // this many rounds (1..kMaxPlateau; 0: off)
   long long max_rounds;
   unsigned long long budget_ns;
   unsigned long long bar_timeout_ns;
@@ -1857,7 +1860,9 @@ __global__ void __launch_bounds__(256, WBPR_PR_MIN_BLOCKS) pr_persistent(const _
 
   int cur = 0, raw = 0, rounds = 0;
   bool need_gr = true;
-  int gr_why = 0;  // trace only: what started the coming global relabel (bit 0 work, 1 rounds, 2 no flow)
+  int gr_why = 0;  // trace only: what started the coming global relabel (bit 0 work, 1 rounds, 2 no
+                   // flow, 3 active set not shrinking)
+  int act_hist[kMaxPlateau];  // active counts of the last gr_plateau rounds, by since_gr % gr_plateau
   // work since the last global relabel: every block adds the per-round
   // counter of the finished round (final at the barrier), so all agree
   unsigned long long work = 0;
@@ -1890,6 +1895,17 @@ __global__ void __launch_bounds__(256, WBPR_PR_MIN_BLOCKS) pr_persistent(const _
     const int nL = ldv(&c->lcount[cur]), nH = ldv(&c->hcount[cur]);
     const int nact = nL + nH;
     if (nact == 0) break;
+    // An active set that stopped shrinking is excess circling without
+    // reaching t (its labels climb a step or two a round): a global relabel
+    // retires what cannot reach t at once.  The counts are final at the
+    // barrier, so every block takes the same branch.
+    if (p.gr_plateau > 0 && since_gr >= p.gr_plateau &&
+        (long long)nact * 10 >= (long long)act_hist[since_gr % p.gr_plateau] * 9 && ldv(&c->gr_ok)) {
+      need_gr = true;
+      if (p.trace) gr_why = 8;
+      continue;
+    }
+    if (p.gr_plateau > 0) act_hist[since_gr % p.gr_plateau] = nact;
     if (ldv(&c->stop)) {
       if (gt == 0) atomicCAS(&c->err, 0, (int)WBPR_ERR_NO_CONVERGENCE);
       break;

@@ -30,6 +30,18 @@ inline int grid_blocks_for(long long units, int sms, int full) {
   return full;
 }
 
+// Global relabel after this many times (n + residual arcs) units of scan work
+// (measured on GB300 with the greedy routing on: R-MAT scale 20 and 22 and
+// layered networks gain 4-18% over 0.75, R-MAT scale 16 and the 2M x 2M
+// matching lose 5-13%; the matching's best is 0.5, which wbpr_autotune finds).
+constexpr double kDefaultGrAlpha = 1.0;
+// Also relabel globally when the active set shrank by less than 10% over
+// this many rounds (0: off).  Measured on GB300 at 4 rounds: the 2M x 2M
+// unit-capacity matching 9.7 -> 7.7 ms and R-MAT scale 16 1.26 -> 0.98 ms,
+// but R-MAT scale 20/22, layered networks, GENRMF and 512 x 512 grids lose
+// 5-50% to extra relabels, so it is off by default and wbpr_autotune tries it.
+constexpr int kDefaultPlateau = 0;
+
 // Default of the no-flow-into-t global-relabel trigger (rounds in a row, 0:
 // off).  On R-MAT scale 20/22 and the 2M x 2M bipartite graph it cut 5-18%
 // of the solve, one round a little more than two after the greedy routing;
