@@ -489,6 +489,7 @@ def run_ours(args) -> None:
         if not args.no_extras and world == 1:
             extras["batch"] = batch_record(args.batch_instances, 3, 3)
             extras["adjoint"] = adjoint_record(args.adjoint_grids, 3)
+            extras["matching"] = matching_record(5, 3)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_s_max * 1e3 / args.steps, "higher_is_better": True,
@@ -579,8 +580,11 @@ def config0(args):
           flows_first=flows[:5], flows_pinned=len(pin) >= len(seeds), verified=True, cpu_baseline=cpu)
 
 
-def config2(args):
-    """Unit-capacity bipartite matching, 2M x 2M, Zipf(2.0) left degrees."""
+def matching_record(steps: int, warmup: int, general_steps: int = 3) -> dict:
+    """Config 2: the 2M x 2M unit-capacity matching, solved through
+    wbpr_solve (which takes the matching kernel for this shape), against the
+    general solver on the same handle (matching=-1, autotuned); the matching
+    size checked against the oracle's pin and the device certificate."""
     import wbpr_gb300 as W
 
     from wbpr_gb300 import workloads as WL
@@ -588,25 +592,34 @@ def config2(args):
     g = WL.config2()
     pin = load_pins().get("config2", {}).get("flow")
     with W.DeviceGraph(g, "bcsr") as d:
-        # the library's own tuning search (wbpr_autotune), outside the timing;
-        # unit-capacity matching gains from more frequent global relabels
-        tu, _ = d.autotune("vc", g.s, g.t)
-        kw = {"tile": tu.tile, "gr_alpha": tu.gr_alpha, "heavy_degree": tu.heavy_degree,
-              "bfs_alpha": tu.bfs_alpha, "gr_plateau": tu.gr_plateau}
-        for _ in range(args.warmup):
-            d.solve("vc", g.s, g.t, **kw)
-        r = [d.solve("vc", g.s, g.t, **kw) for _ in range(args.steps)]
+        for _ in range(warmup):
+            d.solve("vc", g.s, g.t)
+        r = [d.solve("vc", g.s, g.t) for _ in range(steps)]
         rep = d.verify()
-    if not rep["ok"] or len({x.flow for x in r}) != 1:
+        gen = [d.solve("vc", g.s, g.t, matching=-1, gr_alpha=0.5, bfs_alpha=4, gr_plateau=4)
+               for _ in range(general_steps + 1)][1:]
+    if not rep["ok"] or rep["label_violations"] or len({x.flow for x in r + gen}) != 1:
         raise AssertionError(f"certificate failed: {rep}")
     if pin is not None and r[0].flow != pin:
         raise AssertionError(f"matching {r[0].flow} != oracle {pin}")
     ms = statistics.median(x.solve_ms for x in r)
-    _line("max-flow MTEPS (bipartite matching, unit capacity)", g.m / ms / 1e3, "MTEPS", True,
-          f"bipartite_L2M_R2M_zipf2.0 (n={g.n}, m={g.m})", steps=args.steps, warmup=args.warmup,
-          solve_ms=ms, gr_ms=r[-1].gr_ms, rounds=r[-1].rounds, matching=r[0].flow, matching_pinned=pin is not None,
-          verified=True,
-          tuning=kw)
+    gms = statistics.median(x.solve_ms for x in gen)
+    last = r[-1]
+    return {"workload": f"bipartite_L2M_R2M_zipf2.0 (n={g.n}, m={g.m})", "kernel": "pr_match",
+            "path": "matching" if last.matching else "general", "solve_ms": ms, "value": g.m / ms / 1e3,
+            "unit": "MTEPS", "launch_ms": last.launch_ms, "rounds": last.rounds,
+            "global_relabels": last.global_relabels, "gr_ms": last.gr_ms, "matching": r[0].flow,
+            "matching_pinned": pin is not None, "verified": True, "general_solver_ms": gms,
+            "speedup_vs_general": gms / ms, "steps": steps}
+
+
+def config2(args):
+    """Unit-capacity bipartite matching, 2M x 2M, Zipf(2.0) left degrees."""
+    rec = matching_record(args.steps, args.warmup)
+    _line("max-flow MTEPS (bipartite matching, unit capacity)", rec["value"], "MTEPS", True, rec["workload"],
+          steps=args.steps, warmup=args.warmup, solve_ms=rec["solve_ms"], gr_ms=rec["gr_ms"], rounds=rec["rounds"],
+          matching=rec["matching"], matching_pinned=rec["matching_pinned"], verified=True, path=rec["path"],
+          general_solver_ms=rec["general_solver_ms"], speedup_vs_general=rec["speedup_vs_general"])
 
 
 def load_pins() -> dict:

@@ -114,7 +114,11 @@ typedef struct wbpr_tuning {
   int32_t gr_plateau;    /* also relabel globally when the active set shrank by   */
                          /* less than 10% over this many rounds, 1..8 (0 or -1 =  */
                          /* never, the default)                                   */
-  int32_t pad1;
+  int32_t matching;      /* BCSR solves: 0 = a terminal pair whose network is a   */
+                         /* unit-capacity bipartite matching network (s -> left,  */
+                         /* left -> right, right -> t, every capacity 1, no other */
+                         /* arc) is solved by the matching kernel; -1 = always    */
+                         /* the general solver                                    */
 } wbpr_tuning;
 
 typedef struct wbpr_result {
@@ -147,7 +151,8 @@ typedef struct wbpr_result {
   uint64_t bytes_gr;       /* global relabels: 12 per arc inspected, 8 per   */
                            /* vertex check, 4 n per relabel                  */
   float deep_ms;           /* deep passes of the push phases (in push_ms)    */
-  int32_t pad0;
+  int32_t matching;        /* 1: solved by the matching kernel (rounds are   */
+                           /* double-push rounds, pushes their claims)       */
   uint64_t deep_arcs_scanned; /* arcs read by the deep passes (in arcs_scanned) */
 } wbpr_result;
 

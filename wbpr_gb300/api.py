@@ -50,7 +50,7 @@ class Tuning(C.Structure):
                 ("max_ms", C.c_double), ("verify", C.c_int32), ("trace", C.c_int32),
                 ("gr_rounds", C.c_int32), ("grid_blocks", C.c_int32), ("gr_stall", C.c_int32),
                 ("barrier_timeout_ns", C.c_int64), ("greedy", C.c_int32), ("bfs_alpha", C.c_int32),
-                ("gr_plateau", C.c_int32), ("pad1", C.c_int32)]
+                ("gr_plateau", C.c_int32), ("matching", C.c_int32)]
 
 
 class Result(C.Structure):
@@ -62,7 +62,7 @@ class Result(C.Structure):
                 ("push_ms", C.c_float), ("bfs_levels", C.c_int32), ("bfs_bottom_up_levels", C.c_int32),
                 ("heavy_visits", C.c_uint64), ("bytes_push", C.c_uint64), ("bytes_deep", C.c_uint64),
                 ("bytes_relabel", C.c_uint64), ("bytes_gr", C.c_uint64), ("deep_ms", C.c_float),
-                ("pad0", C.c_int32), ("deep_arcs_scanned", C.c_uint64)]
+                ("matching", C.c_int32), ("deep_arcs_scanned", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -26,9 +26,9 @@ CHECKED_SOURCES = ["pr_bcsr.cu", "pr_rcsr.cu"]  # the solver kernels
 CLI = os.path.join(OUT, "maxflow")
 
 ARCH = ["-gencode=arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["pr_bcsr.cu", "pr_rcsr.cu", "graph_dev.cu", "noalloc.cu", "batch.cu"]
+CU_SOURCES = ["pr_bcsr.cu", "pr_rcsr.cu", "graph_dev.cu", "noalloc.cu", "batch.cu", "match.cu"]
 CPP_SOURCES = ["host_graph.cpp"]
-HEADERS = ["pr_kernel.cuh", "pr_launch.h", "wbpr_internal.h"]
+HEADERS = ["pr_kernel.cuh", "pr_launch.h", "wbpr_internal.h", "match.h"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter",
              "-ffp-contract=off", "-pthread"]

@@ -13,6 +13,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include "devmem.h"
+#include "match.h"
 #include "pr_launch.h"
 #include "wbpr_internal.h"
 
@@ -164,6 +165,20 @@ struct wbpr_graph {
   double avg_deg = 0;
   Ctl* ctl = nullptr;
   Stats* st = nullptr;
+  // unit-capacity bipartite shape of the terminal pair (mt_s, mt_t), and the
+  // matching kernel's arrays (allocated at the first check)
+  int mt_s = -1, mt_t = -1;
+  bool mt_ok = false;
+  int mt_nl = 0, mt_nl_light = 0, mt_nr = 0;
+  long long mt_larcs = 0;
+  int* mt_lv = nullptr;
+  int* mt_rv = nullptr;
+  unsigned long long* mt_mate = nullptr;
+  int* mt_claim = nullptr;
+  int* mt_cy = nullptr;
+  int* mt_lmin = nullptr;
+  int* mt_cnt = nullptr;  // the shape check's two counts per vertex
+  MCtl* mt_ctl = nullptr;
   int64_t bytes = 0;
   std::vector<void*> allocs;
 };
@@ -501,6 +516,68 @@ __global__ void caps_kernel(const int* ioff, const int* row, const int2* arc, in
 // The input is validated on the way (what the host
 // checks only for its own builders): non-decreasing offsets here, heads in
 // [0, n) by the sort's first histogram, capacities >= 0 by the forward fill.
+// Unit-capacity bipartite shape of (s, t), pass 1: every forward arc of s
+// (capacity 1, head neither s nor t) counts its head into cl, every arc into t
+// (capacity 1, tail neither s nor t; t's reverse slots) counts its tail into cr.
+__global__ void mt_count(const int* row, const int* ioff, const int2* arc, const int2* arx, int s, int t, int* cl,
+                         int* cr, MCtl* mc) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+  bool bad = false;
+  const int bs = row[s], fs = ioff[s + 1] - ioff[s];
+  for (int i = gt; i < fs; i += gs) {
+    const int x = arc[bs + i].x;
+    if (arx[bs + i].y != 1 || x == s || x == t) bad = true;
+    else atomicAdd(cl + x, 1);
+  }
+  const int et = row[t + 1];
+  for (int a = row[t] + (ioff[t + 1] - ioff[t]) + gt; a < et; a += gs) {
+    const int y = arc[a].x;
+    if (arx[arx[a].x].y != 1 || y == s || y == t) bad = true;
+    else atomicAdd(cr + y, 1);
+  }
+  if (bad) atomicOr(&mc->bad, 1);
+}
+// Pass 2, every input arc u -> v: s -> x with x counted once in cl and never
+// in cr; y -> t with y counted once in cr and never in cl; any other arc of
+// capacity 1 from a left vertex (cl 1, cr 0) to a right one (cr 1, cl 0).
+__global__ void mt_check(const int* ioff, const int* row, const int2* arc, const int2* arx, int n, long long m,
+                         int s, int t, const int* cl, const int* cr, MCtl* mc) {
+  const int lane = threadIdx.x & 31;
+  bool bad = false;
+  FOR_TILES(m) {
+    const TileRows tr = tile_rows(ioff, n, base, m);
+    for (int k = 0; k < kTile / 32; ++k) {
+      const long long i = base + k * 32 + lane;
+      if (i >= m) break;
+      const int u = row_search(ioff, i, tr.lo, tr.hi);
+      const int a = row[u] + (int)(i - ioff[u]);
+      const int v = arc[a].x, c = arx[a].y;
+      if (u == s) bad |= cl[v] != 1 || cr[v] != 0;  // capacity and head checked by pass 1
+      else if (v == t) bad |= c != 1 || cr[u] != 1 || cl[u] != 0;
+      else bad |= c != 1 || cl[u] != 1 || cr[u] != 0 || cr[v] != 1 || cl[v] != 0;
+    }
+  }
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&mc->bad, 1);
+}
+// Pass 3: the left vertices (rows of at most `heavy` forward arcs into lv,
+// longer ones into hv) and the right vertices into rv.
+__global__ void mt_list(const int* row, int n, int heavy, const int* cl, const int* cr, int* lv, int* hv, int* rv,
+                        MCtl* mc) {
+  long long arcs = 0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    if (cl[v] == 1) {
+      const int d = row[v + 1] - row[v] - 1;
+      arcs += d;
+      if (d > heavy) append(hv, &mc->nlist[1], v);
+      else append(lv, &mc->nlist[0], v);
+    } else if (cr[v] == 1) {
+      append(rv, &mc->nlist[2], v);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) arcs += __shfl_down_sync(0xffffffffu, arcs, o);
+  if ((threadIdx.x & 31) == 0 && arcs) atomicAdd((unsigned long long*)&mc->larcs, (unsigned long long)arcs);
+}
+
 __global__ void db_check_off(const int* off, int n, unsigned long long* bad) {
   bool b = false;
   for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < n; u += (long long)gridDim.x * blockDim.x)
@@ -1268,6 +1345,7 @@ struct RunCfg {
   int greedy;
   int bfs_alpha;
   int gr_plateau;
+  bool matching;  // the matching kernel may take unit-capacity bipartite networks
   long long max_rounds;
   unsigned long long budget_ns;
   unsigned long long bar_timeout_ns;
@@ -1281,6 +1359,21 @@ struct RunCfg {
   const int* sinks;
   int n_sinks;
 };
+
+// The event-trace buffers (wbpr_tuning.trace), allocated at first use.
+wbpr_status ensure_trace(wbpr_graph* g) {
+  if (g->trace) return WBPR_OK;
+  g->trace_cap = 1 << 14;
+  wbpr_status st = dalloc(g, &g->trace, 6 * (size_t)g->trace_cap);
+  if (st) return st;
+  st = dalloc(g, &g->bt, 4096);
+  if (st) return st;
+  st = dalloc(g, &g->bt2, 8192);
+  if (st) return st;
+  CK(cudaMemset(g->bt, 0, 8 * 4096));
+  CK(cudaMemset(g->bt2, 0, 8 * 8192));
+  return WBPR_OK;
+}
 
 template <class Topo>
 wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch_ms) {
@@ -1315,17 +1408,8 @@ wbpr_status run_kernel(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch
     p.bfs_excl = -1;
   }
   if (rc.trace) {
-    if (!g->trace) {
-      g->trace_cap = 1 << 14;
-      wbpr_status st = dalloc(g, &g->trace, 6 * (size_t)g->trace_cap);
-      if (st) return st;
-      st = dalloc(g, &g->bt, 4096);
-      if (st) return st;
-      st = dalloc(g, &g->bt2, 8192);
-      if (st) return st;
-      CK(cudaMemset(g->bt, 0, 8 * 4096));
-      CK(cudaMemset(g->bt2, 0, 8 * 8192));
-    }
+    wbpr_status st = ensure_trace(g);
+    if (st) return st;
     p.trace = g->trace;
     p.bt = g->bt;
     p.bt2 = g->bt2;
@@ -1365,6 +1449,130 @@ wbpr_status run(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch_ms = n
                                        : run_kernel<TopoB>(g, rc, hs, launch_ms);
 }
 
+// Rows longer than this are discharged by a whole warp in the matching kernel
+// (the left-vertex lists are split by it once, at the shape check).
+constexpr int kMatchHeavy = 32;
+// The matching kernel's global relabel runs when the active set shrank by
+// less than 10% over this many rounds (wbpr_tuning.gr_plateau overrides it):
+// after the first few rounds most active vertices cannot reach t.
+constexpr int kMatchPlateau = 2;
+
+// Is (s, t) of this BCSR16 graph a unit-capacity bipartite matching network
+// (s -> left, left -> right, right -> t, every capacity 1, no other arc)?
+// Checked on the device in three O(n + m) passes and cached per terminal pair
+// (wbpr_graph_set_capacities drops the cache); on success the left and right
+// vertex lists stay on the device for the matching kernel.
+wbpr_status match_detect(wbpr_graph* g, int s, int t, bool* ok) {
+  *ok = false;
+  if (g->layout != WBPR_LAYOUT_BCSR || g->m == 0 || s == t) return WBPR_OK;
+  if (g->mt_s == s && g->mt_t == t) {
+    *ok = g->mt_ok;
+    return WBPR_OK;
+  }
+  wbpr_status st;
+  const size_t n = (size_t)g->n;
+  if (!g->mt_ctl) {
+    if ((st = dalloc(g, &g->mt_mate, n)) || (st = dalloc(g, &g->mt_claim, n)) || (st = dalloc(g, &g->mt_cnt, 2 * n)) || (st = dalloc(g, &g->mt_cy, n)) ||
+        (st = dalloc(g, &g->mt_lmin, n)) ||
+        (st = dalloc(g, &g->mt_lv, n)) || (st = dalloc(g, &g->mt_rv, n)) || (st = dalloc(g, &g->mt_ctl, 1)))
+      return st;
+  }
+  int* cl = g->mt_cnt;
+  int* cr = g->mt_cnt + n;
+  CK(cudaMemsetAsync(cl, 0, 4 * n, g->stream));
+  CK(cudaMemsetAsync(cr, 0, 4 * n, g->stream));
+  CK(cudaMemsetAsync(g->mt_ctl, 0, sizeof(MCtl), g->stream));
+  mt_count<<<g->sms * 4, 256, 0, g->stream>>>(g->row, g->ioff, g->arc, g->arx, s, t, cl, cr, g->mt_ctl);
+  mt_check<<<g->sms * 8, 256, 0, g->stream>>>(g->ioff, g->row, g->arc, g->arx, g->n, g->m, s, t, cl, cr, g->mt_ctl);
+  mt_list<<<g->sms * 4, 256, 0, g->stream>>>(g->row, g->n, kMatchHeavy, cl, cr, g->mt_lv, g->lq[0], g->mt_rv,
+                                            g->mt_ctl);
+  CK(cudaGetLastError());
+  MCtl hc;
+  CK(cudaMemcpyAsync(&hc, g->mt_ctl, sizeof(MCtl), cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  g->mt_s = s;
+  g->mt_t = t;
+  g->mt_ok = hc.bad == 0 && hc.nlist[0] + hc.nlist[1] > 0 && hc.nlist[2] > 0;
+  if (g->mt_ok) {
+    g->mt_nl_light = hc.nlist[0];
+    g->mt_nl = hc.nlist[0] + hc.nlist[1];
+    g->mt_nr = hc.nlist[2];
+    g->mt_larcs = hc.larcs;
+    if (hc.nlist[1])  // the long rows after the short ones
+      CK(cudaMemcpyAsync(g->mt_lv + hc.nlist[0], g->lq[0], 4 * (size_t)hc.nlist[1], cudaMemcpyDeviceToDevice,
+                         g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+  }
+  *ok = g->mt_ok;
+  return WBPR_OK;
+}
+
+// One launch of the matching kernel (match.cu) for the pair (s, t) that
+// match_detect accepted; the residuals were restored before it.
+wbpr_status run_match(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch_ms) {
+  MatchParams p{};
+  topo_of(g, p.g);
+  p.n = g->n;
+  p.s = rc.s;
+  p.t = rc.t;
+  p.nl = g->mt_nl;
+  p.nl_light = g->mt_nl_light;
+  p.nr = g->mt_nr;
+  p.lv = g->mt_lv;
+  p.rv = g->mt_rv;
+  p.left_arcs = g->mt_larcs;
+  p.mate = g->mt_mate;
+  p.claim = g->mt_claim;
+  p.cy = g->mt_cy;
+  p.lmin = g->mt_lmin;
+  p.lab = g->h;
+  p.e = g->e;
+  for (int k = 0; k < 2; ++k) {
+    p.q[k] = g->lq[k];
+    p.hq[k] = g->hq[k];
+    p.fr[k] = g->fr[k];
+  }
+  p.ctl = g->mt_ctl;
+  p.st = g->st;
+  p.heavy_deg = kMatchHeavy;
+  p.bfs_alpha = rc.bfs_alpha > 0 ? rc.bfs_alpha : kBfsAlpha;
+  p.gr_threshold = rc.gr_threshold;
+  p.gr_rounds = rc.gr_rounds;
+  p.gr_plateau = rc.gr_plateau > 0 ? rc.gr_plateau : kMatchPlateau;
+  p.max_rounds = rc.max_rounds;
+  p.budget_ns = rc.budget_ns;
+  p.bar_timeout_ns = rc.bar_timeout_ns ? rc.bar_timeout_ns : kBarrierTimeoutNs;
+  if (rc.trace) {
+    wbpr_status st = ensure_trace(g);
+    if (st) return st;
+    p.trace = g->trace;
+    p.bt = g->bt;
+    p.trace_cap = g->trace_cap;
+  }
+  const int occ = occupancy_match(rc.threads);
+  if (occ <= 0) {
+    g_last_error = "matching kernel does not fit on an SM";
+    return WBPR_ERR_CUDA;
+  }
+  int blocks = g->sms * (rc.blocks_per_sm > 0 ? std::min(occ, rc.blocks_per_sm) : occ);
+  if (rc.grid_blocks > 0) blocks = std::min(blocks, rc.grid_blocks);
+  else blocks = grid_blocks_for((long long)g->n + g->total_deg, g->sms, blocks);
+  CK(cudaMemsetAsync(g->mt_ctl, 0, sizeof(MCtl), g->stream));
+  CK(cudaMemsetAsync(g->st, 0, sizeof(Stats), g->stream));
+  CK(cudaEventRecord(g->ev2, g->stream));
+  CK(launch_match(p, blocks, rc.threads, g->stream));
+  CK(cudaEventRecord(g->ev3, g->stream));
+  g->full_reset = true;  // the matching's residuals are not in the undo log
+  MCtl hc;
+  CK(cudaMemcpyAsync(&hc, g->mt_ctl, sizeof(MCtl), cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaMemcpyAsync(hs, g->st, sizeof(Stats), cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  if (launch_ms) CK(cudaEventElapsedTime(launch_ms, g->ev2, g->ev3));
+  g->trace_n = rc.trace ? hs->trace_n : 0;
+  if (hc.err) return (wbpr_status)hc.err;
+  return WBPR_OK;
+}
+
 void tuning_defaults(wbpr_tuning* t) {
   std::memset(t, 0, sizeof(*t));
   t->gr_alpha = kDefaultGrAlpha;
@@ -1400,6 +1608,8 @@ wbpr_status make_cfg(wbpr_graph* g, int s, int t, wbpr_algo algo, const wbpr_tun
   if (tu->bfs_alpha < 0) return WBPR_ERR_INVALID_ARG;
   rc->bfs_alpha = tu->bfs_alpha;
   if (tu->gr_plateau < -1 || tu->gr_plateau > kMaxPlateau) return WBPR_ERR_INVALID_ARG;
+  if (tu->matching < -1 || tu->matching > 0) return WBPR_ERR_INVALID_ARG;
+  rc->matching = tu->matching == 0;
   rc->gr_plateau = tu->gr_plateau == 0 ? kDefaultPlateau : (tu->gr_plateau < 0 ? 0 : tu->gr_plateau);
   rc->gr_stall = tu->gr_stall == 0 ? default_gr_stall((long long)g->n + g->total_deg)
                                    : (tu->gr_stall < 0 ? 0 : tu->gr_stall);
@@ -1445,6 +1655,22 @@ PhaseBytes phase_bytes(const wbpr_graph* g, const Stats& s) {
   b.relabel = s.relabels * rel_b;
   b.gr = s.bfs_arcs * bfs_arc_b + s.bfs_vertices * bfs_v_b + (uint64_t)s.grs * g->n * 4;
   b.init = (uint64_t)g->n * 12;  // labels, excess, relabel records
+  return b;
+}
+
+// The same for a matching-kernel launch: 8 bytes per arc scanned (the head of
+// the record + its label), 8 per visit (queue entry, row bounds), 20 per
+// claim (mate exchange, label, the claimer's two words), 8 per BFS arc and
+// vertex check, 12 per left and right vertex per global relabel (label, mate
+// or claim), and 8 n + 16 per vertex of the lists to initialise; the push
+// bytes also count the write-back, 48 per matched edge plus its 3 log entries.
+PhaseBytes match_bytes(const wbpr_graph* g, const Stats& s, int64_t flow) {
+  PhaseBytes b;
+  b.push = s.arcs_scanned * 8 + s.vertex_visits * 8 + s.pushes * 20 + (uint64_t)flow * (48 + 12);
+  b.deep = 0;
+  b.relabel = 0;
+  b.gr = s.bfs_arcs * 8 + s.bfs_vertices * 8 + (uint64_t)s.grs * (uint64_t)(g->mt_nl + g->mt_nr) * 12;
+  b.init = (uint64_t)g->n * 8 + (uint64_t)(g->mt_nl + g->mt_nr) * 16;
   return b;
 }
 
@@ -1507,6 +1733,22 @@ wbpr_status wbpr_autotune(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, w
                           float* best_ms) {
   NvtxRange nvtx_("wbpr_autotune");
   if (!g || !best) return WBPR_ERR_INVALID_ARG;
+  {
+    // a unit-capacity bipartite network goes to the matching kernel, which
+    // has none of the knobs below: the defaults, timed
+    wbpr_tuning tu;
+    wbpr_default_tuning(&tu);
+    wbpr_result r0, r1;
+    wbpr_status st = wbpr_solve(g, s, t, algo, &tu, &r0);
+    if (st) return st;
+    if (r0.matching) {
+      if ((st = wbpr_solve(g, s, t, algo, &tu, &r1))) return st;
+      if (r1.flow != r0.flow) return WBPR_ERR_VERIFY;
+      *best = tu;
+      if (best_ms) *best_ms = std::min(r0.solve_ms, r1.solve_ms);
+      return WBPR_OK;
+    }
+  }
   const int tiles_vc[] = {8, 16, 32};
   const int tiles_tc[] = {0};
   const double alphas[] = {0.5, 1.0, 1.5, 3.0};
@@ -1597,6 +1839,7 @@ wbpr_status wbpr_graph_set_capacities(wbpr_graph* g, const int32_t* capacities) 
   caps_kernel<<<g->sms * 8, 256, 0, g->stream>>>(g->ioff, bcsr ? g->row : nullptr, g->arc, g->arx, g->farc, g->fcap,
                                                 dcap, g->n, g->m, 1, incap, chk);
   g->full_reset = true;  // every residual goes back to its new capacity at the next solve
+  g->mt_s = g->mt_t = -1;  // capacities other than 1 may have come
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(g->stream));
   return WBPR_OK;
@@ -1660,6 +1903,8 @@ wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, cons
   rc.mode = kModeFresh;
   rc.bfs_excl = s;
   CK(cudaSetDevice(g->device));
+  bool matched = false;
+  if (rc.matching && (st = match_detect(g, s, t, &matched))) return st;
   CK(cudaEventRecord(g->ev0, g->stream));
   if (g->layout == WBPR_LAYOUT_RCSR) {
     if (g->m) reset_rcsr<<<g->sms * 8, 256, 0, g->stream>>>(g->farc, g->fcb, g->fcap, g->m);
@@ -1669,7 +1914,7 @@ wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, cons
   CK(cudaGetLastError());
   Stats hs;
   float launch_ms = 0;
-  st = run(g, rc, &hs, &launch_ms);
+  st = matched ? run_match(g, rc, &hs, &launch_ms) : run(g, rc, &hs, &launch_ms);
   CK(cudaEventRecord(g->ev1, g->stream));
   CK(cudaEventSynchronize(g->ev1));
   if (st) return st;
@@ -1690,7 +1935,7 @@ wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, cons
     out->rounds = hs.rounds;
     out->global_relabels = hs.grs;
     out->stranded = hs.stranded;
-    const PhaseBytes pb = phase_bytes(g, hs);
+    const PhaseBytes pb = matched ? match_bytes(g, hs, et) : phase_bytes(g, hs);
     out->alg_bytes = pb.total();
     out->bytes_push = pb.push;
     out->bytes_deep = pb.deep;
@@ -1703,6 +1948,7 @@ wbpr_status wbpr_solve(wbpr_graph* g, int32_t s, int32_t t, wbpr_algo algo, cons
     out->bfs_levels = hs.bfs_levels;
     out->bfs_bottom_up_levels = hs.bu_levels;
     out->heavy_visits = hs.heavy_visits;
+    out->matching = matched ? 1 : 0;
   }
   g->s = s;
   g->t = t;

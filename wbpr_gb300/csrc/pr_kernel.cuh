@@ -423,7 +423,9 @@ __device__ __forceinline__ unsigned atom_add_release(unsigned* p, unsigned x) {
 // later reads after every other block's arrival.  Measured on GB300: 2.1 us
 // per barrier at 456 blocks, against 2.4 us with full fences around a
 // relaxed atomic.
-__device__ __forceinline__ bool grid_sync(Ctl* c, unsigned long long timeout_ns) {
+// C is any control block with an `unsigned bar` word and an `int err` word.
+template <class C>
+__device__ __forceinline__ bool grid_sync(C* c, unsigned long long timeout_ns) {
   // Thread 0 reads the error word once and the block takes its answer: a
   // word another block may set at any moment (a timed-out wait) must not send
   // the threads of one block different ways.
