@@ -660,7 +660,7 @@ def batch_record(count: int, steps: int, warmup: int, loop_sample: int = 96, uni
     ms = statistics.median(x[1] for x in runs)
     rec = {"instances": count, "batch_ms": ms, "instances_per_s": count / ms * 1e3,
            "inst_p50_ms": float(np.percentile(ims, 50)), "inst_p99_ms": float(np.percentile(ims, 99)),
-           "tuning": {"tile": best.tile, "block": best.block, "gr_alpha": best.gr_alpha},
+           "tuning": {"tile": best.tile, "block": best.block, "gr_alpha": best.gr_alpha, "batch_cluster": best.batch_cluster},
            "flows_pinned": pinned, "n_total": int(sum(g.n for g in gs)), "m_total": int(sum(g.m for g in gs))}
     if union:
         # the same instances as one disjoint-union graph, all pairs in one solve

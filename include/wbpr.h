@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define WBPR_ABI_VERSION 1
+#define WBPR_ABI_VERSION 2
 
 typedef enum wbpr_status {
   WBPR_OK = 0,
@@ -119,6 +119,10 @@ typedef struct wbpr_tuning {
                          /* left -> right, right -> t, every capacity 1, no other */
                          /* arc) is solved by the matching kernel; -1 = always    */
                          /* the general solver                                    */
+  int32_t pad2;
+  int64_t batch_cluster; /* batches: instances of at least this many units (n +   */
+                         /* residual arcs) run on 8-block thread-block clusters, */
+                         /* the rest one block each (0 = 3 x 2^17, -1 = none)     */
 } wbpr_tuning;
 
 typedef struct wbpr_result {
@@ -372,8 +376,9 @@ int64_t wbpr_batch_device_bytes(const wbpr_batch* b);
 wbpr_status wbpr_batch_solve(wbpr_batch* b, const wbpr_tuning* tuning, int64_t* flows, float* solve_ms);
 /* Per-instance device time (ms) and rounds of the last solve (either may be NULL). */
 wbpr_status wbpr_batch_instance_stats(wbpr_batch* b, float* inst_ms, int32_t* inst_rounds);
-/* Try tile widths, block sizes and global-relabel frequencies on this batch;
- * return the fastest tuning and its time. */
+/* Try tile widths, block sizes and global-relabel frequencies on this batch,
+ * then which instances run on clusters (batch_cluster: none, 2^18 or 2^19
+ * units); return the fastest tuning and its time. */
 wbpr_status wbpr_batch_autotune(wbpr_batch* b, wbpr_tuning* best, float* best_ms);
 
 /* ---- solve without any device allocation --------------------------------- */

@@ -65,3 +65,23 @@ def test_batch_budget_reports_failed_instances():
         assert ei.value.status == 3
         flows, _ = b.solve()
         assert (flows >= 0).all()
+
+
+def test_batch_clusters_exact():
+    """Instances from a size threshold on run on 8-block thread-block
+    clusters (distributed shared-memory control words, cluster barriers):
+    every threshold, tile and block size gives the oracle's flows."""
+    gs = mixed_instances(80, seed=5) + [W.gen_genrmf(12, 10, 1, 10000, 1), W.gen_layered(30, 200, 3, 6, 1, 1000, 2)]
+    expected = np.array([oracle.dinic(g.n, g.off, g.dst, g.cap, g.s, g.t) for g in gs])
+    with W.Batch(gs) as b:
+        for cl in (1, 200, 2000, 20000, -1):
+            for tile, block in ((8, 512), (16, 256), (32, 128)):
+                flows, ms = b.solve(tile=tile, block=block, batch_cluster=cl)
+                assert np.array_equal(flows, expected), (cl, tile, block)
+        ms_i, rounds = b.instance_stats()
+        assert (ms_i > 0).all()
+        with pytest.raises(W.WbprError) as ei:
+            b.solve(max_rounds=1, gr_alpha=1e9, gr_rounds=1 << 20, batch_cluster=1)
+        assert ei.value.status == 3
+        flows, _ = b.solve(batch_cluster=1)
+        assert np.array_equal(flows, expected)

@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol():
     assert set(declared) == set(W.EXPORTED)
     for name in declared:
         assert hasattr(lib, name), name
-    assert lib.wbpr_abi_version() == 1
+    assert lib.wbpr_abi_version() == 2
 
 
 def test_status_strings():

@@ -50,7 +50,8 @@ class Tuning(C.Structure):
                 ("max_ms", C.c_double), ("verify", C.c_int32), ("trace", C.c_int32),
                 ("gr_rounds", C.c_int32), ("grid_blocks", C.c_int32), ("gr_stall", C.c_int32),
                 ("barrier_timeout_ns", C.c_int64), ("greedy", C.c_int32), ("bfs_alpha", C.c_int32),
-                ("gr_plateau", C.c_int32), ("matching", C.c_int32)]
+                ("gr_plateau", C.c_int32), ("matching", C.c_int32),
+                ("pad2", C.c_int32), ("batch_cluster", C.c_int64)]
 
 
 class Result(C.Structure):

@@ -52,13 +52,19 @@ struct wbpr_batch {
   long long* flows = nullptr;
   unsigned long long* inst_ns = nullptr;
   int* inst_rounds = nullptr;
-  int* next = nullptr;  // work-list cursor
+  int* next = nullptr;  // work-list cursors: one-block instances, cluster instances
+  int* next_big = nullptr;
+  std::vector<int64_t> size_sorted;  // instance sizes (n + residual arcs), largest first
+  cudaStream_t side = nullptr;       // second branch of the captured launch
+  cudaEvent_t fork = nullptr, join = nullptr;
   std::vector<void*> allocs;
   // captured launch
   cudaGraphExec_t exec = nullptr;
   int cap_tile = 0, cap_block = 0;
   double cap_alpha = 0;
   int cap_grr = 0;
+  int64_t cap_cluster = -2;
+  int cap_nbig = 0;
   std::vector<long long> host_flows;
 };
 
@@ -97,27 +103,49 @@ struct BlockCtl {
   int qraw_count[2];
   int fcount[2];
   int item;
-  int stop;   // budget exhausted (decided by thread 0, read after a barrier)
+  int stop;   // budget exhausted (decided by the leader, read after a barrier)
   int gr_ok;  // rounds since the last global relabel took >= half its time
+  unsigned long long work;  // scan work since the last global relabel, all blocks of the group
 };
 
-// Block-level BFS from t over residual arcs (top-down, warp per frontier
-// row); unreached vertices of the instance keep label n.
-__device__ void batch_bfs(const Params<TopoB>& p, int vbase, int* fr0, int* fr1, BlockCtl& bc,
-                          BlockAcc& acc) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int v = vbase + (int)threadIdx.x; v < vbase + p.n; v += blockDim.x) p.lab[v] = (v == p.t) ? 0 : p.n;
-  if (threadIdx.x == 0) {
-    fr0[0] = p.t;
-    bc.fcount[0] = 1;
-    bc.fcount[1] = 0;
+// The threads that solve one instance: one block (CS = 1), or a thread-block
+// cluster of CS blocks whose control words live in the shared memory of its
+// first block (distributed shared memory) and whose barrier is the cluster's
+// hardware barrier.  Every branch of the solve is taken on values read from
+// those words after a barrier, so all blocks of a group take the same one.
+template <int CS>
+struct Group {
+  __device__ __forceinline__ int rank() const { return CS == 1 ? 0 : (int)cg::this_cluster().block_rank(); }
+  __device__ __forceinline__ int tid() const { return rank() * blockDim.x + threadIdx.x; }
+  __device__ __forceinline__ int size() const { return CS * blockDim.x; }
+  __device__ __forceinline__ bool leader() const { return tid() == 0; }
+  __device__ __forceinline__ void sync() const {
+    if (CS == 1) __syncthreads();
+    else cg::this_cluster().sync();
   }
-  __syncthreads();
+  __device__ __forceinline__ BlockCtl* ctl(BlockCtl* local) const {
+    return CS == 1 ? local : cg::this_cluster().map_shared_rank(local, 0);
+  }
+};
+
+// Group-level BFS from t over residual arcs (top-down, warp per frontier
+// row); unreached vertices of the instance keep label n.
+template <int CS>
+__device__ void batch_bfs(const Group<CS>& G, const Params<TopoB>& p, int vbase, int* fr0, int* fr1, BlockCtl* bc,
+                          BlockAcc& acc) {
+  const int lane = threadIdx.x & 31, wid = G.tid() >> 5, nw = G.size() >> 5;
+  for (int v = vbase + G.tid(); v < vbase + p.n; v += G.size()) p.lab[v] = (v == p.t) ? 0 : p.n;
+  if (G.leader()) {
+    fr0[0] = p.t;
+    bc->fcount[0] = 1;
+    bc->fcount[1] = 0;
+  }
+  G.sync();
   unsigned long long arcs = 0;
   for (int level = 0;; ++level) {
     int* cur = (level & 1) ? fr1 : fr0;
     int* nxt = (level & 1) ? fr0 : fr1;
-    const int nf = bc.fcount[level & 1];
+    const int nf = ldv(&bc->fcount[level & 1]);
     if (nf == 0) break;
     for (int i = wid; i < nf; i += nw) {
       const int x = __ldcg(cur + i);
@@ -127,37 +155,43 @@ __device__ void batch_bfs(const Params<TopoB>& p, int vbase, int* fr0, int* fr1,
         const int dst = p.g.head(0, a);
         if (dst == p.s || __ldcg(p.lab + dst) != p.n) continue;
         if (p.g.twin_cf(0, a) <= 0) continue;
-        if (atomicCAS(p.lab + dst, p.n, level + 1) == p.n) append(nxt, &bc.fcount[(level + 1) & 1], dst);
+        if (atomicCAS(p.lab + dst, p.n, level + 1) == p.n) append(nxt, &bc->fcount[(level + 1) & 1], dst);
       }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) bc.fcount[level & 1] = 0;
-    __syncthreads();
+    G.sync();
+    if (G.leader()) bc->fcount[level & 1] = 0;
+    G.sync();
   }
   if (arcs) atomicAdd(&acc.bfs_arcs, arcs);
-  // rebuild the active list of the instance
-  if (threadIdx.x == 0) bc.lcount[0] = 0;
-  __syncthreads();
-  for (int v = vbase + (int)threadIdx.x; v < vbase + p.n; v += blockDim.x) {
+  // rebuild the active list of the instance (the work word was last read
+  // before this relabel's first barrier)
+  if (G.leader()) {
+    bc->lcount[0] = 0;
+    bc->work = 0;
+  }
+  G.sync();
+  for (int v = vbase + G.tid(); v < vbase + p.n; v += G.size()) {
     if (v == p.s || v == p.t) continue;
     const int ev = ldv(p.e + v);
     if (ev > 0 && __ldcg(p.lab + v) < p.n) {
       p.esnap[v] = ev;
-      append(p.lq[0], &bc.lcount[0], v);
+      append(p.lq[0], &bc->lcount[0], v);
     }
   }
-  __syncthreads();
+  G.sync();
 }
 
-template <int W>
+template <int W, int CS>
 __global__ void __launch_bounds__(512, 2) pr_batch(BatchParams bp) {
   __shared__ BlockAcc acc;
-  __shared__ BlockCtl bc;
+  __shared__ BlockCtl bc_local;
+  const Group<CS> G;
+  BlockCtl* bc = G.ctl(&bc_local);
   for (;;) {
-    if (threadIdx.x == 0) bc.item = atomicAdd(bp.next, 1);
-    __syncthreads();
-    const int item = bc.item;
-    __syncthreads();
+    if (G.leader()) bc->item = atomicAdd(bp.next, 1);
+    G.sync();
+    const int item = ldv(&bc->item);
+    G.sync();  // nobody reads the item word after this, so every block may leave
     if (item >= bp.count) return;
     const int id = bp.order[item];
     const BatchInst in = bp.inst[id];
@@ -185,20 +219,22 @@ __global__ void __launch_bounds__(512, 2) pr_batch(BatchParams bp) {
       acc.deep = 0;
       acc.fdeg = 0;
       acc.sink = 0;
-      bc.lcount[0] = bc.lcount[1] = 0;
-      bc.qraw_count[0] = bc.qraw_count[1] = 0;
+    }
+    if (G.leader()) {
+      bc->lcount[0] = bc->lcount[1] = 0;
+      bc->qraw_count[0] = bc->qraw_count[1] = 0;
     }
     // reset residuals and state of this instance, then preflow from s
-    for (int a = abeg + (int)threadIdx.x; a < aend; a += blockDim.x) bp.arc[a].y = __ldg(&bp.arx[a].y);
-    for (int v = in.vbase + (int)threadIdx.x; v < in.vbase + in.n; v += blockDim.x) {
+    for (int a = abeg + G.tid(); a < aend; a += G.size()) bp.arc[a].y = __ldg(&bp.arx[a].y);
+    for (int v = in.vbase + G.tid(); v < in.vbase + in.n; v += G.size()) {
       bp.h[v] = 0;
       bp.e[v] = 0;
       bp.rl_min[v] = kNone;
     }
-    __syncthreads();
+    G.sync();
     {
       const int b = __ldg(bp.row + in.s), e = __ldg(bp.row + in.s + 1);
-      for (int a = b + (int)threadIdx.x; a < e; a += blockDim.x) {
+      for (int a = b + G.tid(); a < e; a += G.size()) {
         int dst, cf;
         p.g.load(0, a, dst, cf);
         if (cf > 0 && dst != in.s) {
@@ -207,63 +243,61 @@ __global__ void __launch_bounds__(512, 2) pr_batch(BatchParams bp) {
         }
       }
     }
-    __syncthreads();
+    G.sync();
     const unsigned long long gr_thr =
         (unsigned long long)(bp.gr_alpha * ((double)in.n + (double)(aend - abeg))) + 1;
     int cur = 0, raw = 0, rounds = 0, since = 0;
-    unsigned long long work = 0;
     bool need_gr = true, failed = false;
-    unsigned long long gr_end = 0, gr_len = 0;  // thread 0 only
+    unsigned long long gr_end = 0, gr_len = 0;  // leader only
     for (;;) {
       if (need_gr) {
         const unsigned long long g0 = gtime();
-        batch_bfs(p, in.vbase, fr0, fr1, bc, acc);
-        if (threadIdx.x == 0) {
+        batch_bfs<CS>(G, p, in.vbase, fr0, fr1, bc, acc);
+        if (G.leader()) {
           gr_end = gtime();
           gr_len = gr_end - g0;
+          bc->lcount[1] = 0;
+          bc->qraw_count[0] = bc->qraw_count[1] = 0;
         }
-        if (threadIdx.x == 0) {
-          bc.lcount[1] = 0;
-          bc.qraw_count[0] = bc.qraw_count[1] = 0;
-        }
-        __syncthreads();
+        G.sync();
         cur = 0;
         raw = 0;
         need_gr = false;
-        work = 0;
         since = 0;
       }
-      if (threadIdx.x == 0)
-        bc.stop = (bp.max_rounds > 0 && rounds >= bp.max_rounds) || gtime() - t_start > bp.budget_ns;
-      __syncthreads();
-      const int nL = bc.lcount[cur];
+      if (G.leader())
+        bc->stop = (bp.max_rounds > 0 && rounds >= bp.max_rounds) || gtime() - t_start > bp.budget_ns;
+      G.sync();
+      const int nL = ldv(&bc->lcount[cur]);
       if (nL == 0) break;
-      if (bc.stop) {
+      if (ldv(&bc->stop)) {
         failed = true;
         break;
       }
       // push phase: tiles over the active list
       const unsigned long long w0 = acc.scanned + acc.visits;
+      // the other raw counter was last read in the previous round's relabel
+      // phase, before the barrier that closed it, and is next written in the
+      // next round
+      if (G.leader()) bc->qraw_count[raw ^ 1] = 0;
       {
-        const int ntiles = blockDim.x / W, tile = threadIdx.x / W;
-        int* rawcnt = raw ? &bc.qraw_count[1] : &bc.qraw_count[0];
+        const int ntiles = G.size() / W, tile = G.tid() / W;
+        int* rawcnt = &bc->qraw_count[raw];
         const int* lq = cur ? p.lq[1] : p.lq[0];
         for (int i = tile; i < nL; i += ntiles) tile_discharge<TopoB, W, 4>(p, __ldcg(lq + i), 0x7fffffff, rawcnt, acc);
       }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        if (acc.sink) {
-          atomicAdd(bp.e + in.t, acc.sink);
-          acc.sink = 0;
-        }
-        bc.lcount[cur ^ 1] = 0;
+      G.sync();
+      if (threadIdx.x == 0 && acc.sink) {
+        atomicAdd(bp.e + in.t, acc.sink);
+        acc.sink = 0;
       }
-      __syncthreads();
+      if (G.leader()) bc->lcount[cur ^ 1] = 0;
+      G.sync();
       // relabel phase: threads over the raw next list
       {
-        const int nq = bc.qraw_count[raw];
+        const int nq = ldv(&bc->qraw_count[raw]);
         unsigned long long rl = 0;
-        for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+        for (int i = G.tid(); i < nq; i += G.size()) {
           const int u = __ldcg(p.qraw + i);
           int m = __ldcg(p.rl_min + u);
           int hu = __ldcg(p.lab + u);
@@ -280,32 +314,31 @@ __global__ void __launch_bounds__(512, 2) pr_batch(BatchParams bp) {
           }
           if (eu > 0 && hu < p.n) {
             p.esnap[u] = eu;
-            if (cur) append(p.lq[0], &bc.lcount[0], u);
-            else append(p.lq[1], &bc.lcount[1], u);
+            if (cur) append(p.lq[0], &bc->lcount[0], u);
+            else append(p.lq[1], &bc->lcount[1], u);
           }
         }
         if (rl) atomicAdd(&acc.relabels, rl);
       }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        bc.qraw_count[raw] = 0;
-        bc.gr_ok = 2 * (gtime() - gr_end) >= gr_len;
-      }
-      work += acc.scanned + acc.visits - w0;
-      __syncthreads();
+      __syncthreads();  // every thread's scan work is in this block's acc
+      if (threadIdx.x == 0) atomicAdd(&bc->work, acc.scanned + acc.visits - w0);
+      if (G.leader()) bc->gr_ok = 2 * (gtime() - gr_end) >= gr_len;
+      G.sync();
       ++rounds;
       ++since;
       cur ^= 1;
       raw ^= 1;
-      // relabel triggers balanced against relabel time, as in the one-instance solver
-      if ((work > gr_thr || since >= bp.gr_rounds) && bc.gr_ok) need_gr = true;
+      // relabel triggers balanced against relabel time, as in the one-instance
+      // solver; the work word and gr_ok are final at the barrier and are next
+      // written after at least two more barriers
+      if ((ldv64u(&bc->work) > gr_thr || since >= bp.gr_rounds) && ldv(&bc->gr_ok)) need_gr = true;
     }
-    if (threadIdx.x == 0) {
+    if (G.leader()) {
       bp.flows[id] = failed ? -1 : (long long)ldv(bp.e + in.t);
       bp.inst_ns[id] = gtime() - t_start;
       bp.inst_rounds[id] = rounds;
     }
-    __syncthreads();
+    G.sync();
   }
 }
 
@@ -336,6 +369,9 @@ void batch_release(wbpr_batch* b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
+  if (b->side) cudaStreamDestroy(b->side);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -349,31 +385,73 @@ void batch_release(wbpr_batch* b) {
     }                                                                             \
   } while (0)
 
-const void* kernel_for(int tile) {
+// Blocks per cluster of the instances that get one (the portable maximum),
+// and the default size from which an instance gets one.
+constexpr int kBatchCluster = 8;
+constexpr int64_t kBatchClusterUnits = 3 << 17;
+
+const void* kernel_for(int tile, bool cluster) {
   switch (tile) {
-    case 8: return (const void*)pr_batch<8>;
-    case 16: return (const void*)pr_batch<16>;
-    case 32: return (const void*)pr_batch<32>;
+    case 8: return cluster ? (const void*)pr_batch<8, kBatchCluster> : (const void*)pr_batch<8, 1>;
+    case 16: return cluster ? (const void*)pr_batch<16, kBatchCluster> : (const void*)pr_batch<16, 1>;
+    case 32: return cluster ? (const void*)pr_batch<32, kBatchCluster> : (const void*)pr_batch<32, 1>;
   }
   return nullptr;
 }
 
+// Capture the batch launch as a CUDA graph: the instances of at least
+// `cluster_units` units (a prefix of the largest-first order) on a second
+// branch, one 8-block cluster each, claimed from their own work list by as
+// many clusters as fit at once; the rest one block each, taking the SMs the
+// clusters leave and then the ones they give back as their list drains.  The
+// largest instances set the batch's makespan (one of 64k vertices takes
+// 440 ms on a block, ~2,800 rounds; 130 ms on a cluster), so they are the
+// ones that get more threads.  Measured on the 4,096 instances of config 3
+// (block 512, tile 8): 434 ms with no clusters; from 2^19, 3 x 2^17, 2^18
+// and 3 x 2^16 units 357, 269, 319 and 368 ms (p99 per instance 180, 150,
+// 114 and 94 ms); half the clusters instead of all of them: 352, 273, 363
+// and 476 ms.
 wbpr_status capture(wbpr_batch* b, int tile, int block, double alpha, int grr, long long max_rounds,
-                    double max_ms) {
-  if (b->exec && b->cap_tile == tile && b->cap_block == block && b->cap_alpha == alpha && b->cap_grr == grr)
+                    double max_ms, int64_t cluster_units) {
+  if (b->exec && b->cap_tile == tile && b->cap_block == block && b->cap_alpha == alpha && b->cap_grr == grr &&
+      b->cap_cluster == cluster_units)
     return WBPR_OK;
   if (b->exec) {
     cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
   }
-  const void* fn = kernel_for(tile);
+  int nbig = 0;
+  if (cluster_units >= 0)
+    while (nbig < b->count && b->size_sorted[(size_t)nbig] >= cluster_units) ++nbig;
+  const void* fn = kernel_for(tile, false);
   int occ = 0;
   BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, block, 0));
   if (occ <= 0) {
     wbpr::set_last_error("batch kernel does not fit on an SM");
     return WBPR_ERR_CUDA;
   }
-  const int grid = std::min<int64_t>((int64_t)b->sms * occ, std::max(1, b->count));
+  const int grid = std::min<int64_t>((int64_t)b->sms * occ, std::max(1, b->count - nbig));
+  cudaLaunchConfig_t big{};
+  cudaLaunchAttribute big_attr[1];
+  const void* fnb = kernel_for(tile, true);
+  if (nbig > 0) {
+    big.blockDim = dim3(block);
+    big.stream = b->stream;
+    big_attr[0].id = cudaLaunchAttributeClusterDimension;
+    big_attr[0].val.clusterDim.x = kBatchCluster;
+    big_attr[0].val.clusterDim.y = 1;
+    big_attr[0].val.clusterDim.z = 1;
+    big.attrs = big_attr;
+    big.numAttrs = 1;
+    big.gridDim = dim3(kBatchCluster * 1024);  // for the occupancy query only
+    int clusters = 0;
+    BCK(cudaOccupancyMaxActiveClusters(&clusters, fnb, &big));
+    if (clusters <= 0) {
+      wbpr::set_last_error("batch cluster kernel does not fit");
+      return WBPR_ERR_CUDA;
+    }
+    big.gridDim = dim3(kBatchCluster * std::min(nbig, clusters));
+  }
   BatchParams bp;
   std::memset(&bp, 0, sizeof(bp));
   bp.row = b->row;
@@ -400,11 +478,25 @@ wbpr_status capture(wbpr_batch* b, int tile, int block, double alpha, int grr, l
   bp.gr_rounds = grr;
   bp.max_rounds = (int)std::min<long long>(max_rounds, 1 << 30);
   bp.budget_ns = (unsigned long long)(max_ms * 1e6);
+  BatchParams bpb = bp;  // the cluster branch: the first nbig instances of the order
+  bpb.count = nbig;
+  bpb.next = b->next_big;
+  bp.order = b->order + nbig;
+  bp.count = b->count - nbig;
   cudaGraph_t graph = nullptr;
   BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-  cudaMemsetAsync(b->next, 0, sizeof(int), b->stream);
+  cudaMemsetAsync(b->next, 0, 2 * sizeof(int), b->stream);  // next and next_big
+  if (nbig > 0) {
+    cudaEventRecord(b->fork, b->stream);
+    cudaStreamWaitEvent(b->side, b->fork, 0);
+    big.stream = b->side;
+    void* bargs[] = {&bpb};
+    cudaLaunchKernelExC(&big, fnb, bargs);
+    cudaEventRecord(b->join, b->side);
+  }
   void* args[] = {&bp};
-  cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, b->stream);
+  if (bp.count > 0) cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, b->stream);
+  if (nbig > 0) cudaStreamWaitEvent(b->stream, b->join, 0);
   BCK(cudaStreamEndCapture(b->stream, &graph));
   cudaError_t e = cudaGraphInstantiate(&b->exec, graph, 0);
   cudaGraphDestroy(graph);
@@ -413,6 +505,8 @@ wbpr_status capture(wbpr_batch* b, int tile, int block, double alpha, int grr, l
   b->cap_block = block;
   b->cap_alpha = alpha;
   b->cap_grr = grr;
+  b->cap_cluster = cluster_units;
+  b->cap_nbig = nbig;
   return WBPR_OK;
 }
 
@@ -471,6 +565,9 @@ wbpr_status wbpr_batch_create(const wbpr_csr* graphs, int32_t count, wbpr_batch*
   TRYBC(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   TRYBC(cudaEventCreate(&b->ev0));
   TRYBC(cudaEventCreate(&b->ev1));
+  TRYBC(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+  TRYBC(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  TRYBC(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
   // concatenate the instances' BCSR16 rows with global ids
   std::vector<int32_t> row((size_t)tn + 1);
   std::vector<int32_t> arc(2 * (size_t)tm), arx(2 * (size_t)tm);
@@ -498,6 +595,8 @@ wbpr_status wbpr_batch_create(const wbpr_csr* graphs, int32_t count, wbpr_batch*
   std::vector<int32_t> order((size_t)count);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return size[a] > size[c]; });
+  b->size_sorted.resize((size_t)count);
+  for (int i = 0; i < count; ++i) b->size_sorted[(size_t)i] = size[(size_t)order[(size_t)i]];
   TRYB(balloc(b, &b->row, (size_t)tn + 1));
   TRYB(balloc(b, &b->arc, (size_t)tm));
   TRYB(balloc(b, &b->arx, (size_t)tm));
@@ -516,7 +615,8 @@ wbpr_status wbpr_batch_create(const wbpr_csr* graphs, int32_t count, wbpr_batch*
   TRYB(balloc(b, &b->flows, (size_t)count));
   TRYB(balloc(b, &b->inst_ns, (size_t)count));
   TRYB(balloc(b, &b->inst_rounds, (size_t)count));
-  TRYB(balloc(b, &b->next, 1));
+  TRYB(balloc(b, &b->next, 2));
+  b->next_big = b->next + 1;
   b->host_flows.resize((size_t)count);
 #undef TRYB
 #undef TRYBC
@@ -549,7 +649,9 @@ wbpr_status wbpr_batch_solve(wbpr_batch* b, const wbpr_tuning* tu, int64_t* flow
   const int grr = tu->gr_rounds > 0 ? tu->gr_rounds : 48;
   const double max_ms = tu->max_ms > 0 ? tu->max_ms : 120000.0;
   BCK(cudaSetDevice(b->device));
-  wbpr_status st = capture(b, tile, block, alpha, grr, tu->max_rounds, max_ms);
+  if (tu->batch_cluster < -1) return WBPR_ERR_INVALID_ARG;
+  const int64_t cl = tu->batch_cluster == 0 ? kBatchClusterUnits : tu->batch_cluster;
+  wbpr_status st = capture(b, tile, block, alpha, grr, tu->max_rounds, max_ms, cl);
   if (st) return st;
   BCK(cudaEventRecord(b->ev0, b->stream));
   BCK(cudaGraphLaunch(b->exec, b->stream));
@@ -609,6 +711,24 @@ wbpr_status wbpr_batch_autotune(wbpr_batch* b, wbpr_tuning* best, float* best_ms
           bt = t;
         }
       }
+  // then, on the best of those, which instances get clusters: none, or
+  // from 2^18 or 2^19 units instead of 3 x 2^17
+  const int64_t cls[] = {-1, 1 << 18, 1 << 19};
+  if (bms < 1e29f)
+    for (int64_t c : cls) {
+      wbpr_tuning t = bt;
+      t.batch_cluster = c;
+      float ms = 0;
+      wbpr_status st = wbpr_batch_solve(b, &t, nullptr, &ms);
+      if (st == WBPR_ERR_NO_CONVERGENCE) continue;
+      if (st) return st;
+      st = wbpr_batch_solve(b, &t, nullptr, &ms);
+      if (st) continue;
+      if (ms < bms) {
+        bms = ms;
+        bt = t;
+      }
+    }
   *best = bt;
   if (best_ms) *best_ms = bms;
   return bms < 1e29f ? WBPR_OK : WBPR_ERR_NO_CONVERGENCE;
