@@ -609,6 +609,7 @@ def matching_record(steps: int, warmup: int, general_steps: int = 3) -> dict:
             "path": "matching" if last.matching else "general", "solve_ms": ms, "value": g.m / ms / 1e3,
             "unit": "MTEPS", "launch_ms": last.launch_ms, "rounds": last.rounds,
             "global_relabels": last.global_relabels, "gr_ms": last.gr_ms, "matching": r[0].flow,
+            "alg_bytes_per_launch": last.alg_bytes, "achieved_gbs": last.alg_bytes / 1e9 / (last.launch_ms * 1e-3),
             "matching_pinned": pin is not None, "verified": True, "general_solver_ms": gms,
             "speedup_vs_general": gms / ms, "steps": steps}
 
