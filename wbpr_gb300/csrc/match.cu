@@ -170,6 +170,54 @@ __device__ __forceinline__ void discharge_warp(const MatchParams& p, int x, int 
   }
 }
 
+// Discharge of active left vertex x (row [b, b + d), early-exit bound) by
+// its own thread, given the least key and word over its first four arcs:
+// the rest of the row four arcs at a time unless the bound is already met,
+// then the compare-and-swap, rescanning after a lost race.
+__device__ __forceinline__ void discharge_thread(const MatchParams& p, int x, int b, int d, int bound,
+                                                 unsigned long long best, unsigned long long bw, int nb, int* qc,
+                                                 int* hc, MAcc& acc) {
+  ++acc.visits;
+  int from = 4;  // arcs already scanned into best
+  for (int tries = 0;; ++tries) {
+    for (int k0 = from; k0 < d && (int)(best >> 32) > bound; k0 += 4) {
+      int y[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) y[j] = k0 + j < d ? __ldg(&p.g.arc[b + k0 + j].x) : -1;
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (y[j] >= 0) {
+          ++acc.scanned;
+          const unsigned long long w = __ldcg(p.mate + y[j]);
+          const unsigned long long key = ((unsigned long long)(unsigned)wlab(w) << 32) | (unsigned)(k0 + j);
+          if (key < best) {
+            best = key;
+            bw = w;
+          }
+        }
+    }
+    const int ml = (int)(best >> 32);
+    if (best == ~0ull || ml >= p.n) {  // cannot reach t
+      p.lab[x] = p.n;
+      return;
+    }
+    int ev;
+    if (take(p, x, b + (int)(unsigned)best, bw, ev)) {
+      ++acc.claims;
+      if (ev >= 0) file_left(p, ev, nb, qc, hc);
+      return;
+    }
+    if (tries == kRetry) {
+      p.lab[x] = ml + 1;  // at most 1 + its least label now
+      file_left(p, x, nb, qc, hc);
+      return;
+    }
+    bound = ml;  // the label just lost to can only have risen
+    best = ~0ull;
+    from = 0;
+  }
+}
+
 // One round: every active left vertex finds its first arc of least label and
 // pushes over it.  A scan stops early at the least label the vertex saw last
 // time (labels never fall between relabels).  Evicted mates, and vertices
@@ -189,49 +237,47 @@ __device__ void match_round(const MatchParams& p, const int* L, int nL, const in
     return;
   }
   for (int i = gw; i < nH; i += nw) discharge_warp(p, __ldcg(H + i), nb, qc, hc, acc);
-  // short rows: a thread each, 4 arcs in flight
-  for (int i = gt; i < nL; i += gs) {
-    const int x = __ldcg(L + i);
-    int b;
-    const int d = left_row(p, x, b);
-    int bound = max(__ldcg(p.lmin + x), 1);
-    ++acc.visits;
-    for (int tries = 0;; ++tries) {
+  // short rows: a thread each, two rows at a time (their first four arcs
+  // and the heads' mate words in flight together), then each row on its own
+  for (int i0 = gt; i0 < nL; i0 += 2 * gs) {
+    int x[2], b[2], d[2], bound[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) x[q] = i0 + q * gs < nL ? __ldcg(L + i0 + q * gs) : -1;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      d[q] = 0;
+      b[q] = 0;
+      bound[q] = 1;
+      if (x[q] >= 0) {
+        d[q] = left_row(p, x[q], b[q]);
+        bound[q] = max(__ldcg(p.lmin + x[q]), 1);
+      }
+    }
+    int y[2][4];
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) y[q][j] = j < d[q] ? __ldg(&p.g.arc[b[q] + j].x) : -1;
+    unsigned long long w[2][4];
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) w[q][j] = y[q][j] >= 0 ? __ldcg(p.mate + y[q][j]) : ~0ull;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (x[q] < 0) continue;
       unsigned long long best = ~0ull, bw = 0;
-      for (int k0 = 0; k0 < d; k0 += 4) {
-        int y[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) y[j] = k0 + j < d ? __ldg(&p.g.arc[b + k0 + j].x) : -1;
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-          if (y[j] >= 0) {
-            ++acc.scanned;
-            const unsigned long long w = __ldcg(p.mate + y[j]);
-            const unsigned long long key = ((unsigned long long)(unsigned)wlab(w) << 32) | (unsigned)(k0 + j);
-            if (key < best) {
-              best = key;
-              bw = w;
-            }
+      for (int j = 0; j < 4; ++j)
+        if (y[q][j] >= 0) {
+          ++acc.scanned;
+          const unsigned long long key = ((unsigned long long)(unsigned)wlab(w[q][j]) << 32) | (unsigned)j;
+          if (key < best) {
+            best = key;
+            bw = w[q][j];
           }
-        if ((int)(best >> 32) <= bound) break;
-      }
-      const int ml = (int)(best >> 32);
-      if (best == ~0ull || ml >= p.n) {  // cannot reach t
-        p.lab[x] = p.n;
-        break;
-      }
-      int ev;
-      if (take(p, x, b + (int)(unsigned)best, bw, ev)) {
-        ++acc.claims;
-        if (ev >= 0) file_left(p, ev, nb, qc, hc);
-        break;
-      }
-      if (tries == kRetry) {
-        p.lab[x] = ml + 1;  // at most 1 + its least label now
-        file_left(p, x, nb, qc, hc);
-        break;
-      }
-      bound = ml;  // the label just lost to can only have risen
+        }
+      discharge_thread(p, x[q], b[q], d[q], bound[q], best, bw, nb, qc, hc, acc);
     }
   }
 }
@@ -252,6 +298,28 @@ __device__ __forceinline__ void visit_left(const MatchParams& p, int x, int k, i
     else count_one(&c->fn[(li + 1) % 3]);
   } else {
     file_left(p, x, qb, &c->gq[0], &c->gq[1]);
+  }
+}
+
+// Bottom-up check of unlabelled left vertex x at level k, given whether its
+// first four arcs hit: the rest of its row four arcs at a time until a
+// neighbour labelled k is found; then x is labelled k + 1.
+__device__ __forceinline__ void bu_finish(const MatchParams& p, int x, int b, int d, bool hit, int k, int li,
+                                          int qb, long long& seen, long long& fdeg, MAcc& acc) {
+  for (int k0 = 4; k0 < d && !hit; k0 += 4) {
+    int y[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) y[j] = k0 + j < d ? __ldg(&p.g.arc[b + k0 + j].x) : -1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (y[j] >= 0) {
+        ++acc.bfs_arcs;
+        hit |= wlab(__ldcg(p.mate + y[j])) == k;
+      }
+  }
+  if (hit) {
+    p.lab[x] = k + 1;
+    visit_left(p, x, k, li, false, qb, seen, fdeg);
   }
 }
 
@@ -417,28 +485,41 @@ __device__ bool match_gr(const MatchParams& p, int qb, MAcc& acc, int& levels, i
           visit_left(p, x, k, li, false, qb, seen, nfd);
         }
       }
-      for (int i = gt; i < p.nl_light; i += gs) {  // short rows: a thread each
-        const int x = __ldg(p.lv + i);
-        if (__ldcg(p.lab + x) != n) continue;
-        ++acc.bfs_vertices;
-        int b;
-        const int d = left_row(p, x, b);
-        bool hit = false;
-        for (int k0 = 0; k0 < d && !hit; k0 += 4) {
-          int y[4];
+      // short rows: a thread each, two at a time (labels, rows and the
+      // first four heads' words of both in flight), then each on its own
+      for (int i0 = gt; i0 < p.nl_light; i0 += 2 * gs) {
+        int x[2], b[2], d[2];
+        bool open[2];
 #pragma unroll
-          for (int j = 0; j < 4; ++j) y[j] = k0 + j < d ? __ldg(&p.g.arc[b + k0 + j].x) : -1;
+        for (int q = 0; q < 2; ++q) x[q] = i0 + q * gs < p.nl_light ? __ldg(p.lv + i0 + q * gs) : -1;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) open[q] = x[q] >= 0 && __ldcg(p.lab + x[q]) == n;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          b[q] = 0;
+          d[q] = 0;
+          if (open[q]) {
+            ++acc.bfs_vertices;
+            d[q] = left_row(p, x[q], b[q]);
+          }
+        }
+        int y[2][4];
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) y[q][j] = j < d[q] ? __ldg(&p.g.arc[b[q] + j].x) : -1;
+        bool hit[2] = {false, false};
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
 #pragma unroll
           for (int j = 0; j < 4; ++j)
-            if (y[j] >= 0) {
+            if (y[q][j] >= 0) {
               ++acc.bfs_arcs;
-              hit |= wlab(__ldcg(p.mate + y[j])) == k;
+              hit[q] |= wlab(__ldcg(p.mate + y[q][j])) == k;
             }
-        }
-        if (hit) {
-          p.lab[x] = k + 1;
-          visit_left(p, x, k, li, false, qb, seen, nfd);
-        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
+          if (open[q]) bu_finish(p, x[q], b[q], d[q], hit[q], k, li, qb, seen, nfd, acc);
       }
     }
     add_block(&c->seen[(li + 1) % 3], seen);
