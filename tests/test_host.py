@@ -441,3 +441,32 @@ def test_snap_reader_edges(tmp_path):
     p.write_text("0 1")
     g = W.read_snap_txt(str(p))
     assert g.n == 2 and list(g.off) == [0, 1, 1] and list(g.dst) == [1]
+
+
+def test_python_structs_match_the_header(tmp_path):
+    """The ctypes mirrors of wbpr_tuning, wbpr_result and wbpr_verify_report
+    (wbpr_gb300/api.py) have the C header's size and field offsets."""
+    import ctypes as C
+    from wbpr_gb300 import api
+    mirrors = {"wbpr_tuning": api.Tuning, "wbpr_result": api.Result, "wbpr_verify_report": api.VerifyReport}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "wbpr.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {}
+    for ln in out:
+        if ln:
+            a, b, v = ln.split()
+            got[(a, b)] = int(v)
+    for cname, py in mirrors.items():
+        assert got[(cname, "sizeof")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)

@@ -406,7 +406,8 @@ const void* kernel_for(int tile, bool cluster) {
 // clusters leave and then the ones they give back as their list drains.  The
 // largest instances set the batch's makespan (one of 64k vertices takes
 // 440 ms on a block, ~2,800 rounds; 130 ms on a cluster), so they are the
-// ones that get more threads.  Measured on the 4,096 instances of config 3
+// ones that get more threads.  Measured on 4,096 uneven instances (half
+// GENRMF, a and b log-uniform in [4, 32] x [4, 64], half layered networks)
 // (block 512, tile 8): 434 ms with no clusters; from 2^19, 3 x 2^17, 2^18
 // and 3 x 2^16 units 357, 269, 319 and 368 ms (p99 per instance 180, 150,
 // 114 and 94 ms); half the clusters instead of all of them: 352, 273, 363

@@ -1768,10 +1768,14 @@ __device__ __forceinline__ void clear_log(const TopoB& g, int gt) {
 __device__ __forceinline__ void clear_log(const TopoR&, int) {}
 
 // ---------------------------------------------------------------------------
-// Resident blocks per SM the register allocation is sized for (80 registers
-// a thread at 3 blocks of 256 threads).
+// Resident blocks per SM the register allocation is sized for: 4 blocks of
+// 256 threads, 64 registers a thread (a few hundred bytes spilled).  Against
+// 3 blocks at 80 registers, measured on GB300: R-MAT scale 22 3.97 -> 3.71 ms
+// (the global relabels' latency-bound levels gain most), the 2M x 2M matching
+// on this solver 9.70 -> 9.38 ms, 512 x 512 grids, layered networks and
+// GENRMF within noise.
 #ifndef WBPR_PR_MIN_BLOCKS
-#define WBPR_PR_MIN_BLOCKS 3
+#define WBPR_PR_MIN_BLOCKS 4
 #endif
 
 template <class Topo, int W>
