@@ -73,6 +73,7 @@ struct Ctl {
   long long fdeg[3];
   alignas(128) unsigned long long dpack;  // deep list of the round: (entries << 32) | chunk items
   alignas(128) int bu_found[3];  // vertices labelled by a bottom-up level, by level % 3
+  alignas(128) int bu_med[3];    // medium-row batches a bottom-up level has handed out, by level % 3
   int mcount;       // materialised frontier: short rows
   int glong;        // greedy routing: walkers left for the warp stage
   alignas(128) int glong_next;  //   and the claim counter of that stage
@@ -1211,7 +1212,13 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
     const int sub = lane >> 3, sl = lane & 7;
     const unsigned smask = 0xffu << (sub * 8);
     const int B = p.n_medium >= 64 * nwarps ? 32 : 8;
-    for (int base = gw * B; base < p.n_medium; base += nwarps * B) {
+    // batches are claimed, not dealt: rows of one batch are neighbours in
+    // vertex order, and R-MAT puts its longer rows together, so a static deal
+    // left some warps many long unlabelled rows (the slowest block of the
+    // level's medium part took 4x the fastest)
+    int* next = &c->bu_med[level % 3];
+    for (int base = gw * B;;) {
+      if (base >= p.n_medium) break;
       const int i = base + lane;
       int x = -1;
       if (lane < B && i < p.n_medium) {
@@ -1297,6 +1304,10 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
           fdeg += (unsigned long long)q.deg;
         }
       }
+      // the first batch of every warp is its own, the rest are claimed
+      int nb = 0;
+      if (lane == 0) nb = nwarps * B + atomicAdd(next, B);
+      base = __shfl_sync(0xffffffffu, nb, 0);
     }
   }
   if (p.trace) {
@@ -1413,6 +1424,7 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
     c->fdeg[0] = d;
     c->fdeg[1] = c->fdeg[2] = 0;
     c->bu_found[0] = c->bu_found[1] = c->bu_found[2] = 0;
+    c->bu_med[0] = c->bu_med[1] = c->bu_med[2] = 0;
     c->mcount = c->mhcount = 0;
     if (queues) {
       c->lcount[cur] = 0;
@@ -1470,6 +1482,7 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
       c->fhcount[fr] = 0;
       c->fdeg[fr] = 0;
       c->bu_found[fn] = 0;
+      c->bu_med[fn] = 0;
       if (!mat) c->mcount = c->mhcount = 0;
       atomicAdd(&p.st->bfs_levels, 1);
       if (bu) atomicAdd(&p.st->bu_levels, 1);
