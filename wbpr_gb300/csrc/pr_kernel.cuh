@@ -1706,7 +1706,7 @@ __device__ __forceinline__ void two_hop_short(const Params<TopoB>& p, BlockAcc& 
 }
 
 // Stage 2: a warp per long walker over arcs kGreedyShort .. kGreedyArcs of
-// x's row, 32 at a time.  The lanes' shares of the excess left follow arc
+// x's row, 128 at a time.  The lanes' shares of the excess left follow arc
 // order by a saturating prefix sum (each capped at what the arc and its
 // y->t arc hold when read), and all lanes route their shares together.
 __device__ __forceinline__ void two_hop_long(const Params<TopoB>& p, BlockAcc& acc) {
@@ -1727,23 +1727,40 @@ __device__ __forceinline__ void two_hop_long(const Params<TopoB>& p, BlockAcc& a
     int xb, xe;
     p.g.seg(x, 0, xb, xe);
     const int xend = min(xe, xb + kGreedyArcs);
-    for (int a0 = xb + kGreedyShort; a0 < xend && budget > 0; a0 += 32) {
-      const int a = a0 + lane;
-      int y = -1, cf = 0, yt = -1, room = 0;
-      if (a < xend) {
-        p.g.load(0, a, y, cf);
-        if (lane == 0) scanned += (unsigned long long)min(32, xend - a0);
+    // 128 arcs a step, four consecutive ones per lane: a walk is at most
+    // eight dependent steps instead of 31
+    for (int a0 = xb + kGreedyShort; a0 < xend && budget > 0; a0 += 128) {
+      int y[4], cf[4], yt[4], room[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int a = a0 + 4 * lane + k;
+        y[k] = -1;
+        cf[k] = 0;
+        if (a < xend) p.g.load(0, a, y[k], cf[k]);
       }
-      if (cf > 0 && y != p.s) {
-        if (y == p.t) {
-          room = cf;
-        } else {
-          yt = __ldcg(p.esnap + y);
-          if (yt >= 0) room = min(cf, ldv(&p.g.arc[yt].y));
+      if (lane == 0) scanned += (unsigned long long)min(128, xend - a0);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        yt[k] = -1;
+        if (cf[k] > 0 && y[k] != p.s && y[k] != p.t && y[k] >= 0) yt[k] = __ldcg(p.esnap + y[k]);
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        room[k] = 0;
+        if (cf[k] > 0 && y[k] != p.s && y[k] >= 0) {
+          if (y[k] == p.t) room[k] = cf[k];
+          else if (yt[k] >= 0) room[k] = min(cf[k], ldv(&p.g.arc[yt[k]].y));
         }
       }
-      unsigned incl = room > 0 ? (unsigned)room : 0u;
-      if (incl > (unsigned)budget) incl = (unsigned)budget;
+      // saturating prefix of the rooms in arc order: the lane's own four,
+      // then over the lanes
+      unsigned own = 0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        own += room[k] > 0 ? (unsigned)room[k] : 0u;
+        if (own > (unsigned)budget) own = (unsigned)budget;
+      }
+      unsigned incl = own;
 #pragma unroll
       for (int d = 1; d < 32; d <<= 1) {
         const unsigned v = __shfl_up_sync(0xffffffffu, incl, d);
@@ -1752,12 +1769,21 @@ __device__ __forceinline__ void two_hop_long(const Params<TopoB>& p, BlockAcc& a
           if (incl > (unsigned)budget) incl = (unsigned)budget;
         }
       }
-      unsigned prev = __shfl_up_sync(0xffffffffu, incl, 1);
-      if (lane == 0) prev = 0;
-      const int share = (int)(incl - prev);
+      unsigned before = __shfl_up_sync(0xffffffffu, incl, 1);
+      if (lane == 0) before = 0;
       int got = 0;
-      if (share > 0) got = route_to_sink(p, a, y == p.t ? -1 : yt, share, cf);
-      if (got > 0) pushes += y == p.t ? 1 : 2;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        unsigned upto = before + (room[k] > 0 ? (unsigned)room[k] : 0u);
+        if (upto > (unsigned)budget) upto = (unsigned)budget;
+        const int share = (int)(upto - before);
+        before = upto;
+        if (share > 0) {
+          const int g1 = route_to_sink(p, a0 + 4 * lane + k, y[k] == p.t ? -1 : yt[k], share, cf[k]);
+          if (g1 > 0) pushes += y[k] == p.t ? 1 : 2;
+          got += g1;
+        }
+      }
       int tot = got;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
