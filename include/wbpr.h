@@ -110,7 +110,7 @@ typedef struct wbpr_tuning {
                          /* same maximum flow, fewer rounds); -1 = off            */
   int32_t bfs_alpha;     /* a global relabel's BFS turns bottom-up when the        */
                          /* frontier's arcs x this exceed the unvisited arcs      */
-                         /* (0 = 14)                                              */
+                         /* (0 = 14; 4 in the matching kernel)                    */
   int32_t gr_plateau;    /* also relabel globally when the active set shrank by   */
                          /* less than 10% over this many rounds, 1..8 (0 or -1 =  */
                          /* never, the default)                                   */
