@@ -28,22 +28,22 @@
 // reach t circle, their labels climbing two a round); the unmatched left
 // vertices it reaches form the next active set, the rest are retired.
 //
-// At the end the matching is written into the BCSR16 residuals (three arc
-// pairs per matched edge; the host then has the next solve rewrite every
-// residual, one streaming pass, cheaper than restoring three scattered pairs
-// per matched edge from the undo log), excess(t) is the
-// matching's size, every other excess is 0 (the residual graph of a maximum
-// flow), and the right vertices' labels are written out from their words.
-// A left vertex's label is kept as it goes: 1 + its least neighbour label at
-// its last push, k + 1 when a global relabel reached it at level k, n when it
-// was found unable to reach t -- valid throughout, as right labels only rise
-// and a push raises exactly the label of the vertex pushed to.  A label of n
-// or more therefore proves a vertex dead for the rest of the solve (the set
-// that cannot reach t is closed under pushes): global relabels mark such
-// vertices n + 1 and never scan them again.  This
-// specialises the general solver (maxflow-cuda/src/push_relabel_kernel.cu:
-// 400-537 and maxflow-cuda/src/global_relabel.cu:4-178 of the reference) to
-// the bipartite inputs of the WBPR paper's matching experiments.
+// At the end the matching is written into the BCSR16 residuals: three arc
+// pairs per matched edge (the host then has the next solve rewrite every
+// residual in one streaming pass, cheaper than restoring three scattered
+// pairs per matched edge from the undo log).  excess(t) is the matching's
+// size, every other excess is 0 (the residual graph of a maximum flow), and
+// the right vertices' labels are written out from their words.  A left
+// vertex's label is kept as it goes: 1 + its least neighbour label at its
+// last push, k + 1 when a global relabel reached it at level k, n when it was
+// found unable to reach t -- valid throughout, as right labels only rise and
+// a push raises exactly the label of the vertex pushed to.  A label of n or
+// more therefore proves a vertex dead for the rest of the solve (the set that
+// cannot reach t is closed under pushes): global relabels mark such vertices
+// n + 1 and never scan them again.  This specialises the general solver
+// (maxflow-cuda/src/push_relabel_kernel.cu:400-537 and
+// maxflow-cuda/src/global_relabel.cu:4-178 of the reference) to the
+// bipartite inputs of the WBPR paper's matching experiments.
 #include "match.h"
 
 namespace wbpr_dev {
