@@ -105,7 +105,7 @@ typedef struct wbpr_tuning {
                          /* > 2^22, else never; -1 = never)                       */
   int64_t barrier_timeout_ns; /* a grid-barrier wait gives up after this long and */
                          /* the solve returns WBPR_ERR_TIMEOUT (0 = 10 s)         */
-  int32_t greedy;        /* BCSR solves with one sink: 0 = route excess along      */
+  int32_t greedy;        /* solves with one sink: 0 = route excess along           */
                          /* x->t and x->y->t paths right after the preflow (the   */
                          /* same maximum flow, fewer rounds); -1 = off            */
   int32_t bfs_alpha;     /* a global relabel's BFS turns bottom-up when the        */

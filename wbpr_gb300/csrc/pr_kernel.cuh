@@ -246,6 +246,13 @@ struct TopoB {  // BCSR16: row[n+1], arc {dst, cf}, arx {rev, cap}
     a = (int)chk(bd, a, bd.na);
     return &arc[chk(bd, __ldg(&arx[a].x), bd.na)].y;
   }
+  // forward arc a of a row (segment 0): its residual word, its twin's, and
+  // its capacity (greedy routing)
+  __device__ __forceinline__ int* resid(int a) const { return &arc[chk(bd, a, bd.na)].y; }
+  __device__ __forceinline__ int* twin_resid(int a) const {
+    return &arc[chk(bd, __ldg(&arx[chk(bd, a, bd.na)].x), bd.na)].y;
+  }
+  __device__ __forceinline__ int cap_of(int a) const { return __ldg(&arx[chk(bd, a, bd.na)].y); }
 };
 
 struct TopoR {  // RCSR: forward {dst, cf_f} + cf_b, reverse {tail, forward id}
@@ -304,6 +311,13 @@ struct TopoR {  // RCSR: forward {dst, cf_f} + cf_b, reverse {tail, forward id}
     return k == 0 ? fcb + a : &farc[chk(bd, __ldg(&rarc[a].y), bd.na)].y;
   }
   __device__ __forceinline__ void log_push(int) const {}
+  __device__ __forceinline__ int* resid(int a) const { return &farc[chk(bd, a, bd.na)].y; }
+  __device__ __forceinline__ int* twin_resid(int a) const { return fcb + chk(bd, a, bd.na); }
+  // residual + flow: the capacity (no capacity array on the device side)
+  __device__ __forceinline__ int cap_of(int a) const {
+    a = (int)chk(bd, a, bd.na);
+    return __ldcg(&farc[a].y) + __ldcg(fcb + a);
+  }
 };
 
 template <class Topo>
@@ -1573,7 +1587,7 @@ constexpr int kGreedyBatch = 8;                //   eight in flight; the rest by
 
 template <class Topo>
 __device__ __forceinline__ bool greedy_applies(const Params<Topo>& p) {
-  return Topo::kSeg == 1 && p.greedy && !p.term && p.t >= 0;
+  return p.greedy && !p.term && p.t >= 0;
 }
 
 // Take up to `want` from the residual word *r (0 if it holds none); `hint`
@@ -1590,8 +1604,18 @@ __device__ __forceinline__ int claim_residual(int* r, int want, int hint = -1) {
   return 0;
 }
 
-template <class Topo>
-__device__ __forceinline__ void two_hop_arcs(const Params<Topo>&) {}
+// The y->t arc of every vertex y into esnap[y].  RCSR: t's reverse entries
+// are {y, forward id of y->t}.
+__device__ __forceinline__ void two_hop_arcs(const Params<TopoR>& p) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+  int b, e;
+  p.g.seg(p.t, 1, b, e);
+  for (int a = b + gt; a < e; a += gs) {
+    const int2 r = __ldg(p.g.rarc + a);  // {tail y, forward arc y->t}
+    if (r.x != p.s && p.g.cap_of(r.y) > 0) p.esnap[r.x] = r.y;
+  }
+}
+// BCSR16: t's records that are twins of arcs into t.
 __device__ __forceinline__ void two_hop_arcs(const Params<TopoB>& p) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   int b, e;
@@ -1609,19 +1633,20 @@ __device__ __forceinline__ void two_hop_arcs(const Params<TopoB>& p) {
 // (y->t), or straight along a when y is t (yt < 0).  Each residual is taken
 // by compare-and-swap; what y->t cannot take goes back to x->y.  Returns
 // the amount that reached t.
-__device__ __forceinline__ int route_to_sink(const Params<TopoB>& p, int a, int yt, int want, int cf_hint) {
-  int* ra = &p.g.arc[a].y;
+template <class Topo>
+__device__ __forceinline__ int route_to_sink(const Params<Topo>& p, int a, int yt, int want, int cf_hint) {
+  int* ra = p.g.resid(a);
   const int got1 = claim_residual(ra, want, cf_hint);
   if (got1 <= 0) return 0;
   int got = got1;
   if (yt >= 0) {
-    got = claim_residual(&p.g.arc[yt].y, got1);
+    got = claim_residual(p.g.resid(yt), got1);
     if (got < got1) atomicAdd(ra, got1 - got);  // hand back what y->t could not take
     if (got <= 0) return 0;
-    atomicAdd(&p.g.arc[__ldg(&p.g.arx[yt].x)].y, got);
+    atomicAdd(p.g.twin_resid(yt), got);
     p.g.log_push(yt);
   }
-  atomicAdd(&p.g.arc[__ldg(&p.g.arx[a].x)].y, got);
+  atomicAdd(p.g.twin_resid(a), got);
   p.g.log_push(a);
   return got;
 }
@@ -1630,22 +1655,19 @@ __device__ __forceinline__ int route_to_sink(const Params<TopoB>& p, int a, int 
 // Only s's own arcs carried preflow (a twin in s's row is the reverse of an
 // arc into s, with capacity 0), and a fresh solve's preflow pushed each one's
 // whole capacity.  Returns the budget, 0 if the arc is no walker.
-__device__ __forceinline__ int walker_of(const Params<TopoB>& p, int sa, int& x) {
-  const int cap = __ldg(&p.g.arx[sa].y);
+template <class Topo>
+__device__ __forceinline__ int walker_of(const Params<Topo>& p, int sa, int& x) {
+  const int cap = p.g.cap_of(sa);
   x = p.g.head(0, sa);
   if (cap <= 0 || x == p.t || x == p.s) return 0;
   return cap;
 }
 
-template <class Topo>
-__device__ __forceinline__ void two_hop_short(const Params<Topo>&, BlockAcc&) {}
-template <class Topo>
-__device__ __forceinline__ void two_hop_long(const Params<Topo>&, BlockAcc&) {}
-
 // Stage 1: a thread per walker over the first kGreedyShort arcs of x's row,
 // eight in flight.  A walker with excess and arcs left joins the list of long
 // walkers (fr[1]: its arc of s, fr[2]: its excess left).
-__device__ __forceinline__ void two_hop_short(const Params<TopoB>& p, BlockAcc& acc) {
+template <class Topo>
+__device__ __forceinline__ void two_hop_short(const Params<Topo>& p, BlockAcc& acc) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
   int sb, se;
@@ -1709,7 +1731,8 @@ __device__ __forceinline__ void two_hop_short(const Params<TopoB>& p, BlockAcc& 
 // x's row, 128 at a time.  The lanes' shares of the excess left follow arc
 // order by a saturating prefix sum (each capped at what the arc and its
 // y->t arc hold when read), and all lanes route their shares together.
-__device__ __forceinline__ void two_hop_long(const Params<TopoB>& p, BlockAcc& acc) {
+template <class Topo>
+__device__ __forceinline__ void two_hop_long(const Params<Topo>& p, BlockAcc& acc) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nl = min(ldv(&p.ctl->glong), p.n);
@@ -1749,7 +1772,7 @@ __device__ __forceinline__ void two_hop_long(const Params<TopoB>& p, BlockAcc& a
         room[k] = 0;
         if (cf[k] > 0 && y[k] != p.s && y[k] >= 0) {
           if (y[k] == p.t) room[k] = cf[k];
-          else if (yt[k] >= 0) room[k] = min(cf[k], ldv(&p.g.arc[yt[k]].y));
+          else if (yt[k] >= 0) room[k] = min(cf[k], ldv(p.g.resid(yt[k])));
         }
       }
       // saturating prefix of the rooms in arc order: the lane's own four,
