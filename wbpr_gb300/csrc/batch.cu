@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(512, 2) pr_batch(BatchParams bp) {
         since = 0;
       }
       if (G.leader())
-        bc->stop = (bp.max_rounds > 0 && rounds >= bp.max_rounds) || gtime() - t_start > bp.budget_ns;
+        bc->stop = (bp.max_rounds > 0 && rounds >= bp.max_rounds) || time_past(t_start, bp.budget_ns);
       G.sync();
       const int nL = ldv(&bc->lcount[cur]);
       if (nL == 0) break;

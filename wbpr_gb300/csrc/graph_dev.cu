@@ -100,6 +100,7 @@ cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t stream) {
 struct wbpr_graph {
   int device = 0;
   int sms = 0;
+  int l2_bytes = 0;
   wbpr_layout layout = WBPR_LAYOUT_BCSR;
   int32_t n = 0;
   int64_t m = 0;
@@ -292,6 +293,26 @@ __device__ __forceinline__ TileRows tile_rows(const int* off, int n, long long b
   t.lo = __shfl_sync(0xffffffffu, r, 0);
   t.hi = __shfl_sync(0xffffffffu, r, 1) + 1;
   return t;
+}
+// The same two rows from a table of every tile's first row (db_tile_rows):
+// the last entry of tile t lies before the first of tile t + 1, so its row
+// is at most trow[t + 1].
+__device__ __forceinline__ TileRows tile_rows_tab(const int* trow, long long base) {
+  const long long t = base / kTile;
+  TileRows r;
+  r.lo = __ldg(trow + t);
+  r.hi = __ldg(trow + t + 1) + 1;
+  return r;
+}
+// trow[t] = the row holding entry t * kTile for the tiles t < ntiles of
+// count entries, trow[ntiles] = the row of the last entry: one independent
+// search per tile, instead of a chain of dependent ones at the start of
+// every tile a warp walks
+__global__ void db_tile_rows(const int* off, int n, long long count, int* trow) {
+  const long long ntiles = (count + kTile - 1) / kTile;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t <= ntiles;
+       t += (long long)gridDim.x * blockDim.x)
+    trow[t] = row_search(off, t < ntiles ? t * kTile : count - 1, 0, n);
 }
 #define FOR_TILES(count)                                                                        \
   for (long long base = (blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5)) * kTile; \
@@ -586,14 +607,12 @@ __global__ void db_check_off(const int* off, int n, unsigned long long* bad) {
 // In-degrees from the heads sorted ascending (all checked to lie in [0, n)):
 // the first position p0 of a head's run adds -p0, its last position p1 adds
 // p1 + 1, so indeg[v] ends as the run length.  Two atomics per head, on
-// distinct words, instead of one per arc on a few hot ones.  pos_of (BCSR):
-// the sorted position of every arc, pos_of[sval[p]] = p.
-__global__ void db_indeg_sorted(const int* skey, const int* sval, long long m, int* indeg, int* pos_of) {
+// distinct words, instead of one per arc on a few hot ones.
+__global__ void db_indeg_sorted(const int* skey, long long m, int* indeg) {
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < m; p += (long long)gridDim.x * blockDim.x) {
     const int v = skey[p];
     if (p == 0 || skey[p - 1] != v) atomicAdd(indeg + v, -(int)p);
     if (p == m - 1 || skey[p + 1] != v) atomicAdd(indeg + v, (int)p + 1);
-    if (pos_of) pos_of[sval[p]] = (int)p;
   }
 }
 __global__ void db_max(const unsigned long long* incap, int n, unsigned long long* out) {
@@ -665,28 +684,34 @@ __device__ __forceinline__ unsigned digit_peers(int d, bool ok) {
   }
   return peers;
 }
-// n_check > 0 (the first pass): also flag keys outside [0, n_check)
+// n_check > 0 (the first pass): also flag keys outside [0, n_check).  Each
+// warp counts into its own shared histogram (lanes of one warp with equal
+// digits are the only conflicts), summed at the end.
 __global__ void __launch_bounds__(256) db_sort_hist(const int* key, long long m, int shift, int ntiles, int* hist,
                                                     int n_check, unsigned long long* bad) {
-  __shared__ int cnt[256];
+  __shared__ int cnt[8][256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int tile = blockIdx.x;
-  cnt[threadIdx.x] = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) cnt[j][threadIdx.x] = 0;
   __syncthreads();
   const long long base = (long long)tile * kSortTile + (long long)w * kSortRounds * 32;
   bool b = false;
+#pragma unroll 4
   for (int r = 0; r < kSortRounds; ++r) {
     const long long i = base + r * 32 + lane;
-    const bool ok = i < m;
-    const int k = ok ? key[i] : 0;
-    if (n_check > 0 && (k < 0 || k >= n_check)) b = true;
-    const int d = (k >> shift) & 255;
-    const unsigned peers = digit_peers(d, ok);
-    if (ok && lane == __ffs(peers) - 1) atomicAdd(&cnt[d], __popc(peers));
+    if (i < m) {
+      const int k = key[i];
+      if (n_check > 0 && (k < 0 || k >= n_check)) b = true;
+      atomicAdd(&cnt[w][(k >> shift) & 255], 1);
+    }
   }
   if (__any_sync(0xffffffffu, b) && lane == 0) atomicOr(bad, 1ull);
   __syncthreads();
-  hist[(long long)threadIdx.x * ntiles + tile] = cnt[threadIdx.x];
+  int t = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) t += cnt[j][threadIdx.x];
+  hist[(long long)threadIdx.x * ntiles + tile] = t;
 }
 __global__ void __launch_bounds__(256) db_sort_scatter(const int* kin, const int* vin, long long m, int shift,
                                                        int ntiles, const int* hist, int* kout, int* vout) {
@@ -759,15 +784,36 @@ __global__ void __launch_bounds__(256) db_sort_scatter(const int* kin, const int
   }
 }
 
-// forward slots, arc-parallel (tails as in the tile walk above); records
-// {tail, forward slot, capacity} per arc for the twin pass; flags negative
-// capacities
-__global__ void db_fill_fwd(const int* off, const int* inoff, const int* dst, const int* cap, const int* pos_of,
-                            int n, long long m, int2* arc, int2* arx, int4* uf, unsigned long long* bad) {
+// The largest capacity (warp maxima, one atomic a warp).
+__device__ __forceinline__ void warp_cap_max(int c, unsigned long long* out) {
+  const int w = __reduce_max_sync(0xffffffffu, max(c, 0));
+  if ((threadIdx.x & 31) == 0 && w > 0) atomicMax(out, (unsigned long long)w);
+}
+// The largest in-degree, from the scanned in-offsets.
+__global__ void db_indeg_max(const int* inoff, int n, unsigned long long* out) {
+  int mx = 0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    mx = max(mx, inoff[v + 1] - inoff[v]);
+  mx = __reduce_max_sync(0xffffffffu, mx);
+  if ((threadIdx.x & 31) == 0 && mx > 0) atomicMax(out, (unsigned long long)mx);
+}
+// Whether some head's incoming capacities could pass int32: only then are
+// they summed (largest capacity x largest in-degree bounds every sum).
+__device__ __forceinline__ bool incap_needed(const unsigned long long* bound) {
+  return bound[0] * bound[1] > 0x7fffffffull;
+}
+
+// forward slots, arc-parallel (tails as in the tile walk above); the tail of
+// every arc for the twin pass; the largest capacity into bound[0]; flags
+// negative capacities
+__global__ void db_fill_fwd(const int* off, const int* trow, const int* inoff, const int* dst, const int* cap,
+                            const int* pos_of, long long m, int2* arc, int2* arx, int* tail,
+                            unsigned long long* bad, unsigned long long* bound) {
   const int lane = threadIdx.x & 31;
   bool b = false;
+  int cm = 0;
   FOR_TILES(m) {
-    const TileRows tr = tile_rows(off, n, base, m);
+    const TileRows tr = tile_rows_tab(trow, base);
 #pragma unroll 4
     for (int k = 0; k < kTile / 32; ++k) {
       const long long i = base + k * 32 + lane;
@@ -775,14 +821,16 @@ __global__ void db_fill_fwd(const int* off, const int* inoff, const int* dst, co
       const int u = row_search(off, i, tr.lo, tr.hi);
       const int v = dst[i], c = cap ? cap[i] : 1;
       if (c < 0) b = true;
+      cm = max(cm, c);
       const int f = (int)i + __ldg(inoff + u);
       const int r = __ldg(off + v + 1) + pos_of[i];
       arc[f] = make_int2(v, c);
       arx[f] = make_int2(r, c);
-      uf[i] = make_int4(u, f, c, 0);
+      tail[i] = u;
     }
   }
   if (__any_sync(0xffffffffu, b) && lane == 0) atomicOr(bad, 1ull);
+  warp_cap_max(cm, bound);
 }
 // Sum of x over the lanes from this one to the end of its run of equal keys
 // (keys ascending across the warp, so a run is a block of adjacent lanes);
@@ -798,27 +846,56 @@ __device__ __forceinline__ unsigned long long run_suffix_sum(int key, unsigned l
   return x;
 }
 // twin slots in sorted order: the twin of sorted position p is off[v + 1] + p,
-// so consecutive p write consecutive slots; every head also gets the sum of
-// its incoming capacities (one atomic per run of the head within a warp)
-__global__ void db_fill_twin(const int* off, const int* skey, const int* sval, const int4* uf, long long m,
-                             int2* arc, int2* arx, unsigned long long* incap) {
+// so consecutive p write consecutive slots, and the forward slot of arc i
+// from tail u is i + inoff[u]; when the bound asks for it, every head also
+// gets the sum of its incoming capacities (one atomic per run of the head
+// within a warp)
+__global__ void db_fill_twin(const int* off, const int* inoff, const int* skey, const int* sval, const int* tail,
+                             const int* cap, const unsigned long long* bound, long long m, int2* arc, int2* arx,
+                             unsigned long long* incap) {
   const int lane = threadIdx.x & 31;
   const long long gs = (long long)gridDim.x * blockDim.x;
+  const bool sum = incap_needed(bound);
   for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < m; base += gs) {
     const long long p = base + lane;
     int v = -1;
     unsigned long long c = 0;
     if (p < m) {
       v = skey[p];
-      const int4 t = uf[sval[p]];
+      const int i = sval[p];
+      const int u = tail[i];
       const int r = __ldg(off + v + 1) + (int)p;
-      arc[r] = make_int2(t.x, 0);
-      arx[r] = make_int2(t.y, 0);
-      c = t.z > 0 ? (unsigned long long)t.z : 0ull;
+      arc[r] = make_int2(u, 0);
+      arx[r] = make_int2(i + __ldg(inoff + u), 0);
+      if (sum) c = cap ? (unsigned long long)max(cap[i], 0) : 1ull;
     }
-    const unsigned long long sum = run_suffix_sum(v, c);
-    const int vp = __shfl_up_sync(0xffffffffu, v, 1);
-    if (v >= 0 && (lane == 0 || vp != v) && sum) atomicAdd(incap + v, sum);
+    if (sum) {
+      const unsigned long long t = run_suffix_sum(v, c);
+      const int vp = __shfl_up_sync(0xffffffffu, v, 1);
+      if (v >= 0 && (lane == 0 || vp != v) && t) atomicAdd(incap + v, t);
+    }
+  }
+}
+
+// pos_of[sval[p]] = p for the arcs with id in [lo, hi).  A pass over all of
+// sval scatters 4-byte writes over the whole array, and the L2 writes most of
+// its sectors back to DRAM only partly filled; with the ids in a window of
+// half the L2, each sector is complete before it leaves.  The sorted ids are
+// read with an evict-first hint so that they do not push the window out.
+__global__ void db_pos_window(const int* sval, long long m, int lo, int hi, int* pos_of) {
+  const long long gs = (long long)gridDim.x * blockDim.x;
+  const long long m4 = m >> 2;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < m4; q += gs) {
+    const int4 i = __ldcs(reinterpret_cast<const int4*>(sval) + q);
+    const int p = (int)(4 * q);
+    if (i.x >= lo && i.x < hi) pos_of[i.x] = p;
+    if (i.y >= lo && i.y < hi) pos_of[i.y] = p + 1;
+    if (i.z >= lo && i.z < hi) pos_of[i.z] = p + 2;
+    if (i.w >= lo && i.w < hi) pos_of[i.w] = p + 3;
+  }
+  for (long long p = 4 * m4 + blockIdx.x * (long long)blockDim.x + threadIdx.x; p < m; p += gs) {
+    const int i = sval[p];
+    if (i >= lo && i < hi) pos_of[i] = (int)p;
   }
 }
 
@@ -895,18 +972,21 @@ __global__ void db_bch_fill(const int* o1, const int* o2, const int* hcls, int n
 
 // RCSR forward arcs in input order, and the tail of every input arc; flags
 // negative capacities
-__global__ void db_rcsr_fwd(const int* off, const int* dst, const int* cap, int n, long long m, int2* farc,
-                            int* fcap, int* fcb, int* tail, unsigned long long* bad) {
+__global__ void db_rcsr_fwd(const int* off, const int* trow, const int* dst, const int* cap, long long m,
+                            int2* farc, int* fcap, int* fcb, int* tail, unsigned long long* bad,
+                            unsigned long long* bound) {
   const int lane = threadIdx.x & 31;
   bool b = false;
+  int cm = 0;
   FOR_TILES(m) {
-    const TileRows tr = tile_rows(off, n, base, m);
+    const TileRows tr = tile_rows_tab(trow, base);
 #pragma unroll 4
     for (int k = 0; k < kTile / 32; ++k) {
       const long long i = base + k * 32 + lane;
       if (i >= m) break;
       const int c = cap ? cap[i] : 1;
       if (c < 0) b = true;
+      cm = max(cm, c);
       farc[i] = make_int2(dst[i], c);
       fcap[i] = c;
       fcb[i] = 0;
@@ -914,14 +994,16 @@ __global__ void db_rcsr_fwd(const int* off, const int* dst, const int* cap, int 
     }
   }
   if (__any_sync(0xffffffffu, b) && lane == 0) atomicOr(bad, 1ull);
+  warp_cap_max(cm, bound);
 }
 // RCSR reverse entries: position p of the arcs stably sorted by head holds
-// {tail, forward arc id} (the reference's rdestinations / flow_index); every
-// head gets the sum of its incoming capacities as in db_fill_twin
-__global__ void db_rcsr_rev(const int* skey, const int* sval, const int* tail, const int* fcap, long long m,
-                            int2* rarc, unsigned long long* incap) {
+// {tail, forward arc id} (the reference's rdestinations / flow_index); heads
+// get the sum of their incoming capacities as in db_fill_twin
+__global__ void db_rcsr_rev(const int* skey, const int* sval, const int* tail, const int* fcap,
+                            const unsigned long long* bound, long long m, int2* rarc, unsigned long long* incap) {
   const int lane = threadIdx.x & 31;
   const long long gs = (long long)gridDim.x * blockDim.x;
+  const bool sum = incap_needed(bound);
   for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < m; base += gs) {
     const long long p = base + lane;
     int v = -1;
@@ -930,12 +1012,13 @@ __global__ void db_rcsr_rev(const int* skey, const int* sval, const int* tail, c
       v = skey[p];
       const int i = sval[p];
       rarc[p] = make_int2(__ldg(tail + i), i);
-      const int ci = __ldg(fcap + i);
-      c = ci > 0 ? (unsigned long long)ci : 0ull;
+      if (sum) c = (unsigned long long)max(__ldg(fcap + i), 0);
     }
-    const unsigned long long sum = run_suffix_sum(v, c);
-    const int vp = __shfl_up_sync(0xffffffffu, v, 1);
-    if (v >= 0 && (lane == 0 || vp != v) && sum) atomicAdd(incap + v, sum);
+    if (sum) {
+      const unsigned long long t = run_suffix_sum(v, c);
+      const int vp = __shfl_up_sync(0xffffffffu, v, 1);
+      if (v >= 0 && (lane == 0 || vp != v) && t) atomicAdd(incap + v, t);
+    }
   }
 }
 
@@ -1032,7 +1115,8 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   const size_t mv = std::max<size_t>((size_t)m, (size_t)n + 1);
   const size_t nh_max = std::max<size_t>((size_t)ntiles * 256 + 1, (size_t)n + 1);
   slab_size = 256 * 16 + 4 * (size_t)m * (in->capacities ? 2 : 1) + 4 * ((size_t)n + 1) +
-              8 * ((size_t)n + 1) + 64 + 16 * mv + 4 * nh_max + 4 * (size_t)m + 16 * (size_t)m;
+              8 * ((size_t)n + 1) + 64 + 16 * mv + 4 * nh_max + 4 * (size_t)m + (bcsr ? 4 * (size_t)m : 0) +
+              4 * ((size_t)m / kTile + 2);
   if (wbpr::pool_alloc((void**)&slab, slab_size, st) != cudaSuccess) {
     cudaGetLastError();
     slab = nullptr;
@@ -1054,9 +1138,10 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   int* vb[2] = {(int*)talloc(4 * mv), (int*)talloc(4 * mv)};
   int* hist = (int*)talloc(4 * nh_max);
   int* tail = (int*)talloc(4 * (size_t)m);  // BCSR: sorted position of each arc; RCSR: its tail
-  int4* uf = (int4*)talloc(16 * (size_t)m);
+  int* utail = bcsr ? (int*)talloc(4 * (size_t)m) : tail;  // BCSR: the tail of each arc (RCSR keeps it in tail)
+  int* trow = (int*)talloc(4 * ((size_t)m / kTile + 2));
   if (!d_dst || (in->capacities && !d_cap) || !inoff || !incap || !cnt || !kb[0] || !kb[1] || !vb[0] || !vb[1] ||
-      !hist || !tail || !uf) {
+      !hist || !tail || !utail || !trow) {
     cudaGetLastError();
     g_last_error = "device build: out of device memory";
     cleanup();
@@ -1071,6 +1156,10 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   DB(cudaMemsetAsync(cnt, 0, 8 * 8, st));
   db_check_off<<<blocks, 256, 0, st>>>(g->ioff, n, cnt + 6);
   DB(cudaGetLastError());
+  if (m) {
+    db_tile_rows<<<blocks, 256, 0, st>>>(g->ioff, n, m, trow);
+    DB(cudaGetLastError());
+  }
   const int bits = n > 1 ? 32 - __builtin_clz((unsigned)(n - 1)) : 1;
   const int passes = (bits + 7) / 8;
   const int* skey = kb[(passes - 1) & 1];
@@ -1102,10 +1191,20 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
     return WBPR_ERR_INVALID_ARG;
   }
   if (m) {
-    db_indeg_sorted<<<blocks, 256, 0, st>>>(skey, sval, m, inoff, bcsr ? tail : nullptr);
+    db_indeg_sorted<<<blocks, 256, 0, st>>>(skey, m, inoff);
     DB(cudaGetLastError());
+    if (bcsr) {
+      // the sorted position of every arc, one window of arc ids at a time
+      const long long win = std::max<long long>(1 << 20, (long long)g->l2_bytes / 8);
+      for (long long lo = 0; lo < m; lo += win) {
+        db_pos_window<<<blocks, 256, 0, st>>>(sval, m, (int)lo, (int)std::min(m, lo + win), tail);
+        DB(cudaGetLastError());
+      }
+    }
   }
   DBS(device_scan(inoff, (long long)n + 1, st));
+  db_indeg_max<<<blocks, 256, 0, st>>>(inoff, n, cnt + 4);
+  DB(cudaGetLastError());
   if (bcsr) {
     db_row<<<blocks, 256, 0, st>>>(g->ioff, inoff, n, g->row);
     DB(cudaGetLastError());
@@ -1116,11 +1215,14 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   if (m && d_cap) DB(cudaStreamWaitEvent(st, side_done, 0));
   if (m) {
     if (bcsr) {
-      db_fill_fwd<<<blocks, 256, 0, st>>>(g->ioff, inoff, d_dst, d_cap, tail, n, m, g->arc, g->arx, uf, cnt + 6);
-      db_fill_twin<<<blocks, 256, 0, st>>>(g->ioff, skey, sval, uf, m, g->arc, g->arx, incap);
+      db_fill_fwd<<<blocks, 256, 0, st>>>(g->ioff, trow, inoff, d_dst, d_cap, tail, m, g->arc, g->arx, utail,
+                                          cnt + 6, cnt + 3);
+      db_fill_twin<<<blocks, 256, 0, st>>>(g->ioff, inoff, skey, sval, utail, d_cap, cnt + 3, m, g->arc, g->arx,
+                                           incap);
     } else {
-      db_rcsr_fwd<<<blocks, 256, 0, st>>>(g->ioff, d_dst, d_cap, n, m, g->farc, g->fcap, g->fcb, tail, cnt + 6);
-      db_rcsr_rev<<<blocks, 256, 0, st>>>(skey, sval, tail, g->fcap, m, g->rarc, incap);
+      db_rcsr_fwd<<<blocks, 256, 0, st>>>(g->ioff, trow, d_dst, d_cap, m, g->farc, g->fcap, g->fcb, tail, cnt + 6,
+                                          cnt + 3);
+      db_rcsr_rev<<<blocks, 256, 0, st>>>(skey, sval, tail, g->fcap, cnt + 3, m, g->rarc, incap);
     }
     DB(cudaGetLastError());
   }
@@ -1224,6 +1326,7 @@ wbpr_status create_impl(const wbpr_csr* in, wbpr_layout layout, wbpr_graph** out
   } while (0)
   TRYC(cudaGetDevice(&g->device));
   TRYC(cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, g->device));
+  TRYC(cudaDeviceGetAttribute(&g->l2_bytes, cudaDevAttrL2CacheSize, g->device));
   TRYC(cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking));
   g->stream = g->own_stream;
   TRYC(cudaEventCreate(&g->ev0));

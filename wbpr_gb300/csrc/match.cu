@@ -619,7 +619,7 @@ __global__ void __launch_bounds__(256, 4) pr_match(MatchParams p) {
     add_block((long long*)&c->work[rounds % 3], (long long)(acc.scanned + acc.visits - w0));
     TRACE_BLOCK(p, tb);
     if (gt == 0) {
-      if ((p.max_rounds > 0 && rounds + 1 >= p.max_rounds) || gtime() - t_start > p.budget_ns) c->stop = 1;
+      if ((p.max_rounds > 0 && rounds + 1 >= p.max_rounds) || time_past(t_start, p.budget_ns)) c->stop = 1;
       c->gr_ok = 2 * (gtime() - gr_end) >= gr_last;
     }
     if (!grid_sync(c, p.bar_timeout_ns)) break;

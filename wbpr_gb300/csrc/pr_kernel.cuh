@@ -115,6 +115,12 @@ __device__ __forceinline__ unsigned long long gtime() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
+// Whether more than limit ns have passed since t0.  The global timer follows
+// the host clock, which can be stepped: the difference is taken signed, so a
+// step back reads as no time passed instead of as a wrapped-around eternity.
+__device__ __forceinline__ bool time_past(unsigned long long t0, unsigned long long limit) {
+  return (long long)(gtime() - t0) > (long long)limit;
+}
 __device__ __forceinline__ int ldv(const int* p) { return *(const volatile int*)p; }
 
 __device__ __forceinline__ void trace_rec(long long* tr, int cap, int* n, unsigned long long t0, int kind,
@@ -453,9 +459,13 @@ __device__ __forceinline__ bool grid_sync(C* c, unsigned long long timeout_ns) {
       if (((old + add) ^ old) & 0x80000000u) {
         ld_acquire(&c->bar);  // last arrival
       } else {
-        const unsigned long long t0 = gtime();
+        // A wait gives up after timeout_ns and at least timeout_ns / 1024
+        // polls (each takes well over a nanosecond): a forward step of the
+        // timer alone cannot end a wait early.
+        const unsigned long long t0 = gtime(), min_polls = timeout_ns >> 10;
+        unsigned long long polls = 0;
         while (!((ld_acquire(&c->bar) ^ old) & 0x80000000u)) {
-          if (gtime() - t0 > timeout_ns) {
+          if (++polls > min_polls && time_past(t0, timeout_ns)) {
             atomicCAS(&c->err, 0, (int)WBPR_ERR_TIMEOUT);
             break;
           }
@@ -1441,14 +1451,19 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
     c->bu_med[0] = c->bu_med[1] = c->bu_med[2] = 0;
     c->mcount = c->mhcount = 0;
     if (queues) {
-      c->lcount[cur] = 0;
-      c->hcount[cur] = 0;
       c->dpack = 0;
       c->light_next = 0;
       c->heavy_next = 0;
     }
   }
   if (!grid_sync(c, p.bar_timeout_ns)) return false;
+  // The active counts are cleared only now: a relabel that the plateau test
+  // starts was decided on them at the top of the round, and a block may not
+  // have read them yet when global thread 0 enters this function.
+  if (queues && gt == 0) {
+    c->lcount[cur] = 0;
+    c->hcount[cur] = 0;
+  }
   if (root < 0) {  // the sinks form level 0
     for (int base = gt - lane; base < p.n_sinks; base += gs) {
       const int i = base + lane;
@@ -2025,7 +2040,7 @@ __global__ void __launch_bounds__(256, WBPR_PR_MIN_BLOCKS) pr_persistent(const _
     flush_work(acc, c, raw);
     if (gt == 0) {
       round_ns += gtime() - t0;
-      if ((p.max_rounds > 0 && rounds + 1 >= p.max_rounds) || gtime() - t_start > p.budget_ns)
+      if ((p.max_rounds > 0 && rounds + 1 >= p.max_rounds) || time_past(t_start, p.budget_ns))
         c->stop = 1;
       c->gr_ok = 2 * (gtime() - gr_end) >= gr_last;
       // excess(t) is final once the push phase's barrier has passed: every
