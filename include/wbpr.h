@@ -114,7 +114,7 @@ typedef struct wbpr_tuning {
   int32_t gr_plateau;    /* also relabel globally when the active set shrank by   */
                          /* less than 10% over this many rounds, 1..8 (0 or -1 =  */
                          /* never, the default)                                   */
-  int32_t matching;      /* BCSR solves: 0 = a terminal pair whose network is a   */
+  int32_t matching;      /* 0 = a terminal pair whose network is a                */
                          /* unit-capacity bipartite matching network (s -> left,  */
                          /* left -> right, right -> t, every capacity 1, no other */
                          /* arc) is solved by the matching kernel; -1 = always    */

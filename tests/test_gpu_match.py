@@ -1,10 +1,11 @@
 """The matching kernel (wbpr_gb300/csrc/match.cu): unit-capacity bipartite
 networks (s -> left -> right -> t, every capacity 1) are recognised at the
 solve and matched by double-push rounds with alternating-path global
-relabels.  Every flow is compared with the oracle's Dinic value and with the
-general solver on the same handle (matching=-1); the state left behind must
-pass the device certificate with valid labels, give a maximum flow after
-wbpr_complete_flow, and let the next solve on the handle start clean."""
+relabels, on both layouts.  Every flow is compared with the oracle's Dinic
+value and with the general solver on the same handle (matching=-1); the state
+left behind must pass the device certificate with valid labels, give a
+maximum flow after wbpr_complete_flow, and let the next solve on the handle
+start clean."""
 import numpy as np
 import pytest
 
@@ -52,10 +53,11 @@ def cases():
     yield "chain", network(k, k, np.array(chain)[::-1])
 
 
+@pytest.mark.parametrize("layout", ["bcsr", "rcsr"])
 @pytest.mark.parametrize("name,g", list(cases()), ids=lambda x: x if isinstance(x, str) else "")
-def test_matching_kernel_exact(name, g):
+def test_matching_kernel_exact(name, g, layout):
     v = dinic(g)
-    with W.DeviceGraph(g, "bcsr") as d:
+    with W.DeviceGraph(g, layout) as d:
         r = d.solve("vc", g.s, g.t)
         assert r.matching == 1
         assert r.flow == v
@@ -76,8 +78,8 @@ def test_matching_kernel_exact(name, g):
         assert np.all(net[inner] == 0) and net[g.t] == v
         d.complete_flow()
         assert np.array_equal(d.read_state()[2], f)
-        # the general solver on the same handle: the undo log restored the
-        # residuals the matching wrote
+        # the general solver on the same handle starts from the capacities
+        # again (BCSR16: one full rewrite after a matching; RCSR: always)
         r2 = d.solve("vc", g.s, g.t, matching=-1)
         assert r2.matching == 0 and r2.flow == v
         assert d.verify()["ok"]
@@ -125,23 +127,22 @@ def not_matching_networks():
     yield "left_also_right", W.Graph.from_arcs(base.n, np.append(tails, 3), np.append(heads, t), np.append(caps, 1), s, t)
 
 
+@pytest.mark.parametrize("layout", ["bcsr", "rcsr"])
 @pytest.mark.parametrize("name,g", list(not_matching_networks()), ids=lambda x: x if isinstance(x, str) else "")
-def test_other_shapes_take_the_general_solver(name, g):
+def test_other_shapes_take_the_general_solver(name, g, layout):
     v = dinic(g)
-    with W.DeviceGraph(g, "bcsr") as d:
+    with W.DeviceGraph(g, layout) as d:
         r = d.solve("vc", g.s, g.t)
         assert r.matching == 0
         assert r.flow == v
         assert d.verify()["ok"]
 
 
-def test_detection_follows_terminals_layout_and_capacities():
+@pytest.mark.parametrize("layout", ["bcsr", "rcsr"])
+def test_detection_follows_terminals_and_capacities(layout):
     g = W.gen_bipartite(3000, 2000, 2.0, 256, 7)
     v = dinic(g)
-    with W.DeviceGraph(g, "rcsr") as d:  # the RCSR layout keeps the general solver
-        r = d.solve("vc", g.s, g.t)
-        assert r.matching == 0 and r.flow == v
-    with W.DeviceGraph(g, "bcsr") as d:
+    with W.DeviceGraph(g, layout) as d:
         assert d.solve("vc", g.s, g.t).matching == 1
         # other terminals on the same handle (s = 0, left vertices 1..3000):
         # the shape is checked per pair
@@ -161,10 +162,11 @@ def test_detection_follows_terminals_layout_and_capacities():
         assert r.matching == 1 and r.flow == v
 
 
-def test_round_budget_leaves_a_usable_handle():
+@pytest.mark.parametrize("layout", ["bcsr", "rcsr"])
+def test_round_budget_leaves_a_usable_handle(layout):
     g = W.gen_bipartite(20000, 20000, 2.0, 4096, 9)
     v = dinic(g)
-    with W.DeviceGraph(g, "bcsr") as d:
+    with W.DeviceGraph(g, layout) as d:
         with pytest.raises(W.WbprError) as ei:
             d.solve("vc", g.s, g.t, max_rounds=1)
         assert ei.value.status == 3  # WBPR_ERR_NO_CONVERGENCE

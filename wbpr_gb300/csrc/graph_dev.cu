@@ -539,20 +539,38 @@ __global__ void caps_kernel(const int* ioff, const int* row, const int2* arc, in
 // Unit-capacity bipartite shape of (s, t), pass 1: every forward arc of s
 // (capacity 1, head neither s nor t) counts its head into cl, every arc into t
 // (capacity 1, tail neither s nor t; t's reverse slots) counts its tail into cr.
-__global__ void mt_count(const int* row, const int* ioff, const int2* arc, const int2* arx, int s, int t, int* cl,
-                         int* cr, MCtl* mc) {
+// (BCSR16: row/arc/arx; RCSR: frow = ioff, farc, fcap and the reverse entries
+// rrow/rarc {tail, forward arc id}, with row null)
+__global__ void mt_count(const int* row, const int* ioff, const int2* arc, const int2* arx, const int2* farc,
+                         const int* fcap, const int* rrow, const int2* rarc, int s, int t, int* cl, int* cr,
+                         MCtl* mc) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   bool bad = false;
-  const int bs = row[s], fs = ioff[s + 1] - ioff[s];
+  const int fs = ioff[s + 1] - ioff[s];
   for (int i = gt; i < fs; i += gs) {
-    const int x = arc[bs + i].x;
-    if (arx[bs + i].y != 1 || x == s || x == t) bad = true;
+    int x, c;
+    if (row) {
+      x = arc[row[s] + i].x;
+      c = arx[row[s] + i].y;
+    } else {
+      x = farc[ioff[s] + i].x;
+      c = fcap[ioff[s] + i];
+    }
+    if (c != 1 || x == s || x == t) bad = true;
     else atomicAdd(cl + x, 1);
   }
-  const int et = row[t + 1];
-  for (int a = row[t] + (ioff[t + 1] - ioff[t]) + gt; a < et; a += gs) {
-    const int y = arc[a].x;
-    if (arx[arx[a].x].y != 1 || y == s || y == t) bad = true;
+  // the arcs into t: BCSR16 the twins after t's own arcs, RCSR t's reverse entries
+  const int tb = row ? row[t] + (ioff[t + 1] - ioff[t]) : rrow[t], te = row ? row[t + 1] : rrow[t + 1];
+  for (int a = tb + gt; a < te; a += gs) {
+    int y, c;
+    if (row) {
+      y = arc[a].x;
+      c = arx[arx[a].x].y;
+    } else {
+      y = rarc[a].x;
+      c = fcap[rarc[a].y];
+    }
+    if (c != 1 || y == s || y == t) bad = true;
     else atomicAdd(cr + y, 1);
   }
   if (bad) atomicOr(&mc->bad, 1);
@@ -560,8 +578,9 @@ __global__ void mt_count(const int* row, const int* ioff, const int2* arc, const
 // Pass 2, every input arc u -> v: s -> x with x counted once in cl and never
 // in cr; y -> t with y counted once in cr and never in cl; any other arc of
 // capacity 1 from a left vertex (cl 1, cr 0) to a right one (cr 1, cl 0).
-__global__ void mt_check(const int* ioff, const int* row, const int2* arc, const int2* arx, int n, long long m,
-                         int s, int t, const int* cl, const int* cr, MCtl* mc) {
+__global__ void mt_check(const int* ioff, const int* row, const int2* arc, const int2* arx, const int2* farc,
+                         const int* fcap, int n, long long m, int s, int t, const int* cl, const int* cr,
+                         MCtl* mc) {
   const int lane = threadIdx.x & 31;
   bool bad = false;
   FOR_TILES(m) {
@@ -570,8 +589,15 @@ __global__ void mt_check(const int* ioff, const int* row, const int2* arc, const
       const long long i = base + k * 32 + lane;
       if (i >= m) break;
       const int u = row_search(ioff, i, tr.lo, tr.hi);
-      const int a = row[u] + (int)(i - ioff[u]);
-      const int v = arc[a].x, c = arx[a].y;
+      int v, c;
+      if (row) {
+        const int a = row[u] + (int)(i - ioff[u]);
+        v = arc[a].x;
+        c = arx[a].y;
+      } else {
+        v = farc[i].x;
+        c = fcap[i];
+      }
       if (u == s) bad |= cl[v] != 1 || cr[v] != 0;  // capacity and head checked by pass 1
       else if (v == t) bad |= c != 1 || cr[u] != 1 || cl[u] != 0;
       else bad |= c != 1 || cl[u] != 1 || cr[u] != 0 || cr[v] != 1 || cl[v] != 0;
@@ -581,12 +607,13 @@ __global__ void mt_check(const int* ioff, const int* row, const int2* arc, const
 }
 // Pass 3: the left vertices (rows of at most `heavy` forward arcs into lv,
 // longer ones into hv) and the right vertices into rv.
-__global__ void mt_list(const int* row, int n, int heavy, const int* cl, const int* cr, int* lv, int* hv, int* rv,
+// A left vertex's arcs are its input arcs (its one incoming arc is s -> x).
+__global__ void mt_list(const int* ioff, int n, int heavy, const int* cl, const int* cr, int* lv, int* hv, int* rv,
                         MCtl* mc) {
   long long arcs = 0;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
     if (cl[v] == 1) {
-      const int d = row[v + 1] - row[v] - 1;
+      const int d = ioff[v + 1] - ioff[v];
       arcs += d;
       if (d > heavy) append(hv, &mc->nlist[1], v);
       else append(lv, &mc->nlist[0], v);
@@ -1571,7 +1598,7 @@ constexpr int kMatchBfsAlpha = 4;
 // vertex lists stay on the device for the matching kernel.
 wbpr_status match_detect(wbpr_graph* g, int s, int t, bool* ok) {
   *ok = false;
-  if (g->layout != WBPR_LAYOUT_BCSR || g->m == 0 || s == t) return WBPR_OK;
+  if (g->m == 0 || s == t) return WBPR_OK;
   if (g->mt_s == s && g->mt_t == t) {
     *ok = g->mt_ok;
     return WBPR_OK;
@@ -1588,7 +1615,8 @@ wbpr_status match_detect(wbpr_graph* g, int s, int t, bool* ok) {
   g->mt_s = s;
   g->mt_t = t;
   g->mt_ok = false;
-  mt_count<<<g->sms * 4, 256, 0, g->stream>>>(g->row, g->ioff, g->arc, g->arx, s, t, cl, cr, g->mt_ctl);
+  mt_count<<<g->sms * 4, 256, 0, g->stream>>>(g->row, g->ioff, g->arc, g->arx, g->farc, g->fcap, g->rrow, g->rarc,
+                                              s, t, cl, cr, g->mt_ctl);
   CK(cudaGetLastError());
   // most graphs fail on s's or t's arcs already (a capacity other than 1):
   // then the pass over every arc (0.35 ms at 65M arcs) is skipped
@@ -1596,7 +1624,8 @@ wbpr_status match_detect(wbpr_graph* g, int s, int t, bool* ok) {
   CK(cudaMemcpyAsync(&bad, &g->mt_ctl->bad, 4, cudaMemcpyDeviceToHost, g->stream));
   CK(cudaStreamSynchronize(g->stream));
   if (bad) return WBPR_OK;
-  mt_check<<<g->sms * 8, 256, 0, g->stream>>>(g->ioff, g->row, g->arc, g->arx, g->n, g->m, s, t, cl, cr, g->mt_ctl);
+  mt_check<<<g->sms * 8, 256, 0, g->stream>>>(g->ioff, g->row, g->arc, g->arx, g->farc, g->fcap, g->n, g->m, s, t,
+                                              cl, cr, g->mt_ctl);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(&bad, &g->mt_ctl->bad, 4, cudaMemcpyDeviceToHost, g->stream));
   CK(cudaStreamSynchronize(g->stream));
@@ -1606,7 +1635,7 @@ wbpr_status match_detect(wbpr_graph* g, int s, int t, bool* ok) {
       ((st = dalloc(g, &g->mt_mate, n)) || (st = dalloc(g, &g->mt_claim, n)) || (st = dalloc(g, &g->mt_cy, n)) ||
        (st = dalloc(g, &g->mt_lmin, n)) || (st = dalloc(g, &g->mt_lv, n)) || (st = dalloc(g, &g->mt_rv, n))))
     return st;
-  mt_list<<<g->sms * 4, 256, 0, g->stream>>>(g->row, g->n, kMatchHeavy, cl, cr, g->mt_lv, g->lq[0], g->mt_rv,
+  mt_list<<<g->sms * 4, 256, 0, g->stream>>>(g->ioff, g->n, kMatchHeavy, cl, cr, g->mt_lv, g->lq[0], g->mt_rv,
                                             g->mt_ctl);
   CK(cudaGetLastError());
   MCtl hc;
@@ -1631,7 +1660,20 @@ wbpr_status match_detect(wbpr_graph* g, int s, int t, bool* ok) {
 // match_detect accepted; the residuals were restored before it.
 wbpr_status run_match(wbpr_graph* g, const RunCfg& rc, Stats* hs, float* launch_ms) {
   MatchParams p{};
-  topo_of(g, p.g);
+  if (g->layout == WBPR_LAYOUT_BCSR) {
+    p.lrow = p.rrow = g->row;
+    p.lhd = g->arc;
+    p.rhd = g->arc;
+    p.ltrim = p.rskip = 1;
+    p.arx = g->arx;
+    p.ulog_n = g->ulog ? g->ulog_n : nullptr;
+  } else {
+    p.lrow = g->frow;
+    p.lhd = g->farc;
+    p.rrow = g->rrow;
+    p.rhd = g->rarc;
+    p.fcb = g->fcb;
+  }
   p.n = g->n;
   p.s = rc.s;
   p.t = rc.t;

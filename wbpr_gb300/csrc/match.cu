@@ -28,10 +28,11 @@
 // reach t circle, their labels climbing two a round); the unmatched left
 // vertices it reaches form the next active set, the rest are retired.
 //
-// At the end the matching is written into the BCSR16 residuals: three arc
-// pairs per matched edge (the host then has the next solve rewrite every
-// residual in one streaming pass, cheaper than restoring three scattered
-// pairs per matched edge from the undo log).  excess(t) is the matching's
+// At the end the matching is written into the residuals of either layout:
+// three arcs per matched edge (on BCSR16 the host then has the next solve
+// rewrite every residual in one streaming pass, cheaper than restoring three
+// scattered arc pairs per matched edge from the undo log; RCSR rewrites them
+// before every solve anyway).  excess(t) is the matching's
 // size, every other excess is 0 (the residual graph of a maximum flow), and
 // the right vertices' labels are written out from their words.  A left
 // vertex's label is kept as it goes: 1 + its least neighbour label at its
@@ -73,11 +74,18 @@ __device__ __forceinline__ void add_block(long long* dst, long long v) {
   if ((threadIdx.x & 31) == 0 && v) atomicAdd((unsigned long long*)dst, (unsigned long long)v);
 }
 
-// forward arcs of left vertex x: [b, b + d); the row's last slot is the twin
-// of s -> x (x has no other incoming arc)
+// arcs of left vertex x to right vertices: [b, b + d)
 __device__ __forceinline__ int left_row(const MatchParams& p, int x, int& b) {
-  b = __ldg(p.g.row + x);
-  return __ldg(p.g.row + x + 1) - b - 1;
+  b = __ldg(p.lrow + x);
+  return __ldg(p.lrow + x + 1) - b - p.ltrim;
+}
+// arcs of right vertex y from left vertices: [b, e)
+__device__ __forceinline__ void right_row(const MatchParams& p, int y, int& b, int& e) {
+  b = __ldg(p.rrow + y) + p.rskip;
+  e = __ldg(p.rrow + y + 1);
+}
+__device__ __forceinline__ int right_deg(const MatchParams& p, int y) {
+  return __ldg(p.rrow + y + 1) - __ldg(p.rrow + y) - p.rskip;
 }
 
 // queue x for the next round by its row length
@@ -97,7 +105,7 @@ __device__ __forceinline__ int mate_of_left(const MatchParams& p, int x) {
 // false when another claim changed the word first.  `evicted` is y's
 // previous mate (-1: y was free, one more unit into t).
 __device__ __forceinline__ bool take(const MatchParams& p, int x, int a, unsigned long long w, int& evicted) {
-  const int y = __ldg(&p.g.arc[a].x);
+  const int y = __ldg(&p.lhd[a].x);
   const int l = wlab(w);
   if (atomicCAS(p.mate + y, w, mword((unsigned)x, min(l + 2, p.n))) != w) return false;
   p.claim[x] = a;
@@ -122,7 +130,7 @@ __device__ __forceinline__ void discharge_warp(const MatchParams& p, int x, int 
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int k = k0 + j * 32 + lane;
-        y[j] = k < d ? __ldg(&p.g.arc[b + k].x) : -1;
+        y[j] = k < d ? __ldg(&p.lhd[b + k].x) : -1;
       }
       unsigned long long kl = ~0ull, wl = 0;
 #pragma unroll
@@ -183,7 +191,7 @@ __device__ __forceinline__ void discharge_thread(const MatchParams& p, int x, in
     for (int k0 = from; k0 < d && (best >> 32) > (unsigned long long)bound; k0 += 4) {
       int y[4];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) y[j] = k0 + j < d ? __ldg(&p.g.arc[b + k0 + j].x) : -1;
+      for (int j = 0; j < 4; ++j) y[j] = k0 + j < d ? __ldg(&p.lhd[b + k0 + j].x) : -1;
 #pragma unroll
       for (int j = 0; j < 4; ++j)
         if (y[j] >= 0) {
@@ -257,7 +265,7 @@ __device__ void match_round(const MatchParams& p, const int* L, int nL, const in
 #pragma unroll
     for (int q = 0; q < 2; ++q)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) y[q][j] = j < d[q] ? __ldg(&p.g.arc[b[q] + j].x) : -1;
+      for (int j = 0; j < 4; ++j) y[q][j] = j < d[q] ? __ldg(&p.lhd[b[q] + j].x) : -1;
     unsigned long long w[2][4];
 #pragma unroll
     for (int q = 0; q < 2; ++q)
@@ -293,7 +301,7 @@ __device__ __forceinline__ void visit_left(const MatchParams& p, int x, int k, i
   const int y = mate_of_left(p, x);
   if (y >= 0) {
     p.mate[y] = mword((unsigned)x, k + 2);  // y's only residual arc leads to x: reached through x alone
-    fdeg += __ldg(p.g.row + y + 1) - __ldg(p.g.row + y) - 1;
+    fdeg += right_deg(p, y);
     if (list) append(p.fr[(li + 1) & 1], &c->fn[(li + 1) % 3], y);
     else count_one(&c->fn[(li + 1) % 3]);
   } else {
@@ -309,7 +317,7 @@ __device__ __forceinline__ void bu_finish(const MatchParams& p, int x, int b, in
   for (int k0 = 4; k0 < d && !hit; k0 += 4) {
     int y[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) y[j] = k0 + j < d ? __ldg(&p.g.arc[b + k0 + j].x) : -1;
+    for (int j = 0; j < 4; ++j) y[j] = k0 + j < d ? __ldg(&p.lhd[b + k0 + j].x) : -1;
 #pragma unroll
     for (int j = 0; j < 4; ++j)
       if (y[j] >= 0) {
@@ -360,7 +368,7 @@ __device__ bool match_gr(const MatchParams& p, int qb, MAcc& acc, int& levels, i
     p.mate[y] = mword((unsigned)x, x < 0 ? 1 : (wlab(w) >= n ? n + 1 : n));
     if (x < 0) {
       append(p.fr[0], &c->fn[0], y);
-      fd += __ldg(p.g.row + y + 1) - __ldg(p.g.row + y) - 1;
+      fd += right_deg(p, y);
     }
   }
   add_block(&c->fdeg[0], fd);
@@ -407,10 +415,11 @@ __device__ bool match_gr(const MatchParams& p, int qb, MAcc& acc, int& levels, i
         // level is then one arc's dependent loads long)
         for (int i = gt >> 5; i < nlist; i += gs >> 5) {
           const int y = __ldcg(F + i);
-          const int b = __ldg(p.g.row + y) + 1, e = __ldg(p.g.row + y + 1);
+          int b, e;
+          right_row(p, y, b, e);
           if (lane == 0) ++acc.bfs_vertices;
           for (int a = b + lane; a < e; a += 32) {
-            const int x = __ldg(&p.g.arc[a].x);
+            const int x = __ldg(&p.rhd[a].x);
             ++acc.bfs_arcs;
             if (__ldcg(p.lab + x) == n && atomicCAS(p.lab + x, n, k + 1) == n)
               visit_left(p, x, k, li, true, qb, seen, nfd);
@@ -422,8 +431,7 @@ __device__ bool match_gr(const MatchParams& p, int qb, MAcc& acc, int& levels, i
           int b = 0, e = 0;
           if (i < nlist) {
             const int y = __ldcg(F + i);
-            b = __ldg(p.g.row + y) + 1;
-            e = __ldg(p.g.row + y + 1);
+            right_row(p, y, b, e);
             ++acc.bfs_vertices;
           }
           const bool big = e - b > 32;
@@ -431,7 +439,7 @@ __device__ bool match_gr(const MatchParams& p, int qb, MAcc& acc, int& levels, i
             for (int a0 = b; a0 < e; a0 += 4) {
               int x[4];
 #pragma unroll
-              for (int j = 0; j < 4; ++j) x[j] = a0 + j < e ? __ldg(&p.g.arc[a0 + j].x) : -1;
+              for (int j = 0; j < 4; ++j) x[j] = a0 + j < e ? __ldg(&p.rhd[a0 + j].x) : -1;
 #pragma unroll
               for (int j = 0; j < 4; ++j)
                 if (x[j] >= 0) {
@@ -444,7 +452,7 @@ __device__ bool match_gr(const MatchParams& p, int qb, MAcc& acc, int& levels, i
             const int src = __ffs(bm) - 1;
             const int bb = __shfl_sync(0xffffffffu, b, src), ee = __shfl_sync(0xffffffffu, e, src);
             for (int a = bb + lane; a < ee; a += 32) {
-              const int x = __ldg(&p.g.arc[a].x);
+              const int x = __ldg(&p.rhd[a].x);
               ++acc.bfs_arcs;
               if (__ldcg(p.lab + x) == n && atomicCAS(p.lab + x, n, k + 1) == n)
                 visit_left(p, x, k, li, true, qb, seen, nfd);
@@ -469,7 +477,7 @@ __device__ bool match_gr(const MatchParams& p, int qb, MAcc& acc, int& levels, i
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
             const int kk = k0 + j * 32 + lane;
-            y[j] = kk < d ? __ldg(&p.g.arc[b + kk].x) : -1;
+            y[j] = kk < d ? __ldg(&p.lhd[b + kk].x) : -1;
           }
           bool h = false;
 #pragma unroll
@@ -507,7 +515,7 @@ __device__ bool match_gr(const MatchParams& p, int qb, MAcc& acc, int& levels, i
 #pragma unroll
         for (int q = 0; q < 2; ++q)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) y[q][j] = j < d[q] ? __ldg(&p.g.arc[b[q] + j].x) : -1;
+          for (int j = 0; j < 4; ++j) y[q][j] = j < d[q] ? __ldg(&p.lhd[b[q] + j].x) : -1;
         bool hit[2] = {false, false};
 #pragma unroll
         for (int q = 0; q < 2; ++q)
@@ -556,7 +564,10 @@ __global__ void __launch_bounds__(256, 4) pr_match(MatchParams p) {
     p.cy[x] = -1;
     p.lmin[x] = 0;
   }
-  clear_log(p.g, gt);
+  if (p.ulog_n && gt < kLogSlots) {  // BCSR16: the undo log starts empty
+    p.ulog_n[gt * kLogStride] = 0;
+    p.ulog_n[gt * kLogStride + 1] = 0;
+  }
   if (!grid_sync(c, p.bar_timeout_ns)) return;
 
   int rounds = 0, since_gr = 0, grs = 0, levels = 0, bu_levels = 0;
@@ -648,15 +659,28 @@ __global__ void __launch_bounds__(256, 4) pr_match(MatchParams p) {
       p.lab[y] = min(wlab(w), n);
       const int x = wmate(w);
       if (x < 0) continue;
-      const int a = __ldcg(p.claim + x);          // x -> y
-      const int ay = __ldg(p.g.row + y);          // y -> t
-      const int ax = __ldg(p.g.row + x + 1) - 1;  // x -> s, the twin of s -> x
-      p.g.arc[a].y = 0;
-      p.g.arc[__ldg(&p.g.arx[a].x)].y = 1;
-      p.g.arc[ay].y = 0;
-      p.g.arc[__ldg(&p.g.arx[ay].x)].y = 1;
-      p.g.arc[ax].y = 1;
-      p.g.arc[__ldg(&p.g.arx[ax].x)].y = 0;
+      const int a = __ldcg(p.claim + x);  // x -> y
+      const int ay = __ldg(p.lrow + y);   // y -> t, the first arc of y's row
+      if (p.arx) {
+        // BCSR16: each arc and its twin; the twin of s -> x ends x's row
+        const int ax = __ldg(p.lrow + x + 1) - 1;
+        p.lhd[a].y = 0;
+        p.lhd[__ldg(&p.arx[a].x)].y = 1;
+        p.lhd[ay].y = 0;
+        p.lhd[__ldg(&p.arx[ay].x)].y = 1;
+        p.lhd[ax].y = 1;
+        p.lhd[__ldg(&p.arx[ax].x)].y = 0;
+      } else {
+        // RCSR: forward residual 0, reverse residual 1; s -> x is the
+        // forward arc of x's one reverse entry
+        const int sx = __ldg(&p.rhd[__ldg(p.rrow + x)].y);
+        p.lhd[a].y = 0;
+        p.fcb[a] = 1;
+        p.lhd[ay].y = 0;
+        p.fcb[ay] = 1;
+        p.lhd[sx].y = 0;
+        p.fcb[sx] = 1;
+      }
       ++cnt;
     }
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);

@@ -36,7 +36,24 @@ struct MCtl {
 };
 
 struct MatchParams {
-  TopoB g;         // BCSR16 residual rows (and the undo log)
+  // The rows as either layout holds them, heads in .x: left vertex x's arcs
+  // to right vertices are lhd[lrow[x], lrow[x + 1] - ltrim), right vertex y's
+  // arcs from left vertices are rhd[rrow[y] + rskip, rrow[y + 1]).  BCSR16:
+  // both are the residual rows (row, arc), a left row ends with the twin of
+  // s -> x (ltrim 1) and a right row starts with y -> t (rskip 1).  RCSR: the
+  // forward rows (frow, farc) and the reverse entries (rrow, rarc {tail,
+  // forward arc id}), ltrim = rskip = 0.
+  const int* lrow;
+  int2* lhd;
+  int ltrim;
+  const int* rrow;
+  const int2* rhd;
+  int rskip;
+  // where the matching is written back: BCSR16 twins (arx, fcb null) or RCSR
+  // reverse residuals (fcb, arx null)
+  const int2* arx;
+  int* fcb;
+  int* ulog_n;  // BCSR16 undo-log counters, cleared at the start (null for RCSR)
   int n, s, t;
   int nl, nl_light, nr;
   const int* lv;   // left vertices: rows of at most heavy_deg arcs first, then the longer ones
