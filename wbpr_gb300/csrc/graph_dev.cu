@@ -700,6 +700,7 @@ __global__ void db_scan_add(int* data, long long count, const int* sums) {
 // in shared memory (digit, then input order), then writes each digit's run
 // to its global place, so consecutive threads write consecutive slots.
 constexpr int kSortRounds = 16;
+constexpr int kHeadChunks = 4;  // pieces the heads are copied in
 constexpr int kSortTile = 8 * kSortRounds * 32;  // 4096 arcs
 __device__ __forceinline__ unsigned digit_peers(int d, bool ok) {
   unsigned peers = __ballot_sync(0xffffffffu, ok);
@@ -713,12 +714,13 @@ __device__ __forceinline__ unsigned digit_peers(int d, bool ok) {
 }
 // n_check > 0 (the first pass): also flag keys outside [0, n_check).  Each
 // warp counts into its own shared histogram (lanes of one warp with equal
-// digits are the only conflicts), summed at the end.
-__global__ void __launch_bounds__(256) db_sort_hist(const int* key, long long m, int shift, int ntiles, int* hist,
-                                                    int n_check, unsigned long long* bad) {
+// digits are the only conflicts), summed at the end.  Block b counts tile
+// tile0 + b.
+__global__ void __launch_bounds__(256) db_sort_hist(const int* key, long long m, int shift, int ntiles, int tile0,
+                                                    int* hist, int n_check, unsigned long long* bad) {
   __shared__ int cnt[8][256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int tile = blockIdx.x;
+  const int tile = blockIdx.x + tile0;
 #pragma unroll
   for (int j = 0; j < 8; ++j) cnt[j][threadIdx.x] = 0;
   __syncthreads();
@@ -1102,11 +1104,17 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
   size_t slab_at = 0, slab_size = 0;
   cudaStream_t side = nullptr;
   cudaEvent_t side_done = nullptr;
+  cudaEvent_t head_done[kHeadChunks] = {};
   auto cleanup = [&]() {
     cudaStreamSynchronize(st);
     if (side) cudaStreamSynchronize(side);
     if (slab) cudaFreeAsync(slab, st);
     if (side_done) cudaEventDestroy(side_done);
+    for (cudaEvent_t& e : head_done)
+      if (e) {
+        cudaEventDestroy(e);
+        e = nullptr;
+      }
     if (side) cudaStreamDestroy(side);
     slab = nullptr;
     side = nullptr;
@@ -1150,7 +1158,9 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
     g_last_error = "device build: out of device memory";
     return WBPR_ERR_CUDA;
   }
-  if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess ||
+  bool ev_ok = true;
+  for (cudaEvent_t& e : head_done) ev_ok = ev_ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  if (!ev_ok || cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&side_done, cudaEventDisableTiming) != cudaSuccess) {
     g_last_error = std::string("device build: ") + cudaGetErrorString(cudaGetLastError());
     cleanup();
@@ -1175,9 +1185,21 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
     return WBPR_ERR_CUDA;
   }
   // Heads first: the sort needs only them, so it runs while the capacities
-  // are copied on a second stream.  The in-degrees come from the sorted heads.
+  // are copied on a second stream.  The heads come in kHeadChunks pieces on
+  // that stream, and the first pass's histogram of each piece runs while the
+  // next one is copied.  The in-degrees come from the sorted heads.
   DB(cudaMemcpyAsync(g->ioff, in->offsets, 4 * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
-  if (m) DB(cudaMemcpyAsync(d_dst, in->destinations, 4 * (size_t)m, cudaMemcpyHostToDevice, st));
+  // the side stream uses the pool's slab only after its allocation on st
+  DB(cudaEventRecord(side_done, st));
+  DB(cudaStreamWaitEvent(side, side_done, 0));
+  const int nchunks = (int)std::min<long long>(kHeadChunks, ntiles);
+  const long long tpc = nchunks ? (ntiles + nchunks - 1) / nchunks : 0;  // tiles per piece
+  for (int k = 0; k < nchunks; ++k) {
+    const long long a0 = k * tpc * kSortTile, a1 = std::min<long long>(m, (k + 1) * tpc * kSortTile);
+    if (a1 <= a0) break;
+    DB(cudaMemcpyAsync(d_dst + a0, in->destinations + a0, 4 * (size_t)(a1 - a0), cudaMemcpyHostToDevice, side));
+    DB(cudaEventRecord(head_done[k], side));
+  }
   DB(cudaMemsetAsync(inoff, 0, 4 * ((size_t)n + 1), st));
   DB(cudaMemsetAsync(incap, 0, 8 * ((size_t)n + 1), st));
   DB(cudaMemsetAsync(cnt, 0, 8 * 8, st));
@@ -1196,8 +1218,18 @@ wbpr_status build_device(wbpr_graph* g, const wbpr_csr* in) {
     for (int p = 0; p < passes; ++p) {
       const int* kin = p ? kb[(p - 1) & 1] : d_dst;
       const int* vin = p ? vb[(p - 1) & 1] : nullptr;
-      db_sort_hist<<<sblocks, 256, 0, st>>>(kin, m, 8 * p, ntiles, hist, p == 0 ? n : 0, cnt + 6);
-      DB(cudaGetLastError());
+      if (p == 0) {
+        for (int k = 0; k < nchunks; ++k) {
+          const long long t0 = k * tpc, t1 = std::min<long long>(ntiles, t0 + tpc);
+          if (t1 <= t0) break;
+          DB(cudaStreamWaitEvent(st, head_done[k], 0));
+          db_sort_hist<<<(unsigned)(t1 - t0), 256, 0, st>>>(kin, m, 0, ntiles, (int)t0, hist, n, cnt + 6);
+          DB(cudaGetLastError());
+        }
+      } else {
+        db_sort_hist<<<sblocks, 256, 0, st>>>(kin, m, 8 * p, ntiles, 0, hist, 0, cnt + 6);
+        DB(cudaGetLastError());
+      }
       DBS(device_scan(hist, (long long)ntiles * 256, st));
       db_sort_scatter<<<sblocks, 256, 0, st>>>(kin, vin, m, 8 * p, ntiles, hist, kb[p & 1], vb[p & 1]);
       DB(cudaGetLastError());
