@@ -44,7 +44,10 @@ constexpr int kNone = -1;
 constexpr int kBig = 0x7fffffff;
 constexpr int kMaxPlateau = 8;
 constexpr int kBfsAlpha = 14;  // default: top-down -> bottom-up when frontier arcs * alpha > unvisited arcs
-constexpr int kBfsBeta = 24;   // bottom-up -> top-down when frontier * beta < n
+#ifndef WBPR_BFS_BETA
+#define WBPR_BFS_BETA 24
+#endif
+constexpr int kBfsBeta = WBPR_BFS_BETA;  // bottom-up -> top-down when frontier * beta < n
 constexpr int kLightDeg = 32;  // BFS: rows up to this length scanned by one thread
 constexpr int kHeavyDeg = 2048;  // BFS: rows longer than this scanned by a whole block
 constexpr int kChunk = 2048;     // BFS: heavy rows are cut into static chunks of this many arcs
@@ -1169,7 +1172,10 @@ __device__ void bfs_bottom_up(const Params<Topo>& p, int level, BlockAcc& acc) {
   unsigned long long arcs = 0, verts = 0, found = 0, fdeg = 0;
   // short rows (<= kLightDeg): a thread each; kBuRows rows advance together,
   // kBuArcs arcs of each in flight per step
-  constexpr int kBuRows = 4, kBuArcs = 4;
+#ifndef WBPR_BU_ROWS
+#define WBPR_BU_ROWS 4
+#endif
+  constexpr int kBuRows = WBPR_BU_ROWS, kBuArcs = 4;
   for (int i0 = gt; i0 < p.n_light; i0 += kBuRows * gs) {
     int xs[kBuRows];
     bool todo[kBuRows];
@@ -1597,8 +1603,11 @@ __device__ bool bfs(const Params<Topo>& p, int root, bool queues, int cur, Block
 #define WBPR_GREEDY_ARCS 1024
 #endif
 constexpr int kGreedyArcs = WBPR_GREEDY_ARCS;  // arcs of x's row a walker tries
-constexpr int kGreedyShort = 32;               // of them by the walker's own thread,
-constexpr int kGreedyBatch = 8;                //   eight in flight; the rest by a warp
+#ifndef WBPR_GREEDY_SHORT
+#define WBPR_GREEDY_SHORT 32
+#endif
+constexpr int kGreedyShort = WBPR_GREEDY_SHORT;  // of them by the walker's own thread,
+constexpr int kGreedyBatch = 8;                  //   eight in flight; the rest by a warp
 
 template <class Topo>
 __device__ __forceinline__ bool greedy_applies(const Params<Topo>& p) {
