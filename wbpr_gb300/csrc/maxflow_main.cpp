@@ -78,8 +78,7 @@ int main(int argc, char** argv) {
   const char* out_path = nullptr;
   const char* cache_path = nullptr;
   // BCSR16 by default: the same results as RCSR (the reference's only layout
-  // in maxflow-cuda) and the fastest path, the one unit-capacity bipartite
-  // networks take to the matching kernel
+  // in maxflow-cuda) and the general solver's fastest path
   wbpr_layout layout = WBPR_LAYOUT_BCSR;
   wbpr_host_csr* g = nullptr;
   int ch;
