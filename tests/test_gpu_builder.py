@@ -5,7 +5,7 @@ maxflow-bcsr/src/graph.cpp:317-360), RCSR reverse offsets, reverse heads and
 flow_index (wbpr_build_rcsr, maxflow-cuda/src/graph.cpp:317-402) -- for every
 shape the sort and the length classes see: empty rows, isolated vertices,
 parallel arcs, rows longer than the push chunk, heads that need one to four
-radix passes."""
+radix passes, more arcs than one window of the sorted-position pass."""
 import numpy as np
 import pytest
 
@@ -53,6 +53,13 @@ def test_random_shapes(n, m):
 def test_long_rows_and_hot_vertex():
     # rows far longer than the 2048-arc push chunk, in and out of one vertex
     same_as_host(random_graph(5000, 120000, 3, hot=17))
+
+
+def test_sorted_positions_in_several_windows():
+    # more arcs than one window of arc ids (half the L2 in 4-byte entries,
+    # about 16M on GB300): the sorted positions are written in two or more
+    # passes, the in-capacity sums are skipped below the int32 bound
+    same_as_host(W.gen_rmat(21, 16, seed=3))
 
 
 def test_four_radix_passes():
