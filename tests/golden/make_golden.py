@@ -32,9 +32,9 @@ sys.path.insert(0, ROOT)
 
 import oracle  # noqa: E402
 import wbpr_gb300 as W  # noqa: E402
-from oracle.build_oracle import build_ref  # noqa: E402
+from oracle.build_oracle import REF_TREE, build_ref  # noqa: E402
 
-REF = "/root/reference"
+REF = REF_TREE  # WBPR_REFERENCE, else the default tree of the recipe
 FIXTURES = [
     ("ref_test_DIMACS", "maxflow-serial/input/test_DIMACS.txt", 2, None, None),
     ("ref_serial_test_graph", "maxflow-serial/test_graph.txt", 0, 0, 4),
