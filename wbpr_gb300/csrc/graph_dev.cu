@@ -635,8 +635,21 @@ __global__ void db_check_off(const int* off, int n, unsigned long long* bad) {
 // the first position p0 of a head's run adds -p0, its last position p1 adds
 // p1 + 1, so indeg[v] ends as the run length.  Two atomics per head, on
 // distinct words, instead of one per arc on a few hot ones.
+// Four positions per thread from one 16-byte load (and the two neighbours).
 __global__ void db_indeg_sorted(const int* skey, long long m, int* indeg) {
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < m; p += (long long)gridDim.x * blockDim.x) {
+  const long long gs = (long long)gridDim.x * blockDim.x, m4 = m >> 2;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < m4; q += gs) {
+    const int4 k = __ldcs(reinterpret_cast<const int4*>(skey) + q);
+    const long long p = 4 * q;
+    // heads lie in [0, n): -1 marks the ends of the array
+    const int ks[6] = {p > 0 ? __ldg(skey + p - 1) : -1, k.x, k.y, k.z, k.w, p + 4 < m ? __ldg(skey + p + 4) : -1};
+#pragma unroll
+    for (int j = 1; j <= 4; ++j) {
+      if (ks[j - 1] != ks[j]) atomicAdd(indeg + ks[j], -(int)(p + j - 1));
+      if (ks[j + 1] != ks[j]) atomicAdd(indeg + ks[j], (int)(p + j));
+    }
+  }
+  for (long long p = 4 * m4 + blockIdx.x * (long long)blockDim.x + threadIdx.x; p < m; p += gs) {
     const int v = skey[p];
     if (p == 0 || skey[p - 1] != v) atomicAdd(indeg + v, -(int)p);
     if (p == m - 1 || skey[p + 1] != v) atomicAdd(indeg + v, (int)p + 1);
